@@ -1,0 +1,430 @@
+"""Benchmark of the GB300 sparse Krylov engine.
+
+Headline (one "step" = one full solve): plain FP64 pipelined CG
+(linalg::solve(A, b, cg_tag(1e-10, 10000)), the reference's no-preconditioner
+path) on the 3D 7-point Laplacian 128^3 = 2,097,152 rows / 14,581,760 nnz,
+b ~ U[-1,1] (seed 1), to relative residual 1e-10; value = seconds per solve
+with the matrix and b resident in HBM.  e2e = the same solve through the
+public API starting from pinned host CSR arrays and b (H2D copies, matrix
+creation, solve, D2H of x inside the timed region).
+
+Secondary fields: SpMV GB/s per format on the 128^3 Laplacian and the 4M-row
+lognormal matrix, BiCGStab and GMRES(30) on the lognormal matrix, the 192^3
+variable-coefficient diffusion solved by FP32-inner/FP64-refined CG against
+the plain FP64 Jacobi-PCG path, and the reference's CPU-runnable 256^2 case.
+
+--impl reference times the reference's own CPU algorithm (the C restatement
+in oracle/, OpenMP on all host cores) on the headline workload.
+Multi-GPU: the path does not shard, so N ranks run N independent replicas.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "viennacl-dev_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import vclgb_gen as gen  # noqa: E402
+
+METRIC = "CG solve s @1e-10 FP64 resid: mixed/batched vs plain FP64 on GPU; SpMV GB/s"
+WORKLOAD = "3D 7-point Laplacian 128^3 (2,097,152 rows, 14,581,760 nnz), FP64 CSR, pipelined CG to 1e-10"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def spmv_bytes(n, nnz, sv=8, beta=False):
+    """Algorithmic bytes of one SpMV (format independent): values+indices once,
+    row_ptr once, x read once, y written once (+ read when beta != 0)."""
+    return nnz * (sv + 4) + (n + 1) * 4 + n * sv + n * sv + (n * sv if beta else 0)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(backend):
+    import torch.distributed as dist
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(value, ws):
+    """Max of a float over ranks (identity on one rank)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def time_events(fn, reps):
+    """Average device time of fn() over reps, CUDA events, synchronised both sides."""
+    import torch
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / 1e3 / reps
+
+
+def spmv_gbs(V, M, n, nnz, reps, x, y):
+    t = time_events(lambda: V.prod(M, x, y=y), reps)
+    b = spmv_bytes(n, nnz)
+    return t, b / t / 1e9
+
+
+def run_ours(args):
+    import torch
+    import vclgb as V
+    ws, rank, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    peak, peak_kind = peaks()
+    out = {"metric": METRIC, "unit": "s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, vclgb_gen.py)"}
+
+    # ---- headline workload -------------------------------------------------
+    rp, ci, v = gen.laplace3d(128)
+    n, nnz = len(rp) - 1, int(rp[-1])
+    b = gen.rhs_uniform(n, 1)
+    A = V.compressed_matrix(rp, ci, v)
+    bd = torch.tensor(b, device="cuda")
+    xd = torch.empty(n, dtype=torch.float64, device="cuda")
+    tol, maxit = 1e-10, 10000
+
+    def solve_once():
+        tag = V.cg_tag(tol, maxit)
+        V.solve(A, bd, tag, None, x=xd)
+        return tag
+
+    for _ in range(max(args.warmup, 3)):
+        tag = solve_once()
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = A.be.launches()
+    clk = ClockSampler(local)
+    clk.start()
+    tags = []
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.steps):
+        tags.append(solve_once())
+    e.record()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier(ws)
+    t_solve = s.elapsed_time(e) / 1e3 / args.steps
+    t_solve = max_over_ranks(t_solve, ws)
+    launches = A.be.launches() - l0
+    iters = tags[-1].iters()
+    import oracle
+    rel = oracle.rel_residual(rp, ci, v, xd.cpu().numpy(), b)
+    out["value"] = t_solve
+    out["ms_per_step"] = t_solve * 1e3
+    out["config"] = {"workload": WORKLOAD, "solver": "pipelined CG (cg.hpp:128-187), no preconditioner",
+                     "tol": tol, "rhs": "U[-1,1] seed 1", "iterations": iters,
+                     "true_rel_residual": rel, "solver_error_estimate": tags[-1].error(),
+                     "l2": "working set (250 MB) larger than the 126 MB L2; no flush",
+                     "parallelism": "replicas" if ws > 1 else "single GPU"}
+    out["gpu_launches"] = int(launches)
+    out["clocks"] = clocks
+
+    # ---- roofline: the dominant kernel is the CSR SpMV ----------------------
+    xs = torch.tensor(gen.rhs_uniform(n, 11), device="cuda")
+    ys = torch.empty(n, dtype=torch.float64, device="cuda")
+    for _ in range(5):
+        V.prod(A, xs, y=ys)
+    t_spmv, gbs = spmv_gbs(V, A, n, nnz, 50, xs, ys)
+    out["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                       "frac": gbs / peak, "peak_kind": peak_kind,
+                       "kernel": "csr_adaptive_kernel<double> (8 lanes/row bin, 128^3 Laplacian)",
+                       "algorithmic_bytes_per_launch": spmv_bytes(n, nnz),
+                       "avg_launch_us": t_spmv * 1e6,
+                       "traffic": args.traffic}
+
+    # ---- e2e from host buffers ----------------------------------------------
+    h_rp = torch.from_numpy(rp.view(np.int32)).pin_memory()
+    h_ci = torch.from_numpy(ci.view(np.int32)).pin_memory()
+    h_v = torch.from_numpy(v).pin_memory()
+    h_b = torch.from_numpy(b).pin_memory()
+    h_x = torch.empty(n, dtype=torch.float64).pin_memory()
+    d_rp = torch.empty_like(h_rp, device="cuda")
+    d_ci = torch.empty_like(h_ci, device="cuda")
+    d_v = torch.empty_like(h_v, device="cuda")
+    d_b = torch.empty_like(h_b, device="cuda")
+
+    def e2e_step():
+        d_rp.copy_(h_rp, non_blocking=True)
+        d_ci.copy_(h_ci, non_blocking=True)
+        d_v.copy_(h_v, non_blocking=True)
+        d_b.copy_(h_b, non_blocking=True)
+        M = V.compressed_matrix(d_rp, d_ci, d_v, n, n)
+        tag = V.cg_tag(tol, maxit)
+        x = V.solve(M, d_b, tag)
+        h_x.copy_(x, non_blocking=True)
+        return tag
+
+    for _ in range(2):
+        e2e_step()
+    t_e2e = time_events(e2e_step, args.steps)
+    t_e2e = max_over_ranks(t_e2e, ws)
+    h2d = h_rp.numel() * 4 + h_ci.numel() * 4 + h_v.numel() * 8 + h_b.numel() * 8
+    out["e2e"] = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
+                  "d2h_bytes_per_step": int(n * 8),
+                  "what": "pinned host CSR+b -> H2D, compressed_matrix (validate+analyse), "
+                          "solve, x -> host"}
+    del A
+
+    # ---- secondary measurements ----------------------------------------------
+    sec = {}
+    if not args.quick:
+        sec = secondaries(V, torch, peak, args)
+    out["secondary"] = sec
+
+    # ---- CPU baseline (rank 0, N=1): the reference algorithm on host cores ---
+    if rank == 0 and ws == 1 and not args.quick:
+        out["cpu_baseline"] = cpu_baseline_cg(rp, ci, v, b, tol, maxit)
+    else:
+        out["cpu_baseline"] = None
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def secondaries(V, torch, peak, args):
+    sec = {}
+    # SpMV format sweep on the 128^3 Laplacian
+    rp, ci, v = gen.laplace3d(128)
+    n, nnz = len(rp) - 1, int(rp[-1])
+    A = V.compressed_matrix(rp, ci, v)
+    x = torch.tensor(gen.rhs_uniform(n, 1), device="cuda")
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    r = {}
+    for name, M in (("csr", A), ("ell", V.ell_matrix(A)), ("sell_c32_s1", V.sliced_ell_matrix(A, 32, 1)),
+                    ("hyb", V.hyb_matrix(A))):
+        for _ in range(3):
+            V.prod(M, x, y=y)
+        t, g = spmv_gbs(V, M, n, nnz, 30, x, y)
+        r[name] = {"us": t * 1e6, "GBs": g, "frac_of_peak": g / peak,
+                   "GFLOPs": 2 * nnz / t / 1e9}
+    sec["spmv_laplace3d_128"] = r
+    del A
+    # 4M-row lognormal matrix
+    t0 = time.time()
+    rp, ci, v = gen.lognormal_random(4194304, seed=1)
+    n, nnz = len(rp) - 1, int(rp[-1])
+    gen_s = time.time() - t0
+    A = V.compressed_matrix(rp, ci, v)
+    x = torch.tensor(gen.rhs_uniform(n, 1), device="cuda")
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    r = {"rows": n, "nnz": nnz, "generate_s": gen_s}
+    mats = [("csr", A), ("sell_c32_s256", V.sliced_ell_matrix(A, 32, 256)),
+            ("sell_c32_s1", V.sliced_ell_matrix(A, 32, 1)), ("hyb", V.hyb_matrix(A))]
+    for name, M in mats:
+        for _ in range(3):
+            V.prod(M, x, y=y)
+        t, g = spmv_gbs(V, M, n, nnz, 20, x, y)
+        r[name] = {"us": t * 1e6, "GBs": g, "frac_of_peak": g / peak, "stored": int(M.info().stored)}
+    r["ell"] = "skipped: max row length 2000 pads ELL to ~100 GB"
+    del mats
+    sec["spmv_lognormal_4M"] = r
+    # BiCGStab / GMRES(30) on the lognormal matrix (no preconditioner, as configured)
+    import oracle
+    b = gen.rhs_uniform(n, 1)
+    bd = torch.tensor(b, device="cuda")
+    s = {}
+    for name, tag in (("bicgstab", V.bicgstab_tag(1e-10, 3000)), ("gmres30", V.gmres_tag(1e-10, 3000, 30))):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        xx = V.solve(A, bd, tag)
+        torch.cuda.synchronize()
+        s[name] = {"s": time.time() - t0, "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
+                   "error_estimate": tag.error(),
+                   "true_rel_residual": oracle.rel_residual(rp, ci, v, xx.cpu().numpy(), b)}
+    sec["solvers_lognormal_4M"] = s
+    del A
+    # 192^3 variable-coefficient diffusion: refined (FP32 inner) vs plain FP64 Jacobi-PCG
+    rp, ci, v, f = gen.diffusion3d(192)
+    n = len(rp) - 1
+    A = V.compressed_matrix(rp, ci, v)
+    fd = torch.tensor(f, device="cuda")
+    P = V.jacobi_precond(A)
+    res = {}
+    for name in ("plain_fp64_jacobi_pcg", "refined_fp32_inner"):
+        ts = []
+        for rep in range(2):
+            tag = V.cg_tag(1e-10, 20000) if name.startswith("plain") else V.refined_cg_tag(1e-10, 40000, 1e-4)
+            torch.cuda.synchronize()
+            t0 = time.time()
+            xx = V.solve(A, fd, tag, P if name.startswith("plain") else None)
+            torch.cuda.synchronize()
+            ts.append(time.time() - t0)
+        res[name] = {"s": min(ts), "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
+                     "true_rel_residual": oracle.rel_residual(rp, ci, v, xx.cpu().numpy(), f)}
+        if not name.startswith("plain"):
+            res[name]["outer"] = tag.outer
+    res["speedup"] = res["plain_fp64_jacobi_pcg"]["s"] / res["refined_fp32_inner"]["s"]
+    sec["diffusion3d_192_mixed_vs_plain"] = res
+    del A, P
+    # the reference's CPU-runnable case: 256^2 Laplacian, Jacobi-PCG to 1e-8
+    rp, ci, v = gen.laplace2d(256, 256, scaled=True)
+    b = gen.rhs_uniform(len(rp) - 1, 0)
+    A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A)
+    bd = torch.tensor(b, device="cuda")
+    for _ in range(3):
+        V.solve(A, bd, V.cg_tag(1e-8, 2000), P)
+    tag = V.cg_tag(1e-8, 2000)
+    t = time_events(lambda: V.solve(A, bd, tag, P), 10)
+    sec["laplace2d_256_jacobi_pcg"] = {"s": t, "iters": tag.iters()}
+    return sec
+
+
+def cpu_baseline_cg(rp, ci, v, b, tol, maxit):
+    import oracle
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    t0 = time.time()
+    x, it, err = oracle.solve("cg", rp, ci, v, b, tol, maxit, "none")
+    t = time.time() - t0
+    return {"value": t, "unit": "s", "cores": cores, "kind": "port",
+            "sample": "one full pipelined-CG solve of the headline workload (%d iterations)" % it,
+            "iters": it}
+
+
+def run_reference(args):
+    """The reference's own CPU algorithm (C restatement, OpenMP, all host cores)."""
+    ws, rank, local = dist_setup("gloo")
+    if rank != 0:
+        return
+    import oracle
+    rp, ci, v = gen.laplace3d(128)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 1)
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    tol, maxit = 1e-10, 10000
+    for _ in range(args.warmup):
+        oracle.solve("cg", rp, ci, v, b, tol, maxit, "none")
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.time()
+        x, it, err = oracle.solve("cg", rp, ci, v, b, tol, maxit, "none")
+        ts.append(time.time() - t0)
+    t = sum(ts) / len(ts)
+    out = {"impl": "reference", "metric": METRIC, "value": t, "unit": "s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded generators, vclgb_gen.py)",
+           "config": {"workload": WORKLOAD, "iterations": it,
+                      "true_rel_residual": oracle.rel_residual(rp, ci, v, x, b)},
+           "cpu_baseline": {"value": t, "unit": "s", "cores": cores, "kind": "port",
+                            "sample": "full pipelined-CG solves of the headline workload"},
+           "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline only (for profiling runs)")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu DRAM bytes per SpMV launch, from the committed profile")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,246 @@
+/*
+ * vclgb.h -- C ABI of the GB300 sparse Krylov engine.
+ *
+ * The engine stands in for ViennaCL's CUDA backend on the sparse path.  Each
+ * entry point below names the ViennaCL interface it replaces (paths relative
+ * to the ViennaCL source tree).  The conventions follow libviennacl's C API
+ * (libviennacl/include/viennacl.hpp): an opaque backend handle, a precision
+ * enum, plain device pointers plus offset/stride for vectors, and a status
+ * code in place of C++ exceptions.
+ *
+ * All pointers named d_* are device pointers on the backend's GPU.  Calls are
+ * asynchronous on the backend's stream unless documented otherwise; solver
+ * calls return after the solve has finished (they read back the iteration
+ * count and residual estimate).  Everything is re-entrant across backends;
+ * one backend must not be used from two host threads at once.
+ */
+#ifndef VCLGB_H
+#define VCLGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define VCLGB_API __attribute__((visibility("default")))
+#else
+#define VCLGB_API
+#endif
+
+/* ---- status codes (libviennacl/include/viennacl.hpp:95-99 has only
+ *      ViennaCLSuccess / ViennaCLGenericFailure; the codes are extended) ---- */
+typedef enum {
+  VCLGB_SUCCESS = 0,
+  VCLGB_GENERIC_FAILURE = 1,
+  VCLGB_INVALID_ARGUMENT = 2,
+  VCLGB_INVALID_MATRIX = 3,     /* row_ptr not monotone, column out of range, ... */
+  VCLGB_OUT_OF_MEMORY = 4,
+  VCLGB_CUDA_ERROR = 5,
+  VCLGB_NOT_CONVERGED = 6,      /* max iterations reached (result still written) */
+  VCLGB_BREAKDOWN = 7,          /* NaN/Inf or zero divisor inside a solver */
+  VCLGB_ZERO_ON_DIAGONAL = 8,   /* viennacl::zero_on_diagonal_exception (forwards.h:621) */
+  VCLGB_TIMEOUT = 9,            /* a bounded device-side wait gave up */
+  VCLGB_UNSUPPORTED = 10
+} vclgbStatus;
+
+/* ViennaCLPrecision (libviennacl/include/viennacl.hpp:75-80) */
+typedef enum { VCLGB_FLOAT32 = 0, VCLGB_FLOAT64 = 1 } vclgbPrecision;
+
+/* ---- backend: ViennaCLBackend (libviennacl/include/viennacl.hpp:104-113) -- */
+typedef struct vclgbBackend_st *vclgbBackend;
+
+/* Creates a backend on the current CUDA device using the given stream
+ * (NULL = the legacy default stream, as the reference's launches use). */
+VCLGB_API vclgbStatus vclgbBackendCreate(vclgbBackend *backend, void *cuda_stream);
+VCLGB_API vclgbStatus vclgbBackendDestroy(vclgbBackend *backend);
+VCLGB_API vclgbStatus vclgbBackendSetStream(vclgbBackend backend, void *cuda_stream);
+VCLGB_API vclgbStatus vclgbBackendSynchronize(vclgbBackend backend);
+/* Message of the last failure on this backend (never NULL). */
+VCLGB_API const char *vclgbBackendLastError(vclgbBackend backend);
+/* Number of kernel launches issued by this backend so far. */
+VCLGB_API uint64_t vclgbBackendLaunchCount(vclgbBackend backend);
+/* Library version string. */
+VCLGB_API const char *vclgbVersion(void);
+
+/* ---- sparse matrices ----------------------------------------------------- */
+typedef struct vclgbMatrix_st *vclgbMatrix;
+
+typedef enum {
+  VCLGB_CSR = 0,   /* viennacl::compressed_matrix   (compressed_matrix.hpp:629-1198) */
+  VCLGB_ELL = 1,   /* viennacl::ell_matrix          (ell_matrix.hpp:52-120) */
+  VCLGB_SELL = 2,  /* viennacl::sliced_ell_matrix   (sliced_ell_matrix.hpp:45-133) */
+  VCLGB_HYB = 3    /* viennacl::hyb_matrix          (hyb_matrix.hpp:37-132) */
+} vclgbFormat;
+
+/* compressed_matrix(row_ptr, cols, vals, CUDA_MEMORY, rows, cols, nnz): wraps
+ * existing device arrays without copying (compressed_matrix.hpp:740-781).  The
+ * caller keeps ownership and must keep them alive until the matrix is
+ * destroyed.  Validates row_ptr/cols on the device (VCLGB_INVALID_MATRIX) and
+ * runs the row-length analysis the adaptive CSR kernel uses. */
+VCLGB_API vclgbStatus vclgbCsrCreate(vclgbBackend be, vclgbPrecision prec, uint32_t rows,
+                                     uint32_t cols, uint32_t nnz, const uint32_t *d_row_ptr,
+                                     const uint32_t *d_col_idx, const void *d_values,
+                                     vclgbMatrix *out);
+
+/* Format conversions, performed on the GPU from a CSR matrix; the result owns
+ * its arrays.  Bit-identical to viennacl::copy(host_matrix, ...) of the same
+ * rows with columns in CSR order:
+ *   ELL : ell_matrix.hpp:123-171 (AlignmentV = 1)
+ *   SELL: sliced_ell_matrix.hpp:140-214 for sigma = 1 (slice height C);
+ *         sigma > 1 sorts rows by decreasing length in windows of sigma rows
+ *         (stable) before slicing -- SELL-C-sigma, which the reference lacks
+ *   HYB : hyb_matrix.hpp:135-234 with csr_threshold (ELL width = smallest k
+ *         with at least threshold*rows rows of length <= k, compared in the
+ *         matrix precision); the tail is kept both as the reference's CSR
+ *         arrays and as COO for the segmented-reduction kernel. */
+VCLGB_API vclgbStatus vclgbMatrixToEll(vclgbBackend be, vclgbMatrix csr, vclgbMatrix *out);
+VCLGB_API vclgbStatus vclgbMatrixToSell(vclgbBackend be, vclgbMatrix csr, uint32_t slice_height,
+                                        uint32_t sigma, vclgbMatrix *out);
+VCLGB_API vclgbStatus vclgbMatrixToHyb(vclgbBackend be, vclgbMatrix csr, double csr_threshold,
+                                       vclgbMatrix *out);
+/* FP32 copy of a matrix (same format and pattern), as mixed_precision_cg.hpp:128-137
+ * builds for its inner iterations. */
+VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend be, vclgbMatrix m, vclgbMatrix *out);
+VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m);
+
+typedef struct {
+  int32_t format;        /* vclgbFormat */
+  int32_t precision;     /* vclgbPrecision */
+  uint32_t rows, cols;
+  uint64_t nnz;          /* nonzeros of the source pattern */
+  uint64_t stored;       /* stored slots incl. padding (ELL/SELL/HYB-ELL part) */
+  uint32_t ell_width;    /* ELL: maxnnz; HYB: ellnnz */
+  uint32_t slice_height; /* SELL: C */
+  uint32_t sigma;        /* SELL: sort window */
+  uint32_t num_slices;   /* SELL */
+  uint64_t tail_nnz;     /* HYB: csr_nnz() incl. the one placeholder of an empty tail */
+  uint32_t num_bins;     /* CSR: row-length bins of the adaptive kernel */
+  uint32_t reserved;
+} vclgbMatrixInfo;
+VCLGB_API vclgbStatus vclgbMatrixGetInfo(vclgbMatrix m, vclgbMatrixInfo *info);
+
+/* Copies one internal array into a caller-provided device buffer (sized from
+ * vclgbMatrixGetInfo), for inspection and bit-exact parity checks:
+ *   ELL : 0 coords u32[rows*width] (handle2), 1 elements T[rows*width] (handle)
+ *   SELL: 0 columns_per_block u32[slices] (handle1), 1 column indices u32[stored]
+ *         (handle2), 2 block_start u32[slices] (handle3), 3 elements T[stored]
+ *         (handle), 4 row permutation u32[rows] (position -> row)
+ *   HYB : 0 ell coords, 1 ell elements, 2 tail row_ptr u32[rows+1] (handle3),
+ *         3 tail cols u32[tail_nnz] (handle4), 4 tail elements T[tail_nnz] (handle5)
+ *   CSR : 0 row_ptr, 1 cols, 2 values, 3 row blocks u32[nblocks+1] of
+ *         generate_row_block_information (compressed_matrix.hpp:1152-1188);
+ *         use vclgbCsrRowBlockCount for its length. */
+VCLGB_API vclgbStatus vclgbMatrixExport(vclgbBackend be, vclgbMatrix m, int which, void *d_dst);
+VCLGB_API vclgbStatus vclgbCsrRowBlockCount(vclgbBackend be, vclgbMatrix csr, uint32_t *count);
+
+/* ---- SpMV: linalg::prod_impl(A, x, alpha, y, beta)
+ *      (linalg/sparse_matrix_operations.hpp:90-121 -> linalg/cuda/sparse_matrix_operations.hpp
+ *      prod_impl for compressed/ell/sliced_ell/hyb).  y = alpha*A*x + beta*y,
+ *      y not read when beta == 0.  x/y are T arrays in the matrix precision;
+ *      element i lives at start + i*stride.  x and y must not overlap. ---- */
+VCLGB_API vclgbStatus vclgbSpmv(vclgbBackend be, vclgbMatrix A, double alpha, const void *d_x,
+                                int64_t x_start, int64_t x_stride, double beta, void *d_y,
+                                int64_t y_start, int64_t y_stride);
+
+/* ---- vector reductions: inner_prod / norm_2 (linalg/inner_prod.hpp,
+ *      linalg/norm_2.hpp -> cuda/vector_operations.hpp:1272-1585, 2017-2448).
+ *      The result is written to a device scalar (d_result, same precision),
+ *      with no host synchronisation. ---- */
+VCLGB_API vclgbStatus vclgbDot(vclgbBackend be, vclgbPrecision prec, uint64_t n, const void *d_x,
+                               int64_t x_start, int64_t x_stride, const void *d_y,
+                               int64_t y_start, int64_t y_stride, void *d_result);
+VCLGB_API vclgbStatus vclgbNorm2(vclgbBackend be, vclgbPrecision prec, uint64_t n,
+                                 const void *d_x, int64_t x_start, int64_t x_stride,
+                                 void *d_result);
+
+/* ---- preconditioners -------------------------------------------------------- */
+typedef struct vclgbPrecond_st *vclgbPrecond;
+
+/* jacobi_precond<compressed_matrix>(A, jacobi_tag()) (linalg/jacobi_precond.hpp:103-130):
+ * extracts diag(A) on the device (row_info SPARSE_ROW_DIAGONAL).  A zero
+ * diagonal entry returns VCLGB_ZERO_ON_DIAGONAL. */
+VCLGB_API vclgbStatus vclgbJacobiCreate(vclgbBackend be, vclgbMatrix A, vclgbPrecond *out);
+/* ilu0_precond<compressed_matrix>(A, ilu0_tag(use_level_scheduling))
+ * (linalg/detail/ilu/ilu0.hpp:189-352).  The factorisation runs on the
+ * device, level-scheduled row by row; the level sets of L and U are built on
+ * the device with the reference's elimination order (detail/ilu/common.hpp:50-187). */
+VCLGB_API vclgbStatus vclgbIlu0Create(vclgbBackend be, vclgbMatrix A, int use_level_scheduling,
+                                      vclgbPrecond *out);
+/* precond.apply(vec) in place on a contiguous device vector of length rows. */
+VCLGB_API vclgbStatus vclgbPrecondApply(vclgbBackend be, vclgbPrecond P, void *d_vec);
+VCLGB_API vclgbStatus vclgbPrecondDestroy(vclgbPrecond *P);
+
+typedef struct {
+  uint32_t num_levels_L, num_levels_U;
+  uint64_t rows_L, rows_U, nnz_L, nnz_U;
+} vclgbIlu0Info;
+VCLGB_API vclgbStatus vclgbIlu0GetInfo(vclgbPrecond P, vclgbIlu0Info *info);
+/* Exports the ILU0 factors and level sets (flattened over levels):
+ *   0 LU values T[nnz] (A's pattern, unit L implicit), 1 U diagonal T[rows],
+ *   L: 2 level_ptr u32[levels+1], 3 row_index u32[rows_L], 4 row_ptr u32[rows_L+1],
+ *      5 cols u32[nnz_L], 6 vals T[nnz_L];  U: 7..11 likewise (vals pre-divided
+ *      by the row's U diagonal, as detail/ilu/common.hpp:162 does). */
+VCLGB_API vclgbStatus vclgbIlu0Export(vclgbBackend be, vclgbPrecond P, int which, void *d_dst);
+
+/* ---- iterative solvers ------------------------------------------------------ */
+/* Mirrors cg_tag / bicgstab_tag / gmres_tag (linalg/cg.hpp:48-87,
+ * linalg/bicgstab.hpp:47-90, linalg/gmres.hpp:49-101); iters and error are
+ * outputs, like the tags' mutable members. */
+typedef struct {
+  double tol;                       /* relative tolerance */
+  double abs_tol;                   /* absolute tolerance (default 0) */
+  uint32_t max_iters;
+  uint32_t krylov_dim;              /* GMRES restart length */
+  uint32_t max_iters_before_restart;/* BiCGStab (generic preconditioned variant) */
+  uint32_t check_every;             /* iterations between host polls of the device
+                                       convergence flag (0 = automatic) */
+  /* outputs */
+  uint32_t iters;
+  uint32_t status;                  /* vclgbStatus of the solve */
+  double error;                     /* the solver's own relative residual estimate */
+} vclgbSolverTag;
+
+/* Fills a tag with the reference defaults of the given solver kind
+ * (0 = cg: 1e-8/300, 1 = bicgstab: 1e-8/400/200, 2 = gmres: 1e-10/300/20). */
+VCLGB_API void vclgbSolverTagInit(vclgbSolverTag *tag, int kind);
+
+/* linalg::solve(A, b, cg_tag[, precond]).  precond == NULL runs the pipelined
+ * Chronopoulos-Gear CG (linalg/cg.hpp:128-187), otherwise the preconditioned
+ * CG of linalg/cg.hpp:257-322, with the same stopping tests.  The whole
+ * iteration (SpMV, reductions, scalar recurrences, convergence test) runs on
+ * the device; the host only polls a flag every check_every iterations.
+ * d_b, d_x: contiguous device vectors of length rows; x is overwritten
+ * (initial guess 0, as in the reference). */
+VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
+                                   vclgbSolverTag *tag, vclgbPrecond precond);
+/* linalg::solve(A, b, bicgstab_tag[, precond]): pipelined (bicgstab.hpp:96-215)
+ * without, generic (bicgstab.hpp:398-489) with a preconditioner. */
+VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend be, vclgbMatrix A, const void *d_b,
+                                         void *d_x, vclgbSolverTag *tag, vclgbPrecond precond);
+/* linalg::solve(A, b, gmres_tag): pipelined "simpler GMRES" with classical
+ * Gram-Schmidt (gmres.hpp:181-367).  The restart bookkeeping (triangular
+ * solve of size krylov_dim) runs on the device too. */
+VCLGB_API vclgbStatus vclgbSolveGMRES(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
+                                      vclgbSolverTag *tag);
+/* linalg::solve(A, b, mixed_precision_cg_tag(tol, max_iters, inner_tol))
+ * (mixed_precision_cg.hpp:99-186): FP32 CG restarted from an FP64 residual. */
+VCLGB_API vclgbStatus vclgbSolveMixedCG(vclgbBackend be, vclgbMatrix A, const void *d_b,
+                                        void *d_x, vclgbSolverTag *tag, float inner_tol);
+
+/* FP64 iterative refinement around FP32 Jacobi-PCG inner solves (no reference
+ * counterpart).  FP64 is used only for r = b - A x, x += d and ||r||; the
+ * inner solves run on an FP32 copy of A (built once and cached on A) to the
+ * relative tolerance inner_tol (tightened no further than the outer target
+ * needs).  tag->iters = total inner iterations; outer_iters (optional) gets
+ * the number of refinement steps; tag->error = true FP64 ||b-Ax||/||b||. */
+VCLGB_API vclgbStatus vclgbSolveRefinedCG(vclgbBackend be, vclgbMatrix A, const void *d_b,
+                                          void *d_x, vclgbSolverTag *tag, double inner_tol,
+                                          uint32_t max_outer, uint32_t *outer_iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VCLGB_H */

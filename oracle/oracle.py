@@ -1,0 +1,344 @@
+"""ctypes binding of liboracle.so -- the CPU restatement of ViennaCL's host
+backend (vcl_oracle.c).  TEST INFRASTRUCTURE ONLY: imported by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline legs as the checker; the
+GPU engine never imports it.
+
+Also drives oracle/_ref/ref_driver (the reference's own host backend compiled
+from its headers) where that binary exists.
+"""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_U32, _SZ, _D, _I = ctypes.c_uint32, ctypes.c_size_t, ctypes.c_double, ctypes.c_int
+
+
+class Tag(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("abs_tol", ctypes.c_double),
+                ("max_iters", ctypes.c_uint32), ("krylov_dim", ctypes.c_uint32),
+                ("max_iters_before_restart", ctypes.c_uint32), ("iters", ctypes.c_uint32),
+                ("error", ctypes.c_double)]
+
+
+class Precond(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("diag", ctypes.c_void_p), ("rp", ctypes.c_void_p),
+                ("ci", ctypes.c_void_p), ("lu", ctypes.c_void_p), ("udiag", ctypes.c_void_p)]
+
+
+def build():
+    """Compiles liboracle.so (and the reference driver where the reference exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if os.path.isdir("/root/reference/viennacl"):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        L.vo_csr_spmv_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _D, _D, _f64p]
+        L.vo_csr_spmv_s.argtypes = [_U32, _u32p, _u32p, _f32p, _f32p, ctypes.c_float,
+                                    ctypes.c_float, _f32p]
+        L.vo_csr_spmv_strided_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _SZ, _SZ, _D, _D,
+                                            _f64p, _SZ, _SZ]
+        L.vo_csr_diag_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p]
+        L.vo_csr_row_blocks.argtypes = [_U32, _u32p, _u32p]
+        L.vo_csr_row_blocks.restype = _SZ
+        L.vo_ell_width.argtypes = [_U32, _u32p]
+        L.vo_ell_width.restype = _U32
+        L.vo_ell_fill_d.argtypes = [_U32, _u32p, _u32p, _f64p, _U32, _u32p, _f64p]
+        L.vo_ell_spmv_d.argtypes = [_U32, _U32, _u32p, _f64p, _f64p, _D, _D, _f64p]
+        L.vo_sell_layout.argtypes = [_U32, _u32p, _U32, _U32, _u32p, _u32p, _u32p]
+        L.vo_sell_layout.restype = _SZ
+        L.vo_sell_fill_d.argtypes = [_U32, _u32p, _u32p, _f64p, _U32, _u32p, _u32p, _u32p, _u32p,
+                                     _f64p]
+        L.vo_sell_spmv_d.argtypes = [_U32, _U32, _u32p, _u32p, _u32p, _u32p, _f64p, _f64p, _D, _D,
+                                     _f64p]
+        L.vo_hyb_width.argtypes = [_U32, _U32, _u32p, _D, _I, ctypes.POINTER(_SZ)]
+        L.vo_hyb_width.restype = _U32
+        L.vo_hyb_fill_d.argtypes = [_U32, _u32p, _u32p, _f64p, _U32, _u32p, _f64p, _u32p, _u32p,
+                                    _f64p]
+        L.vo_hyb_spmv_d.argtypes = [_U32, _U32, _u32p, _f64p, _u32p, _u32p, _f64p, _f64p, _D, _D,
+                                    _f64p]
+        for name in ("vo_cg_d", "vo_bicgstab_d"):
+            getattr(L, name).argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p,
+                                         ctypes.POINTER(Tag), ctypes.POINTER(Precond)]
+        L.vo_gmres_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, ctypes.POINTER(Tag)]
+        L.vo_mixed_cg_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, ctypes.POINTER(Tag),
+                                    ctypes.c_float]
+        L.vo_ir_jacobi_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, _D, _U32, _D, _U32,
+                                     ctypes.POINTER(_U32), ctypes.POINTER(_U32),
+                                     ctypes.POINTER(_D)]
+        L.vo_ilu0_factor_d.argtypes = [_U32, _u32p, _u32p, _f64p]
+        L.vo_level_setup_d.argtypes = [_U32, _u32p, _u32p, _f64p, ctypes.c_void_p, _I,
+                                       ctypes.POINTER(_SZ), ctypes.POINTER(_SZ), ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+        L.vo_level_setup_d.restype = _SZ
+        L.vo_level_substitute_d.argtypes = [_SZ, _u32p, _u32p, _u32p, _u32p, _f64p, _f64p]
+        L.vo_dot_d.argtypes = [_SZ, _f64p, _f64p]
+        L.vo_dot_d.restype = _D
+        L.vo_rel_residual_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p]
+        L.vo_rel_residual_d.restype = _D
+        L.vo_csr_transpose_d.argtypes = [_U32, _U32, _u32p, _u32p, _f64p, _u32p, _u32p, _f64p,
+                                         _u32p]
+        L.vo_set_gmres_host_quirk.argtypes = [_I]
+        L.vo_max_threads.restype = _I
+        L.vo_set_threads.argtypes = [_I]
+        _lib = L
+    return _lib
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def set_threads(n):
+    lib().vo_set_threads(int(n))
+
+
+def max_threads():
+    return lib().vo_max_threads()
+
+
+def spmv(rp, ci, v, x, alpha=1.0, beta=0.0, y=None):
+    n = len(rp) - 1
+    y = np.zeros(n) if y is None else _c(y, np.float64).copy()
+    lib().vo_csr_spmv_d(n, _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64),
+                        _c(x, np.float64), alpha, beta, y)
+    return y
+
+
+def spmv_f32(rp, ci, v, x):
+    n = len(rp) - 1
+    y = np.zeros(n, np.float32)
+    lib().vo_csr_spmv_s(n, _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float32),
+                        _c(x, np.float32), 1.0, 0.0, y)
+    return y
+
+
+def spmv_strided(rp, ci, v, x, xs, xi, alpha, beta, y, ys, yi):
+    n = len(rp) - 1
+    y = _c(y, np.float64).copy()
+    lib().vo_csr_spmv_strided_d(n, _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64),
+                                _c(x, np.float64), xs, xi, alpha, beta, y, ys, yi)
+    return y
+
+
+def diag(rp, ci, v):
+    n = len(rp) - 1
+    d = np.zeros(n)
+    lib().vo_csr_diag_d(n, _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64), d)
+    return d
+
+
+def row_blocks(rp):
+    n = len(rp) - 1
+    out = np.zeros(n + 1, np.uint32)
+    k = lib().vo_csr_row_blocks(n, _c(rp, np.uint32), out)
+    return out[:k + 1]
+
+
+def ell(rp, ci, v):
+    n = len(rp) - 1
+    rp, ci, v = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64)
+    w = lib().vo_ell_width(n, rp)
+    coords = np.zeros(max(n * w, 1), np.uint32)
+    elems = np.zeros(max(n * w, 1))
+    lib().vo_ell_fill_d(n, rp, ci, v, w, coords, elems)
+    return w, coords[:n * w], elems[:n * w]
+
+
+def sell(rp, ci, v, C=32, sigma=1):
+    n = len(rp) - 1
+    rp, ci, v = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64)
+    ns = (n - 1) // C + 1
+    perm = np.zeros(n, np.uint32)
+    cpb = np.zeros(ns, np.uint32)
+    bs = np.zeros(ns, np.uint32)
+    total = lib().vo_sell_layout(n, rp, C, sigma, perm, cpb, bs)
+    cols = np.zeros(max(total, 1), np.uint32)
+    elems = np.zeros(max(total, 1))
+    lib().vo_sell_fill_d(n, rp, ci, v, C, perm, cpb, bs, cols, elems)
+    return dict(perm=perm, cpb=cpb, bs=bs, cols=cols[:total], elems=elems[:total])
+
+
+def sell_spmv(S, n, C, x):
+    y = np.zeros(n)
+    lib().vo_sell_spmv_d(n, C, S["perm"], S["cpb"], S["bs"], _c(S["cols"], np.uint32),
+                         _c(S["elems"], np.float64), _c(x, np.float64), 1.0, 0.0, y)
+    return y
+
+
+def hyb(rp, ci, v, ncols, threshold=0.8, is_float=False):
+    n = len(rp) - 1
+    rp, ci, v = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64)
+    t = _SZ()
+    w = lib().vo_hyb_width(n, ncols, rp, threshold, 1 if is_float else 0, ctypes.byref(t))
+    tn = t.value
+    ec = np.zeros(max(n * w, 1), np.uint32)
+    ee = np.zeros(max(n * w, 1))
+    trp = np.zeros(n + 1, np.uint32)
+    tci = np.zeros(max(tn, 1), np.uint32)
+    tv = np.zeros(max(tn, 1))
+    lib().vo_hyb_fill_d(n, rp, ci, v, w, ec, ee, trp, tci, tv)
+    return dict(width=w, ell_coords=ec[:n * w], ell_elems=ee[:n * w], tail_rp=trp,
+                tail_ci=tci[:max(tn, 1)], tail_v=tv[:max(tn, 1)], tail_nnz=tn)
+
+
+def _precond(kind, rp=None, ci=None, v=None):
+    P = Precond()
+    P.kind = {"none": 0, "jacobi": 1, "ilu0": 2}[kind]
+    keep = []
+    if kind == "jacobi":
+        d = diag(rp, ci, v)
+        keep.append(d)
+        P.diag = d.ctypes.data
+    elif kind == "ilu0":
+        lu = _c(v, np.float64).copy()
+        rp32, ci32 = _c(rp, np.uint32), _c(ci, np.uint32)
+        lib().vo_ilu0_factor_d(len(rp) - 1, rp32, ci32, lu)
+        keep += [lu, rp32, ci32]
+        P.rp, P.ci, P.lu = rp32.ctypes.data, ci32.ctypes.data, lu.ctypes.data
+    return P, keep
+
+
+def solve(kind, rp, ci, v, b, tol, max_iters, precond="none", krylov_dim=30,
+          max_before_restart=200, inner_tol=1e-2):
+    """Runs cg / bicgstab / gmres / mixed_cg; returns (x, iters, error)."""
+    n = len(rp) - 1
+    rp, ci, v, b = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64), _c(b, np.float64)
+    x = np.zeros(n)
+    t = Tag(tol=tol, abs_tol=0.0, max_iters=max_iters, krylov_dim=krylov_dim,
+            max_iters_before_restart=max_before_restart)
+    P, keep = _precond(precond, rp, ci, v)
+    if kind == "cg":
+        lib().vo_cg_d(n, rp, ci, v, b, x, ctypes.byref(t), ctypes.byref(P))
+    elif kind == "bicgstab":
+        lib().vo_bicgstab_d(n, rp, ci, v, b, x, ctypes.byref(t), ctypes.byref(P))
+    elif kind == "gmres":
+        lib().vo_gmres_d(n, rp, ci, v, b, x, ctypes.byref(t))
+    elif kind == "mixed_cg":
+        lib().vo_mixed_cg_d(n, rp, ci, v, b, x, ctypes.byref(t), inner_tol)
+    else:
+        raise ValueError(kind)
+    del keep
+    return x, t.iters, t.error
+
+
+def refined_cg(rp, ci, v, b, tol=1e-10, max_outer=30, inner_tol=1e-4, max_inner=100000):
+    n = len(rp) - 1
+    x = np.zeros(n)
+    o, it, rr = _U32(), _U32(), _D()
+    lib().vo_ir_jacobi_d(n, _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64),
+                         _c(b, np.float64), x, tol, max_outer, inner_tol, max_inner,
+                         ctypes.byref(o), ctypes.byref(it), ctypes.byref(rr))
+    return x, o.value, it.value, rr.value
+
+
+def rel_residual(rp, ci, v, x, b):
+    return lib().vo_rel_residual_d(len(rp) - 1, _c(rp, np.uint32), _c(ci, np.uint32),
+                                   _c(v, np.float64), _c(x, np.float64), _c(b, np.float64))
+
+
+def ilu0_factor(rp, ci, v):
+    lu = _c(v, np.float64).copy()
+    lib().vo_ilu0_factor_d(len(rp) - 1, _c(rp, np.uint32), _c(ci, np.uint32), lu)
+    return lu
+
+
+def level_setup(rp, ci, lu, udiag, upper):
+    n = len(rp) - 1
+    rp, ci, lu = _c(rp, np.uint32), _c(ci, np.uint32), _c(lu, np.float64)
+    ud = _c(udiag, np.float64)
+    tr, tn = _SZ(), _SZ()
+    nlev = lib().vo_level_setup_d(n, rp, ci, lu, ud.ctypes.data, int(upper), ctypes.byref(tr),
+                                  ctypes.byref(tn), None, None, None, None, None)
+    lp = np.zeros(nlev + 1, np.uint32)
+    ri = np.zeros(max(tr.value, 1), np.uint32)
+    rr = np.zeros(tr.value + 1, np.uint32)
+    cc = np.zeros(max(tn.value, 1), np.uint32)
+    vv = np.zeros(max(tn.value, 1))
+    lib().vo_level_setup_d(n, rp, ci, lu, ud.ctypes.data, int(upper), ctypes.byref(tr),
+                           ctypes.byref(tn), lp.ctypes.data, ri.ctypes.data, rr.ctypes.data,
+                           cc.ctypes.data, vv.ctypes.data)
+    return dict(level_ptr=lp, row_index=ri[:tr.value], row_ptr=rr, cols=cc[:tn.value],
+                vals=vv[:tn.value])
+
+
+def level_substitute(L, vec):
+    vec = _c(vec, np.float64).copy()
+    lib().vo_level_substitute_d(len(L["level_ptr"]) - 1, L["level_ptr"], L["row_index"],
+                                L["row_ptr"], _c(L["cols"], np.uint32), _c(L["vals"], np.float64),
+                                vec)
+    return vec
+
+
+def ilu0_apply(rp, ci, v, vec):
+    """Level-scheduled ILU0 apply as ilu0_precond::apply with level scheduling."""
+    lu = ilu0_factor(rp, ci, v)
+    ud = diag(rp, ci, lu)
+    L = level_setup(rp, ci, lu, ud, False)
+    U = level_setup(rp, ci, lu, ud, True)
+    z = level_substitute(L, vec)
+    z = z / ud
+    return level_substitute(U, z)
+
+
+def transpose(nrows, ncols, rp, ci, v):
+    nnz = int(rp[-1])
+    trp = np.zeros(ncols + 1, np.uint32)
+    tci = np.zeros(max(nnz, 1), np.uint32)
+    tv = np.zeros(max(nnz, 1))
+    mp = np.zeros(max(nnz, 1), np.uint32)
+    lib().vo_csr_transpose_d(nrows, ncols, _c(rp, np.uint32), _c(ci, np.uint32),
+                             _c(v, np.float64), trp, tci, tv, mp)
+    return trp, tci[:nnz], tv[:nnz], mp[:nnz]
+
+
+# ---- the reference's own host backend (oracle/_ref/ref_driver) ---------------
+def have_ref():
+    return os.path.exists(REF_DRIVER)
+
+
+def run_ref(cmd, rp, ci, v, ncols=None, args=(), **vecs):
+    """Runs ref_driver <cmd> on the arrays; returns a dict of its output files."""
+    n = len(rp) - 1
+    ncols = n if ncols is None else ncols
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, "meta.txt"), "w") as f:
+            f.write("%d %d %d\n" % (n, ncols, int(rp[-1])))
+        _c(rp, np.uint32).tofile(os.path.join(d, "rp.u32"))
+        _c(ci, np.uint32).tofile(os.path.join(d, "ci.u32"))
+        _c(v, np.float64).tofile(os.path.join(d, "v.f64"))
+        for k, a in vecs.items():
+            _c(a, np.float64).tofile(os.path.join(d, k + ".f64"))
+        subprocess.run([REF_DRIVER, cmd, d] + [str(a) for a in args], check=True)
+        out = {}
+        for f in os.listdir(d):
+            p = os.path.join(d, f)
+            if f.endswith(".u32"):
+                out[f[:-4]] = np.fromfile(p, np.uint32)
+            elif f.endswith(".f64"):
+                out[f[:-4]] = np.fromfile(p, np.float64)
+            elif f.endswith(".f32"):
+                out[f[:-4]] = np.fromfile(p, np.float32)
+            elif f == "info.txt":
+                it, err, sec = open(p).read().split()
+                out["iters"], out["error"], out["seconds"] = int(it), float(err), float(sec)
+        return out

@@ -1,0 +1,126 @@
+"""GPU conversions CSR -> ELL / SELL-C-sigma / HYB: bit-exact against the
+reference's copy() output (golden) and the oracle, plus SpMV per format."""
+import numpy as np
+import pytest
+
+import oracle
+import vclgb_gen as gen
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def V():
+    import torch
+    import vclgb
+    torch.cuda.set_device(0)
+    return vclgb
+
+
+def _u32(t):
+    return t.cpu().numpy().view(np.uint32)
+
+
+def _ell_arrays(M, n):
+    import torch
+    inf = M.info()
+    w = inf.ell_width
+    return w, _u32(M.export(0, n * w, torch.int32)), M.export(1, n * w, torch.float64).cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["formats_lognormal.npz", "formats_laplace2d.npz"])
+def test_golden_conversions(V, golden, name):
+    import torch
+    d = golden(name)
+    rp, ci, v, x = d["rp"], d["ci"], d["v"], d["x"]
+    n = len(rp) - 1
+    A = V.compressed_matrix(rp, ci, v)
+    E = V.ell_matrix(A)
+    w, coords, elems = _ell_arrays(E, n)
+    assert w == int(d["ell_width"][0])
+    assert np.array_equal(coords, d["ell_coords"]) and np.array_equal(elems, d["ell_elems"])
+    S = V.sliced_ell_matrix(A, int(d["C"]), 1)
+    inf = S.info()
+    assert np.array_equal(_u32(S.export(0, inf.num_slices, torch.int32)), d["sell_cpb"])
+    assert np.array_equal(_u32(S.export(2, inf.num_slices, torch.int32)), d["sell_bs"])
+    assert np.array_equal(_u32(S.export(1, inf.stored, torch.int32)), d["sell_cols"])
+    assert np.array_equal(S.export(3, inf.stored, torch.float64).cpu().numpy(), d["sell_elems"])
+    H = V.hyb_matrix(A, float(d["threshold"]))
+    hi = H.info()
+    assert hi.ell_width == int(d["hyb_width"][0]) and hi.tail_nnz == int(d["hyb_tail_nnz"][0])
+    assert np.array_equal(_u32(H.export(0, n * hi.ell_width, torch.int32)), d["hyb_ell_coords"])
+    assert np.array_equal(H.export(1, n * hi.ell_width, torch.float64).cpu().numpy(),
+                          d["hyb_ell_elems"])
+    assert np.array_equal(_u32(H.export(2, n + 1, torch.int32)), d["hyb_tail_rp"])
+    assert np.array_equal(_u32(H.export(3, hi.tail_nnz, torch.int32)), d["hyb_tail_ci"])
+    assert np.array_equal(H.export(4, hi.tail_nnz, torch.float64).cpu().numpy(), d["hyb_tail_v"])
+    for M, key in ((E, "y_ell"), (S, "y_sell"), (H, "y_hyb")):
+        if key in d:
+            assert rel_err(V.prod(M, x).cpu().numpy(), d[key]) < 1e-13, key
+
+
+def test_hyb_float_threshold(V, golden):
+    d = golden("hyb_f32_laplace2d.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"].astype(np.float32))
+    assert V.hyb_matrix(A, 0.8).info().ell_width == int(d["width"][0])
+
+
+@pytest.mark.parametrize("sigma", [1, 8, 256])
+@pytest.mark.parametrize("C", [32, 64, 7])
+def test_sell_sigma_against_oracle(V, C, sigma):
+    import torch
+    rp, ci, v = gen.lognormal_random(20000, mu=2.0, sigma=1.0, hi=300, seed=5)
+    n = len(rp) - 1
+    ref = oracle.sell(rp, ci, v, C=C, sigma=sigma)
+    A = V.compressed_matrix(rp, ci, v)
+    S = V.sliced_ell_matrix(A, C, sigma)
+    inf = S.info()
+    assert inf.stored == ref["cols"].size
+    assert np.array_equal(_u32(S.export(4, n, torch.int32)), ref["perm"])
+    assert np.array_equal(_u32(S.export(0, inf.num_slices, torch.int32)), ref["cpb"])
+    assert np.array_equal(_u32(S.export(2, inf.num_slices, torch.int32)), ref["bs"])
+    assert np.array_equal(_u32(S.export(1, inf.stored, torch.int32)), ref["cols"])
+    assert np.array_equal(S.export(3, inf.stored, torch.float64).cpu().numpy(), ref["elems"])
+    x = np.random.default_rng(2).uniform(-1, 1, n)
+    assert rel_err(V.prod(S, x).cpu().numpy(), oracle.spmv(rp, ci, v, x)) < 1e-13
+    if sigma > 1:  # sorting windows shrink the padding
+        assert inf.stored <= oracle.sell(rp, ci, v, C=C, sigma=1)["cols"].size
+
+
+@pytest.mark.parametrize("thr", [0.5, 0.8, 0.95, 1.0])
+def test_hyb_tail_segments(V, thr):
+    # long tails spanning many warp chunks exercise the segmented reduction
+    rp, ci, v = gen.lognormal_random(30000, mu=2.5, sigma=1.2, hi=2000, seed=9)
+    n = len(rp) - 1
+    ref = oracle.hyb(rp, ci, v, n, thr)
+    A = V.compressed_matrix(rp, ci, v)
+    H = V.hyb_matrix(A, thr)
+    hi = H.info()
+    assert hi.ell_width == ref["width"]
+    assert hi.tail_nnz == max(ref["tail_nnz"], 1)
+    x = np.random.default_rng(4).uniform(-1, 1, n)
+    y0 = np.random.default_rng(5).uniform(-1, 1, n)
+    import torch
+    y = torch.tensor(y0, device="cuda")
+    V.prod(H, x, alpha=-0.75, y=y, beta=2.0)
+    assert rel_err(y.cpu().numpy(), oracle.spmv(rp, ci, v, x, -0.75, 2.0, y0)) < 1e-13
+
+
+def test_ell_float32(V):
+    rp, ci, v = gen.laplace3d(20)
+    A = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    x = np.random.default_rng(3).uniform(-1, 1, len(rp) - 1).astype(np.float32)
+    for M in (V.ell_matrix(A), V.sliced_ell_matrix(A, 32, 1), V.hyb_matrix(A)):
+        assert rel_err(V.prod(M, x).cpu().numpy(), oracle.spmv(rp, ci, v, x)) < 1e-5
+
+
+def test_full_size_lognormal_formats(V):
+    # 1M-row lognormal matrix: all formats agree with the oracle (size-independent check)
+    rp, ci, v = gen.lognormal_random(1 << 20, seed=1)
+    n = len(rp) - 1
+    x = np.random.default_rng(1).uniform(-1, 1, n)
+    ref = oracle.spmv(rp, ci, v, x)
+    A = V.compressed_matrix(rp, ci, v)
+    for M in (A, V.sliced_ell_matrix(A, 32, 256), V.hyb_matrix(A)):
+        assert rel_err(V.prod(M, x).cpu().numpy(), ref) < 1e-13

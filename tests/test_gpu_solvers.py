@@ -1,0 +1,177 @@
+"""Solvers on the GPU against the reference's golden outputs and the oracle:
+same stopping rule, iteration counts within 2%, solutions within tolerance,
+true FP64 relative residuals reported."""
+import numpy as np
+import pytest
+
+import oracle
+import vclgb_gen as gen
+from conftest import iters_close, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def V():
+    import torch
+    import vclgb
+    torch.cuda.set_device(0)
+    return vclgb
+
+
+def _np(t):
+    return t.cpu().numpy()
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi", "ilu0"])
+def test_cg_golden(V, golden, pc):
+    d = golden("cg_laplace2d.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    P = {"none": None, "jacobi": V.jacobi_precond(A), "ilu0": V.ilu0_precond(A)}[pc]
+    tag = V.cg_tag(float(d["tol"]), int(d["max_iters"]))
+    x = _np(V.solve(A, d["b"], tag, P))
+    assert tag.status() == V.SUCCESS
+    assert iters_close(tag.iters(), int(d["iters_" + pc]))
+    assert rel_err(x, d["x_" + pc]) < 1e-6
+    assert abs(tag.error() - float(d["error_" + pc])) < 0.05 * float(d["error_" + pc])
+    assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 1e-7
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_bicgstab_golden(V, golden, pc):
+    d = golden("bicgstab_convdiff.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.bicgstab_tag(float(d["tol"]), int(d["max_iters"]))
+    x = _np(V.solve(A, d["b"], tag, P))
+    assert tag.status() == V.SUCCESS
+    assert iters_close(tag.iters(), int(d["iters_" + pc]))
+    assert rel_err(x, d["x_" + pc]) < 1e-7
+
+
+def test_gmres_against_oracle_and_reference(V, golden):
+    d = golden("gmres_convdiff_1thread.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    tag = V.gmres_tag(1e-10, 600, 30)
+    x = _np(V.solve(A, d["b"], tag))
+    xo, it_o, err_o = oracle.solve("gmres", d["rp"], d["ci"], d["v"], d["b"], 1e-10, 600,
+                                   krylov_dim=30)
+    assert tag.status() == V.SUCCESS
+    assert iters_close(tag.iters(), it_o)
+    assert rel_err(x, xo) < 1e-7
+    # the reference host backend needs more iterations (its stage-1 defect)
+    assert tag.iters() <= int(d["iters"])
+    assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 2e-10
+
+
+def test_mixed_cg_golden(V, golden):
+    d = golden("mixed_cg_laplace2d.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    tag = V.mixed_precision_cg_tag(float(d["tol"]), int(d["max_iters"]), float(d["inner_tol"]))
+    x = _np(V.solve(A, d["b"], tag))
+    assert tag.status() == V.SUCCESS
+    # FP32 inner products round differently on the GPU: allow 5% on iterations
+    assert abs(tag.iters() - int(d["iters"])) <= max(2, 0.05 * int(d["iters"]))
+    assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 1e-8
+
+
+def test_refined_cg_reaches_fp64_residual(V):
+    rp, ci, v, f = gen.diffusion3d(32, corr=4.0, contrast=1e4, seed=2)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.refined_cg_tag(1e-10, 100000, 1e-4)
+    x = _np(V.solve(A, f, tag))
+    assert tag.status() == V.SUCCESS
+    rr = oracle.rel_residual(rp, ci, v, x, f)
+    assert rr < 1e-10 and tag.outer >= 2
+    assert abs(rr - tag.error()) < 1e-3 * rr + 1e-16
+    xo, outer, inner, rro = oracle.refined_cg(rp, ci, v, f, tol=1e-10, inner_tol=1e-4)
+    assert rro < 1e-10
+    # same algorithm, different FP32 rounding: inner totals within 15%
+    assert abs(tag.iters() - inner) <= 0.15 * inner + 5
+
+
+def test_reference_cpu_case_laplace256(V):
+    # 256x256 Laplacian (h = 1/257), b ~ U[-1,1] seed 0, Jacobi-PCG to 1e-8, max 2000
+    rp, ci, v = gen.laplace2d(256, 256, scaled=True)
+    b = gen.rhs_uniform(len(rp) - 1, 0)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.cg_tag(1e-8, 2000)
+    x = _np(V.solve(A, b, tag, V.jacobi_precond(A)))
+    xo, it_o, err_o = oracle.solve("cg", rp, ci, v, b, 1e-8, 2000, "jacobi")
+    assert iters_close(tag.iters(), it_o)
+    assert rel_err(x, xo) < 1e-6
+
+
+@pytest.mark.parametrize("fmt", ["ell", "sell", "hyb"])
+def test_pipelined_cg_other_formats(V, fmt):
+    rp, ci, v = gen.laplace3d(24)
+    b = gen.rhs_uniform(len(rp) - 1, 4)
+    A = V.compressed_matrix(rp, ci, v)
+    M = {"ell": lambda: V.ell_matrix(A), "sell": lambda: V.sliced_ell_matrix(A, 32, 1),
+         "hyb": lambda: V.hyb_matrix(A)}[fmt]()
+    tag = V.cg_tag(1e-10, 1000)
+    x = _np(V.solve(M, b, tag))
+    xo, it_o, _ = oracle.solve("cg", rp, ci, v, b, 1e-10, 1000)
+    assert iters_close(tag.iters(), it_o)
+    assert rel_err(x, xo) < 1e-8
+
+
+def test_bicgstab_on_hyb_and_sell(V):
+    rp, ci, v = gen.lognormal_random(20000, mu=2.0, sigma=0.5, hi=60, seed=7)
+    b = gen.rhs_uniform(len(rp) - 1, 1)
+    A = V.compressed_matrix(rp, ci, v)
+    xo, it_o, _ = oracle.solve("bicgstab", rp, ci, v, b, 1e-10, 400)
+    for M in (A, V.sliced_ell_matrix(A, 32, 256), V.hyb_matrix(A)):
+        tag = V.bicgstab_tag(1e-10, 400)
+        x = _np(V.solve(M, b, tag))
+        assert tag.status() == V.SUCCESS
+        assert abs(tag.iters() - it_o) <= max(2, 0.1 * it_o)
+        assert oracle.rel_residual(rp, ci, v, x, b) < 1e-8
+
+
+def test_float32_cg(V):
+    rp, ci, v = gen.laplace2d(64)
+    b = gen.rhs_uniform(len(rp) - 1, 2)
+    A = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    tag = V.cg_tag(1e-5, 2000)
+    x = _np(V.solve(A, b.astype(np.float32), tag, V.jacobi_precond(A)))
+    assert tag.status() == V.SUCCESS
+    assert oracle.rel_residual(rp, ci, v, x.astype(np.float64), b) < 1e-4
+
+
+def test_max_iterations_status(V):
+    rp, ci, v = gen.laplace2d(64)
+    b = gen.rhs_uniform(len(rp) - 1, 2)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.cg_tag(1e-14, 7)
+    V.solve(A, b, tag)
+    assert tag.status() == V.NOT_CONVERGED and tag.iters() == 7
+    xo, it_o, err_o = oracle.solve("cg", rp, ci, v, b, 1e-14, 7)
+    assert abs(tag.error() - err_o) < 1e-6 * err_o
+
+
+def test_zero_rhs(V):
+    rp, ci, v = gen.laplace2d(16)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.cg_tag(1e-8, 100)
+    x = _np(V.solve(A, np.zeros(len(rp) - 1), tag))
+    assert tag.iters() == 0 and not x.any()
+
+
+def test_invalid_matrix_rejected(V):
+    rp = np.array([0, 2, 1, 3], np.uint32)  # not monotone
+    with pytest.raises(V.VclgbError) as e:
+        V.compressed_matrix(rp, np.array([0, 1, 2], np.uint32), np.ones(3))
+    assert e.value.status == V.INVALID_MATRIX
+    rp = np.array([0, 1, 2], np.uint32)
+    with pytest.raises(V.VclgbError) as e:
+        V.compressed_matrix(rp, np.array([0, 5], np.uint32), np.ones(2), 2, 2)
+    assert e.value.status == V.INVALID_MATRIX
+
+
+def test_zero_on_diagonal(V):
+    rp = np.array([0, 1, 2], np.uint32)
+    A = V.compressed_matrix(rp, np.array([0, 0], np.uint32), np.ones(2), 2, 2)
+    with pytest.raises(V.VclgbError) as e:
+        V.jacobi_precond(A)
+    assert e.value.status == V.ZERO_ON_DIAGONAL

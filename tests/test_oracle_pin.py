@@ -1,0 +1,173 @@
+"""The CPU oracle (oracle/vcl_oracle.c) against ViennaCL's own host backend:
+golden fixtures produced by tests/golden/make_golden.py, the small literal
+matrices of the reference's tests/src/sparse.cpp, and -- where the reference
+tree exists -- live runs of oracle/_ref/ref_driver."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+
+
+def test_kat_strided_spmv():
+    # tests/src/sparse.cpp:163-177: project(result, slice(1,3,5)) =
+    #   prod(A, project(rhs, slice(3,2,4))) with the 5x4 literal matrix
+    rows = [{0: 2.0, 2: -1.0}, {0: 3.0, 2: -5.0}, {1: 5.0, 2: -2.0}, {2: 1.0, 3: -6.0},
+            {1: 7.0, 2: -5.0}]
+    rp = np.zeros(6, np.uint32)
+    ci, v = [], []
+    for i, r in enumerate(rows):
+        for c in sorted(r):
+            ci.append(c)
+            v.append(r[c])
+        rp[i + 1] = len(ci)
+    rhs = np.arange(1, 12, dtype=np.float64) * 0.5
+    y = np.full(16, 7.0)
+    out = oracle.spmv_strided(rp, np.array(ci, np.uint32), np.array(v), rhs, 3, 2, 1.0, 0.0,
+                              y, 1, 3)
+    expect = y.copy()
+    for i, r in enumerate(rows):
+        expect[1 + 3 * i] = sum(val * rhs[3 + 2 * c] for c, val in r.items())
+    assert np.array_equal(out, expect)
+
+
+def test_spmv_alpha_beta_golden(golden):
+    d = golden("spmv_lognormal.npz")
+    y = oracle.spmv(d["rp"], d["ci"], d["v"], d["x"], float(d["alpha"]), float(d["beta"]), d["y0"])
+    assert rel_err(y, d["y"]) < 1e-14
+    assert np.array_equal(oracle.row_blocks(d["rp"]), d["row_blocks"])
+
+
+def test_spmv_f32_golden(golden):
+    d = golden("spmv_f32_lognormal.npz")
+    y = oracle.spmv_f32(d["rp"], d["ci"], d["v"].astype(np.float32), d["x"].astype(np.float32))
+    assert rel_err(y, d["yf"]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["formats_lognormal.npz", "formats_laplace2d.npz"])
+def test_conversions_golden(golden, name):
+    d = golden(name)
+    rp, ci, v, x = d["rp"], d["ci"], d["v"], d["x"]
+    n = len(rp) - 1
+    w, coords, elems = oracle.ell(rp, ci, v)
+    assert w == int(d["ell_width"][0])
+    assert np.array_equal(coords, d["ell_coords"]) and np.array_equal(elems, d["ell_elems"])
+    S = oracle.sell(rp, ci, v, C=int(d["C"]), sigma=1)
+    for k, g in (("cpb", "sell_cpb"), ("bs", "sell_bs"), ("cols", "sell_cols"),
+                 ("elems", "sell_elems")):
+        assert np.array_equal(S[k], d[g]), k
+    H = oracle.hyb(rp, ci, v, n, float(d["threshold"]))
+    assert H["width"] == int(d["hyb_width"][0])
+    assert max(H["tail_nnz"], 1) == int(d["hyb_tail_nnz"][0])
+    assert np.array_equal(H["ell_coords"], d["hyb_ell_coords"])
+    assert np.array_equal(H["ell_elems"], d["hyb_ell_elems"])
+    assert np.array_equal(H["tail_rp"], d["hyb_tail_rp"])
+    assert np.array_equal(H["tail_ci"], d["hyb_tail_ci"])
+    assert np.array_equal(H["tail_v"], d["hyb_tail_v"])
+    y = oracle.spmv(rp, ci, v, x)
+    assert rel_err(y, d["y_ell"]) < 1e-14
+    assert rel_err(y, d["y_hyb"]) < 1e-14
+    if "y_sell" in d:
+        assert rel_err(oracle.sell_spmv(S, n, int(d["C"]), x), d["y_sell"]) < 1e-14
+
+
+def test_hyb_float_threshold_golden(golden):
+    d = golden("hyb_f32_laplace2d.npz")
+    n = len(d["rp"]) - 1
+    H = oracle.hyb(d["rp"], d["ci"], d["v"], n, 0.8, is_float=True)
+    assert H["width"] == int(d["width"][0])
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi", "ilu0"])
+def test_cg_golden(golden, pc):
+    d = golden("cg_laplace2d.npz")
+    x, it, err = oracle.solve("cg", d["rp"], d["ci"], d["v"], d["b"], float(d["tol"]),
+                              int(d["max_iters"]), pc)
+    assert it == int(d["iters_" + pc])
+    assert abs(err - float(d["error_" + pc])) <= 1e-6 * float(d["error_" + pc])
+    assert rel_err(x, d["x_" + pc]) < 1e-12
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_bicgstab_golden(golden, pc):
+    d = golden("bicgstab_convdiff.npz")
+    x, it, err = oracle.solve("bicgstab", d["rp"], d["ci"], d["v"], d["b"], float(d["tol"]),
+                              int(d["max_iters"]), pc)
+    assert abs(it - int(d["iters_" + pc])) <= 1
+    assert rel_err(x, d["x_" + pc]) < 1e-9
+
+
+def test_gmres_golden_single_thread(golden):
+    # the host stage-1 kernel drops vector tails depending on the thread count,
+    # so this pin runs in a child process with one OpenMP thread and the
+    # restatement's switch that reproduces that partition
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    code = (
+        "import sys; sys.path.insert(0, %r); import oracle, numpy as np\n"
+        "d = dict(np.load(%r))\n"
+        "oracle.lib().vo_set_gmres_host_quirk(1)\n"
+        "x, it, err = oracle.solve('gmres', d['rp'], d['ci'], d['v'], d['b'], 1e-10, 600, "
+        "krylov_dim=30)\n"
+        "assert it == int(d['iters']), (it, d['iters'])\n"
+        "assert np.array_equal(x, d['x'])\n"
+        "assert err == float(d['error'])\n") % (
+        os.path.dirname(oracle.__file__),
+        os.path.join(os.path.dirname(__file__), "golden", "gmres_convdiff_1thread.npz"))
+    subprocess.run([sys.executable, "-c", code], env=env, check=True)
+
+
+def test_gmres_converges_without_host_defect(golden):
+    d = golden("gmres_convdiff_1thread.npz")
+    x, it, err = oracle.solve("gmres", d["rp"], d["ci"], d["v"], d["b"], 1e-10, 600, krylov_dim=30)
+    assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 2e-10
+    assert it <= int(d["iters"])
+
+
+def test_mixed_cg_golden(golden):
+    d = golden("mixed_cg_laplace2d.npz")
+    x, it, err = oracle.solve("mixed_cg", d["rp"], d["ci"], d["v"], d["b"], float(d["tol"]),
+                              int(d["max_iters"]), inner_tol=float(d["inner_tol"]))
+    assert it == int(d["iters"])
+    assert rel_err(x, d["x"]) < 1e-12
+
+
+def test_ilu0_golden(golden):
+    d = golden("ilu0_convdiff.npz")
+    rp, ci, v = d["rp"], d["ci"], d["v"]
+    lu = oracle.ilu0_factor(rp, ci, v)
+    assert np.array_equal(lu, d["lu"])  # same operation order, no FMA: bit-identical
+    ud = oracle.diag(rp, ci, lu)
+    assert np.array_equal(ud, d["udiag"])
+    for tri, upper in (("L", False), ("U", True)):
+        lv = oracle.level_setup(rp, ci, lu, ud, upper)
+        assert np.array_equal(lv["level_ptr"], d[tri + "_level_ptr"])
+        assert np.array_equal(lv["row_index"], d[tri + "_row_index"])
+        assert np.array_equal(lv["row_ptr"], d[tri + "_row_ptr"])
+        assert np.array_equal(lv["cols"], d[tri + "_cols"])
+        assert np.array_equal(lv["vals"], d[tri + "_vals"])
+    z = oracle.ilu0_apply(rp, ci, v, d["b"])
+    assert rel_err(z, d["z"]) < 1e-14
+
+
+def test_refined_cg_reaches_tolerance():
+    import vclgb_gen as gen
+    rp, ci, v, f = gen.diffusion3d(16, corr=3.0, contrast=1e3, seed=2)
+    x, outer, inner, rr = oracle.refined_cg(rp, ci, v, f, tol=1e-10, inner_tol=1e-4)
+    assert rr < 1e-10 and outer >= 2
+    assert oracle.rel_residual(rp, ci, v, x, f) < 1e-10
+
+
+@pytest.mark.skipif(not oracle.have_ref(), reason="ViennaCL tree not present here")
+def test_live_reference_cg_jacobi_laplace256():
+    # the reference's own CPU-runnable case: 256x256 Laplacian, Jacobi-PCG to 1e-8
+    import vclgb_gen as gen
+    rp, ci, v = gen.laplace2d(256, 256, scaled=True)
+    b = gen.rhs_uniform(len(rp) - 1, 0)
+    r = oracle.run_ref("cg", rp, ci, v, args=(1e-8, 2000, "jacobi"), b=b)
+    x, it, err = oracle.solve("cg", rp, ci, v, b, 1e-8, 2000, "jacobi")
+    assert abs(it - r["iters"]) <= 1
+    assert rel_err(x, r["x"]) < 1e-10

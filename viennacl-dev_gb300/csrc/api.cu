@@ -1,0 +1,443 @@
+// api.cu -- the extern "C" entry points declared in include/vclgb.h.
+#include <algorithm>
+
+#include "formats.hpp"
+#include "vecpass.cuh"
+
+namespace vclgb {
+template <typename T>
+void cg_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Precond *);
+template <typename T>
+void bicgstab_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Precond *);
+template <typename T>
+void gmres_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *);
+void mixed_cg_solve(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, float);
+void refined_cg_solve(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, double,
+                      uint32_t, uint32_t *);
+}  // namespace vclgb
+
+using namespace vclgb;
+
+namespace {
+template <class F>
+static vclgbStatus convert(vclgbBackend h, vclgbMatrix src, vclgbMatrix *out, F &&f) {
+  if (!h || !src || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    std::unique_ptr<Matrix> m = f(*be, *M(src));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
+template <class F>
+static vclgbStatus solve_entry(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
+                               vclgbSolverTag *tag, F &&f) {
+  if (!h || !A || !tag || !b || !x) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  vclgbStatus s = guarded(be, [&]() { f(*be, *M(A)); });
+  if (s != VCLGB_SUCCESS) {
+    tag->status = s;
+    return s;
+  }
+  return (vclgbStatus)tag->status;
+}
+
+}  // namespace
+
+extern "C" {
+
+VCLGB_API const char *vclgbVersion(void) { return "vclgb 0.1 (sm_103a)"; }
+
+VCLGB_API vclgbStatus vclgbBackendCreate(vclgbBackend *out, void *stream) {
+  if (!out) return VCLGB_INVALID_ARGUMENT;
+  auto be = new (std::nothrow) Backend();
+  if (!be) return VCLGB_OUT_OF_MEMORY;
+  vclgbStatus s = guarded(be, [&]() {
+    VCLGB_CUDA(cudaGetDevice(&be->device));
+    cudaDeviceProp prop;
+    VCLGB_CUDA(cudaGetDeviceProperties(&prop, be->device));
+    be->num_sms = prop.multiProcessorCount;
+    be->max_threads_per_sm = prop.maxThreadsPerMultiProcessor;
+    be->max_smem_per_block = prop.sharedMemPerBlockOptin;
+    if (stream) {
+      be->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      // a blocking stream of our own: ordered with the legacy default stream,
+      // and capturable into CUDA graphs
+      VCLGB_CUDA(cudaStreamCreateWithFlags(&be->stream, cudaStreamDefault));
+      be->own_stream = true;
+    }
+    VCLGB_CUDA(cudaMallocHost(&be->host_flags, 64));
+    be->red_partials.alloc(8 * kMaxSpmvGrid * sizeof(double), be->stream);
+    be->red_counter.alloc(64, be->stream);
+    VCLGB_CUDA(cudaMemsetAsync(be->red_counter.ptr, 0, 64, be->stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+  });
+  if (s != VCLGB_SUCCESS) {
+    delete be;
+    return s;
+  }
+  *out = reinterpret_cast<vclgbBackend>(be);
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbBackendDestroy(vclgbBackend *h) {
+  if (!h || !*h) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(*h);
+  cudaStreamSynchronize(be->stream);
+  be->red_partials.release();
+  be->red_counter.release();
+  cudaStreamSynchronize(be->stream);
+  if (be->host_flags) cudaFreeHost(be->host_flags);
+  if (be->own_stream) cudaStreamDestroy(be->stream);
+  delete be;
+  *h = nullptr;
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbBackendSetStream(vclgbBackend h, void *stream) {
+  if (!h) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(stream != nullptr, VCLGB_INVALID_ARGUMENT, "stream must not be NULL");
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    if (be->own_stream) VCLGB_CUDA(cudaStreamDestroy(be->stream));
+    be->own_stream = false;
+    be->stream = static_cast<cudaStream_t>(stream);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbBackendSynchronize(vclgbBackend h) {
+  if (!h) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { VCLGB_CUDA(cudaStreamSynchronize(be->stream)); });
+}
+
+VCLGB_API const char *vclgbBackendLastError(vclgbBackend h) {
+  return h ? B(h)->last_error.c_str() : "no backend";
+}
+
+VCLGB_API uint64_t vclgbBackendLaunchCount(vclgbBackend h) { return h ? B(h)->launches : 0; }
+
+// ---------------------------------------------------------------------------
+VCLGB_API vclgbStatus vclgbCsrCreate(vclgbBackend h, vclgbPrecision prec, uint32_t rows,
+                                     uint32_t cols, uint32_t nnz, const uint32_t *d_row_ptr,
+                                     const uint32_t *d_col_idx, const void *d_values,
+                                     vclgbMatrix *out) {
+  if (!h || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(prec == VCLGB_FLOAT32 || prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "bad precision");
+    require(d_row_ptr != nullptr, VCLGB_INVALID_ARGUMENT, "row_ptr is NULL");
+    require(nnz == 0 || (d_col_idx && d_values), VCLGB_INVALID_ARGUMENT, "cols/values are NULL");
+    auto m = std::make_unique<Matrix>();
+    m->format = VCLGB_CSR;
+    m->prec = prec;
+    m->rows = rows;
+    m->cols = cols;
+    m->nnz = nnz;
+    m->row_ptr = d_row_ptr;
+    m->col_idx = d_col_idx;
+    m->values = d_values;
+    csr_validate(*be, *m);
+    csr_analyse(*be, *m);
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbMatrixToEll(vclgbBackend h, vclgbMatrix csr, vclgbMatrix *out) {
+  return convert(h, csr, out, [](Backend &be, Matrix &m) { return convert_ell(be, m); });
+}
+VCLGB_API vclgbStatus vclgbMatrixToSell(vclgbBackend h, vclgbMatrix csr, uint32_t C,
+                                        uint32_t sigma, vclgbMatrix *out) {
+  return convert(h, csr, out,
+                 [&](Backend &be, Matrix &m) { return convert_sell(be, m, C, sigma); });
+}
+VCLGB_API vclgbStatus vclgbMatrixToHyb(vclgbBackend h, vclgbMatrix csr, double thr,
+                                       vclgbMatrix *out) {
+  return convert(h, csr, out, [&](Backend &be, Matrix &m) { return convert_hyb(be, m, thr); });
+}
+VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend h, vclgbMatrix m, vclgbMatrix *out) {
+  return convert(h, m, out, [&](Backend &be, Matrix &mm) { return convert_f32(be, mm); });
+}
+
+VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m) {
+  if (!m || !*m) return VCLGB_INVALID_ARGUMENT;
+  Matrix *mm = M(*m);
+  cudaDeviceSynchronize();
+  delete mm;
+  *m = nullptr;
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbMatrixGetInfo(vclgbMatrix h, vclgbMatrixInfo *info) {
+  if (!h || !info) return VCLGB_INVALID_ARGUMENT;
+  const Matrix &m = *M(h);
+  std::memset(info, 0, sizeof(*info));
+  info->format = m.format;
+  info->precision = m.prec;
+  info->rows = m.rows;
+  info->cols = m.cols;
+  info->nnz = m.nnz;
+  switch (m.format) {
+    case VCLGB_CSR: info->stored = m.nnz; info->num_bins = m.num_bins; break;
+    case VCLGB_ELL: info->stored = (uint64_t)m.rows * m.ell_width; info->ell_width = m.ell_width; break;
+    case VCLGB_SELL:
+      info->stored = m.sell_stored;
+      info->slice_height = m.C;
+      info->sigma = m.sigma;
+      info->num_slices = m.num_slices;
+      break;
+    case VCLGB_HYB:
+      info->stored = (uint64_t)m.rows * m.ell_width;
+      info->ell_width = m.ell_width;
+      info->tail_nnz = m.tail_nnz ? m.tail_nnz : 1;
+      break;
+  }
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbCsrRowBlockCount(vclgbBackend h, vclgbMatrix csr, uint32_t *count) {
+  if (!h || !csr || !count) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(M(csr)->format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "not a CSR matrix");
+    csr_row_blocks(*be, *M(csr));
+    *count = M(csr)->num_row_blocks;
+  });
+}
+
+VCLGB_API vclgbStatus vclgbMatrixExport(vclgbBackend h, vclgbMatrix mh, int which, void *dst) {
+  if (!h || !mh || !dst) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    Matrix &m = *M(mh);
+    const void *src = nullptr;
+    size_t bytes = 0;
+    const size_t vs = m.vsize();
+    switch (m.format) {
+      case VCLGB_CSR:
+        if (which == 0) { src = m.row_ptr; bytes = ((size_t)m.rows + 1) * 4; }
+        else if (which == 1) { src = m.col_idx; bytes = m.nnz * 4; }
+        else if (which == 2) { src = m.values; bytes = m.nnz * vs; }
+        else if (which == 3) {
+          csr_row_blocks(*be, m);
+          src = m.row_blocks.ptr;
+          bytes = ((size_t)m.num_row_blocks + 1) * 4;
+        }
+        break;
+      case VCLGB_ELL:
+        if (which == 0) { src = m.ell_coords.ptr; bytes = (size_t)m.rows * m.ell_width * 4; }
+        else if (which == 1) { src = m.ell_elems.ptr; bytes = (size_t)m.rows * m.ell_width * vs; }
+        break;
+      case VCLGB_SELL:
+        if (which == 0) { src = m.sell_cpb.ptr; bytes = (size_t)m.num_slices * 4; }
+        else if (which == 1) { src = m.sell_cols.ptr; bytes = m.sell_stored * 4; }
+        else if (which == 2) { src = m.sell_start.ptr; bytes = (size_t)m.num_slices * 4; }
+        else if (which == 3) { src = m.sell_elems.ptr; bytes = m.sell_stored * vs; }
+        else if (which == 4) {
+          if (m.sigma > 1) { src = m.sell_perm.ptr; bytes = (size_t)m.rows * 4; }
+          else {
+            std::vector<uint32_t> id(m.rows);
+            for (uint32_t i = 0; i < m.rows; ++i) id[i] = i;
+            VCLGB_CUDA(cudaMemcpyAsync(dst, id.data(), id.size() * 4, cudaMemcpyHostToDevice, be->stream));
+            VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+            return;
+          }
+        }
+        break;
+      case VCLGB_HYB: {
+        size_t t = m.tail_nnz ? m.tail_nnz : 1;
+        if (which == 0) { src = m.ell_coords.ptr; bytes = (size_t)m.rows * m.ell_width * 4; }
+        else if (which == 1) { src = m.ell_elems.ptr; bytes = (size_t)m.rows * m.ell_width * vs; }
+        else if (which == 2) { src = m.tail_rp.ptr; bytes = ((size_t)m.rows + 1) * 4; }
+        else if (which == 3) { src = m.tail_ci.ptr; bytes = t * 4; }
+        else if (which == 4) { src = m.tail_v.ptr; bytes = t * vs; }
+        break;
+      }
+    }
+    require(which >= 0 && (src != nullptr || bytes == 0) && which <= 4, VCLGB_INVALID_ARGUMENT,
+            "no such array for this format");
+    if (bytes)
+      VCLGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, be->stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+  });
+}
+
+VCLGB_API vclgbStatus vclgbSpmv(vclgbBackend h, vclgbMatrix A, double alpha, const void *x,
+                                int64_t xs, int64_t xinc, double beta, void *y, int64_t ys,
+                                int64_t yinc) {
+  if (!h || !A) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    Matrix &m = *M(A);
+    require(m.rows == 0 || (x && y), VCLGB_INVALID_ARGUMENT, "x or y is NULL");
+    if (m.rows == 0) return;
+    Reduction red{be->red_partials.ptr, be->red_counter.as<unsigned>()};
+    DevBuf hyb;
+    if (m.format == VCLGB_HYB && m.tail_nnz) hyb.alloc(hyb_scratch_bytes(m), be->stream);
+    if (m.prec == VCLGB_FLOAT64) {
+      EpiAxpby<double> e{alpha, beta, static_cast<double *>(y), ys, yinc};
+      spmv_launch<double>(*be, m, static_cast<const double *>(x), xs, xinc, e, red,
+                          static_cast<double *>(y), ys, yinc, alpha, beta, nullptr, hyb.ptr);
+    } else {
+      EpiAxpby<float> e{(float)alpha, (float)beta, static_cast<float *>(y), ys, yinc};
+      spmv_launch<float>(*be, m, static_cast<const float *>(x), xs, xinc, e, red,
+                         static_cast<float *>(y), ys, yinc, (float)alpha, (float)beta, nullptr,
+                         hyb.ptr);
+    }
+  });
+}
+
+VCLGB_API vclgbStatus vclgbDot(vclgbBackend h, vclgbPrecision prec, uint64_t n, const void *x,
+                               int64_t xs, int64_t xinc, const void *y, int64_t ys, int64_t yinc,
+                               void *d_result) {
+  if (!h || !d_result) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { dot_launch(*be, prec, n, x, xs, xinc, y, ys, yinc, d_result, false); });
+}
+
+VCLGB_API vclgbStatus vclgbNorm2(vclgbBackend h, vclgbPrecision prec, uint64_t n, const void *x,
+                                 int64_t xs, int64_t xinc, void *d_result) {
+  if (!h || !d_result) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { dot_launch(*be, prec, n, x, xs, xinc, x, xs, xinc, d_result, true); });
+}
+
+// ---------------------------------------------------------------------------
+VCLGB_API vclgbStatus vclgbJacobiCreate(vclgbBackend h, vclgbMatrix A, vclgbPrecond *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    auto P = jacobi_create(*be, *M(A));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbPrecond>(P.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbIlu0Create(vclgbBackend h, vclgbMatrix A, int lvl, vclgbPrecond *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    auto P = ilu0_create(*be, *M(A), lvl != 0);
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbPrecond>(P.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbPrecondApply(vclgbBackend h, vclgbPrecond P, void *vec) {
+  if (!h || !P || !vec) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { precond_apply(*be, *vclgb::P(P), vec, nullptr); });
+}
+
+VCLGB_API vclgbStatus vclgbPrecondDestroy(vclgbPrecond *p) {
+  if (!p || !*p) return VCLGB_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  delete vclgb::P(*p);
+  *p = nullptr;
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbIlu0GetInfo(vclgbPrecond p, vclgbIlu0Info *info) {
+  if (!p || !info || vclgb::P(p)->kind != 2) return VCLGB_INVALID_ARGUMENT;
+  const Precond &P = *vclgb::P(p);
+  info->num_levels_L = P.L.levels;
+  info->num_levels_U = P.U.levels;
+  info->rows_L = P.L.rows;
+  info->rows_U = P.U.rows;
+  info->nnz_L = P.L.nnz;
+  info->nnz_U = P.U.nnz;
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbIlu0Export(vclgbBackend h, vclgbPrecond p, int which, void *dst) {
+  if (!h || !p || !dst) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    const Precond &P = *vclgb::P(p);
+    require(P.kind == 2, VCLGB_INVALID_ARGUMENT, "not an ILU0 preconditioner");
+    size_t vs = P.prec == VCLGB_FLOAT64 ? 8 : 4;
+    const void *src = nullptr;
+    size_t bytes = 0;
+    const Precond::Tri &t = which >= 7 ? P.U : P.L;
+    int w = which >= 7 ? which - 5 : which;
+    switch (w) {
+      case 0: src = P.lu.ptr; bytes = P.nnz * vs; break;
+      case 1: src = P.diag.ptr; bytes = (size_t)P.rows * vs; break;
+      case 2: src = t.level_ptr.ptr; bytes = ((size_t)t.levels + 1) * 4; break;
+      case 3: src = t.row_index.ptr; bytes = t.rows * 4; break;
+      case 4: src = t.row_ptr.ptr; bytes = (t.rows + 1) * 4; break;
+      case 5: src = t.cols.ptr; bytes = t.nnz * 4; break;
+      case 6: src = t.vals.ptr; bytes = t.nnz * vs; break;
+      default: throw Error(VCLGB_INVALID_ARGUMENT, "no such ILU0 array");
+    }
+    if (bytes) VCLGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, be->stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+  });
+}
+
+// ---------------------------------------------------------------------------
+VCLGB_API void vclgbSolverTagInit(vclgbSolverTag *t, int kind) {
+  if (!t) return;
+  std::memset(t, 0, sizeof(*t));
+  if (kind == 1) { t->tol = 1e-8; t->max_iters = 400; t->max_iters_before_restart = 200; }
+  else if (kind == 2) { t->tol = 1e-10; t->max_iters = 300; t->krylov_dim = 20; }
+  else { t->tol = 1e-8; t->max_iters = 300; }
+}
+
+VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
+                                   vclgbSolverTag *tag, vclgbPrecond P) {
+  return solve_entry(h, A, b, x, tag, [&](Backend &be, Matrix &m) {
+    if (m.prec == VCLGB_FLOAT64)
+      cg_solve<double>(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag,
+                       P ? vclgb::P(P) : nullptr);
+    else
+      cg_solve<float>(be, m, static_cast<const float *>(b), static_cast<float *>(x), tag,
+                      P ? vclgb::P(P) : nullptr);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
+                                         vclgbSolverTag *tag, vclgbPrecond P) {
+  return solve_entry(h, A, b, x, tag, [&](Backend &be, Matrix &m) {
+    if (m.prec == VCLGB_FLOAT64)
+      bicgstab_solve<double>(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag,
+                             P ? vclgb::P(P) : nullptr);
+    else
+      bicgstab_solve<float>(be, m, static_cast<const float *>(b), static_cast<float *>(x), tag,
+                            P ? vclgb::P(P) : nullptr);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbSolveGMRES(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
+                                      vclgbSolverTag *tag) {
+  return solve_entry(h, A, b, x, tag, [&](Backend &be, Matrix &m) {
+    if (m.prec == VCLGB_FLOAT64)
+      gmres_solve<double>(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag);
+    else
+      gmres_solve<float>(be, m, static_cast<const float *>(b), static_cast<float *>(x), tag);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbSolveMixedCG(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
+                                        vclgbSolverTag *tag, float inner_tol) {
+  return solve_entry(h, A, b, x, tag, [&](Backend &be, Matrix &m) {
+    require(m.prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "mixed CG takes an FP64 matrix");
+    mixed_cg_solve(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag, inner_tol);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbSolveRefinedCG(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
+                                          vclgbSolverTag *tag, double inner_tol,
+                                          uint32_t max_outer, uint32_t *outer_iters) {
+  return solve_entry(h, A, b, x, tag, [&](Backend &be, Matrix &m) {
+    require(m.prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "refined CG takes an FP64 matrix");
+    refined_cg_solve(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag,
+                     inner_tol, max_outer, outer_iters);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,657 @@
+// formats.cu -- CSR validation and row-length analysis, and the GPU conversions
+// CSR -> ELL / SELL-C-sigma / HYB.  The reference performs these conversions on
+// the host inside viennacl::copy (ell_matrix.hpp:123-171,
+// sliced_ell_matrix.hpp:140-214, hyb_matrix.hpp:135-234); here every pass is a
+// device kernel and the results are bit-identical to the reference layout.
+#include <algorithm>
+#include <cmath>
+
+#include "formats.hpp"
+
+namespace vclgb {
+
+// ---------------------------------------------------------------------------
+// device-wide exclusive scan (u32 in, u64 out), three passes
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <typename In>
+__global__ void scan_tile_sums(const In *__restrict__ in, size_t n, uint64_t *tile_sums) {
+  __shared__ uint64_t sm[kScanThreads / 32];
+  size_t base = (size_t)blockIdx.x * kScanTile;
+  uint64_t s = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    size_t k = base + (size_t)i * kScanThreads + threadIdx.x;
+    if (k < n) s += in[k];
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += sm[w];
+    tile_sums[blockIdx.x] = t;
+  }
+}
+
+// single block: exclusive scan of the tile sums in place, total at [ntiles]
+__global__ void scan_tile_offsets(uint64_t *tile_sums, size_t ntiles) {
+  __shared__ uint64_t sm[1024];
+  uint64_t carry = 0;
+  for (size_t base = 0; base < ntiles; base += blockDim.x) {
+    size_t k = base + threadIdx.x;
+    uint64_t v = k < ntiles ? tile_sums[k] : 0;
+    sm[threadIdx.x] = v;
+    __syncthreads();
+    for (unsigned o = 1; o < blockDim.x; o <<= 1) {
+      uint64_t t = threadIdx.x >= o ? sm[threadIdx.x - o] : 0;
+      __syncthreads();
+      sm[threadIdx.x] += t;
+      __syncthreads();
+    }
+    uint64_t incl = sm[threadIdx.x];
+    if (k < ntiles) tile_sums[k] = carry + incl - v;
+    uint64_t tot = sm[blockDim.x - 1];
+    __syncthreads();
+    carry += tot;
+  }
+  if (threadIdx.x == 0) tile_sums[ntiles] = carry;
+}
+
+template <typename In, typename Out>
+__global__ void scan_tiles(const In *__restrict__ in, size_t n, const uint64_t *tile_offsets,
+                           Out *out) {
+  __shared__ uint64_t sm[kScanTile];
+  size_t base = (size_t)blockIdx.x * kScanTile;
+  for (int i = 0; i < kScanItems; ++i) {
+    size_t k = base + (size_t)i * kScanThreads + threadIdx.x;
+    sm[i * kScanThreads + threadIdx.x] = k < n ? (uint64_t)in[k] : 0;
+  }
+  __syncthreads();
+  // each thread scans kScanItems consecutive values
+  uint64_t loc[kScanItems], s = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    loc[i] = s;
+    s += sm[threadIdx.x * kScanItems + i];
+  }
+  __shared__ uint64_t ts[kScanThreads];
+  ts[threadIdx.x] = s;
+  __syncthreads();
+  for (unsigned o = 1; o < kScanThreads; o <<= 1) {
+    uint64_t t = threadIdx.x >= o ? ts[threadIdx.x - o] : 0;
+    __syncthreads();
+    ts[threadIdx.x] += t;
+    __syncthreads();
+  }
+  uint64_t pre = ts[threadIdx.x] - s + tile_offsets[blockIdx.x];
+  for (int i = 0; i < kScanItems; ++i) {
+    size_t k = base + (size_t)threadIdx.x * kScanItems + i;
+    if (k < n) out[k] = (Out)(pre + loc[i]);
+  }
+}
+
+// out[0..n) = exclusive scan of in, out[n] = total (out must hold n+1); returns total
+template <typename In, typename Out>
+uint64_t exclusive_scan(Backend &be, const In *in, size_t n, Out *out) {
+  size_t ntiles = (n + kScanTile - 1) / kScanTile;
+  if (ntiles == 0) ntiles = 1;
+  DevBuf tiles((ntiles + 1) * sizeof(uint64_t), be.stream);
+  scan_tile_sums<In><<<(unsigned)ntiles, kScanThreads, 0, be.stream>>>(in, n, tiles.as<uint64_t>());
+  scan_tile_offsets<<<1, 1024, 0, be.stream>>>(tiles.as<uint64_t>(), ntiles);
+  scan_tiles<In, Out><<<(unsigned)ntiles, kScanThreads, 0, be.stream>>>(in, n, tiles.as<uint64_t>(), out);
+  be.launches += 3;
+  VCLGB_CHECK_LAUNCH();
+  uint64_t total = 0;
+  VCLGB_CUDA(cudaMemcpyAsync(&total, tiles.as<uint64_t>() + ntiles, sizeof(uint64_t),
+                             cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  Out last = (Out)total;
+  VCLGB_CUDA(cudaMemcpyAsync(out + n, &last, sizeof(Out), cudaMemcpyHostToDevice, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  return total;
+}
+
+// ---------------------------------------------------------------------------
+// validation
+// ---------------------------------------------------------------------------
+__global__ void csr_validate_kernel(uint32_t rows, uint32_t cols, uint32_t nnz,
+                                    const uint32_t *__restrict__ rp,
+                                    const uint32_t *__restrict__ ci, unsigned *bad) {
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0 && (rp[0] != 0 || rp[rows] != nnz)) atomicOr(bad, 1u);
+  for (size_t r = t; r < rows; r += stride)
+    if (rp[r + 1] < rp[r]) atomicOr(bad, 2u);
+  for (size_t k = t; k < nnz; k += stride)
+    if (ci[k] >= cols) atomicOr(bad, 4u);
+}
+
+void csr_validate(Backend &be, const Matrix &m) {
+  DevBuf flag(sizeof(unsigned), be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), be.stream));
+  int g = waves_grid(be, 256, 8, std::max<size_t>(m.rows, m.nnz));
+  csr_validate_kernel<<<g, 256, 0, be.stream>>>(m.rows, m.cols, (uint32_t)m.nnz, m.row_ptr,
+                                                m.col_idx, flag.as<unsigned>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  unsigned h = 0;
+  VCLGB_CUDA(cudaMemcpyAsync(&h, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  if (h & 1) throw Error(VCLGB_INVALID_MATRIX, "row_ptr[0] != 0 or row_ptr[rows] != nnz");
+  if (h & 2) throw Error(VCLGB_INVALID_MATRIX, "row_ptr is not monotone");
+  if (h & 4) throw Error(VCLGB_INVALID_MATRIX, "column index out of range");
+}
+
+// ---------------------------------------------------------------------------
+// row-length analysis for the adaptive CSR kernel
+// ---------------------------------------------------------------------------
+// bin of a row: 0..5 = 1,2,4,8,16,32 lanes per row, 6 = one block per row
+__device__ __host__ inline int lane_bin(uint32_t len) {
+  if (len <= 1) return 0;
+  if (len <= 2) return 1;
+  if (len <= 4) return 2;
+  if (len <= 8) return 3;
+  if (len <= 16) return 4;
+  if (len <= 1024) return 5;
+  return 6;
+}
+constexpr int kLaneBins = 7;
+constexpr uint32_t kBinLanes[kLaneBins] = {1, 2, 4, 8, 16, 32, 0};
+
+constexpr int kPartThreads = 256;
+constexpr int kPartRows = 2048;  // rows per partition tile
+
+__global__ void row_stats_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                 unsigned long long *stats /* [kLaneBins] counts, max, min */) {
+  __shared__ unsigned cnt[kLaneBins];
+  __shared__ unsigned mx, mn;
+  if (threadIdx.x < kLaneBins) cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) { mx = 0; mn = 0xffffffffu; }
+  __syncthreads();
+  unsigned lmx = 0, lmn = 0xffffffffu;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    uint32_t len = rp[r + 1] - rp[r];
+    atomicAdd(&cnt[lane_bin(len)], 1u);
+    lmx = max(lmx, len);
+    lmn = min(lmn, len);
+  }
+  atomicMax(&mx, lmx);
+  atomicMin(&mn, lmn);
+  __syncthreads();
+  if (threadIdx.x < kLaneBins) atomicAdd(&stats[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+  if (threadIdx.x == 0) {
+    atomicMax(&stats[kLaneBins], (unsigned long long)mx);
+    atomicMin(&stats[kLaneBins + 1], (unsigned long long)mn);
+  }
+}
+
+// stable partition of the rows by bin: per-tile counts, scan, scatter
+__global__ void part_count_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                  uint32_t *tile_counts /* [kLaneBins][ntiles] */, size_t ntiles) {
+  __shared__ unsigned cnt[kLaneBins];
+  if (threadIdx.x < kLaneBins) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  size_t r0 = (size_t)blockIdx.x * kPartRows;
+  for (size_t r = r0 + threadIdx.x; r < r0 + kPartRows && r < rows; r += blockDim.x)
+    atomicAdd(&cnt[lane_bin(rp[r + 1] - rp[r])], 1u);
+  __syncthreads();
+  if (threadIdx.x < kLaneBins) tile_counts[threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void part_scatter_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                    const uint64_t *__restrict__ tile_offsets /* scanned */,
+                                    size_t ntiles, uint32_t *out) {
+  // one warp-synchronous pass per 256 rows keeps the order stable
+  __shared__ unsigned base[kLaneBins];
+  __shared__ unsigned wcnt[kLaneBins][kPartThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < kLaneBins) base[threadIdx.x] = (unsigned)tile_offsets[threadIdx.x * ntiles + blockIdx.x];
+  __syncthreads();
+  size_t r0 = (size_t)blockIdx.x * kPartRows;
+  for (size_t c = r0; c < r0 + kPartRows && c < rows; c += blockDim.x) {
+    size_t r = c + threadIdx.x;
+    bool ok = r < rows && r < r0 + kPartRows;
+    int b = ok ? lane_bin(rp[r + 1] - rp[r]) : -1;
+    unsigned my_rank = 0;
+    for (int q = 0; q < kLaneBins; ++q) {
+      unsigned m = __ballot_sync(0xffffffffu, b == q);
+      if (b == q) my_rank = __popc(m & ((1u << lane) - 1u));
+      if (lane == 0) wcnt[q][warp] = __popc(m);
+    }
+    __syncthreads();
+    if (ok) {
+      unsigned off = base[b];
+      for (int w = 0; w < warp; ++w) off += wcnt[b][w];
+      out[off + my_rank] = (uint32_t)r;
+    }
+    __syncthreads();
+    if (threadIdx.x < kLaneBins) {
+      unsigned t = 0;
+      for (int w = 0; w < kPartThreads / 32; ++w) t += wcnt[threadIdx.x][w];
+      base[threadIdx.x] += t;
+    }
+    __syncthreads();
+  }
+}
+
+void csr_analyse(Backend &be, Matrix &m) {
+  DevBuf stats((kLaneBins + 2) * sizeof(unsigned long long), be.stream);
+  unsigned long long init[kLaneBins + 2] = {0};
+  init[kLaneBins + 1] = ~0ull;
+  VCLGB_CUDA(cudaMemcpyAsync(stats.ptr, init, sizeof(init), cudaMemcpyHostToDevice, be.stream));
+  int g = waves_grid(be, 256, 8, m.rows);
+  row_stats_kernel<<<g, 256, 0, be.stream>>>(m.rows, m.row_ptr, stats.as<unsigned long long>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  unsigned long long h[kLaneBins + 2];
+  VCLGB_CUDA(cudaMemcpyAsync(h, stats.ptr, sizeof(h), cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  uint32_t maxlen = m.rows ? (uint32_t)h[kLaneBins] : 0;
+  m.max_row_len = maxlen;
+  double avg = m.rows ? (double)m.nnz / m.rows : 0.0;
+  m.num_bins = 0;
+  if (m.rows == 0) return;
+  // near-uniform rows (stencils): one bin over all rows in order, no row list
+  if (maxlen <= 1024 && (double)maxlen <= 2.0 * avg + 1.0) {
+    CsrBin b;
+    b.lanes = kBinLanes[lane_bin(maxlen)];
+    b.count = m.rows;
+    b.offset = 0;
+    b.identity = 1;
+    m.bins[0] = b;
+    m.num_bins = 1;
+    return;
+  }
+  size_t ntiles = (m.rows + kPartRows - 1) / kPartRows;
+  DevBuf counts(kLaneBins * ntiles * sizeof(uint32_t), be.stream);
+  DevBuf offs((kLaneBins * ntiles + 1) * sizeof(uint64_t), be.stream);
+  part_count_kernel<<<(unsigned)ntiles, kPartThreads, 0, be.stream>>>(m.rows, m.row_ptr,
+                                                                     counts.as<uint32_t>(), ntiles);
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  exclusive_scan<uint32_t, uint64_t>(be, counts.as<uint32_t>(), kLaneBins * ntiles,
+                                     offs.as<uint64_t>());
+  m.bin_rows.alloc((size_t)m.rows * sizeof(uint32_t), be.stream);
+  part_scatter_kernel<<<(unsigned)ntiles, kPartThreads, 0, be.stream>>>(
+      m.rows, m.row_ptr, offs.as<uint64_t>(), ntiles, m.bin_rows.as<uint32_t>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  uint64_t off = 0;
+  for (int q = 0; q < kLaneBins; ++q) {
+    if (h[q] == 0) continue;
+    CsrBin b;
+    b.lanes = kBinLanes[q];
+    b.count = (uint32_t)h[q];
+    b.offset = (uint32_t)off;
+    b.identity = 0;
+    m.bins[m.num_bins++] = b;
+    off += h[q];
+  }
+  // the longest rows first: their blocks start while the short-row bins stream
+  std::reverse(m.bins, m.bins + m.num_bins);
+}
+
+// ---------------------------------------------------------------------------
+// reference CSR-adaptive row blocks (compressed_matrix.hpp:1152-1188), built
+// like the reference from row_ptr on the host; only exported for inspection.
+// ---------------------------------------------------------------------------
+void csr_row_blocks(Backend &be, Matrix &m) {
+  if (m.row_blocks_built) return;
+  std::vector<uint32_t> rp(m.rows + 1);
+  VCLGB_CUDA(cudaMemcpyAsync(rp.data(), m.row_ptr, rp.size() * sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  std::vector<uint32_t> blocks(m.rows + 1);
+  size_t num = 0, count = 0;
+  blocks[0] = 0;
+  for (long i = 0; i < (long)m.rows; ++i) {
+    count += rp[i + 1] - rp[i];
+    if (count > 1024) {
+      if ((size_t)i - blocks[num] > 0) {
+        blocks[++num] = (uint32_t)i;
+        --i;
+      } else {
+        blocks[++num] = (uint32_t)(i + 1);
+      }
+      count = 0;
+    }
+  }
+  if (count > 0) blocks[++num] = m.rows;
+  m.num_row_blocks = (uint32_t)num;
+  m.row_blocks.alloc((num + 1) * sizeof(uint32_t), be.stream);
+  VCLGB_CUDA(cudaMemcpyAsync(m.row_blocks.ptr, blocks.data(), (num + 1) * sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  m.row_blocks_built = true;
+}
+
+// ---------------------------------------------------------------------------
+// ELL / HYB-ELL fill: thread per row writes slots j*rows + row (coalesced in j)
+// ---------------------------------------------------------------------------
+template <typename W>
+__global__ void ell_fill_kernel(uint32_t rows, uint32_t width, const uint32_t *__restrict__ rp,
+                                const uint32_t *__restrict__ ci, const W *__restrict__ v,
+                                uint32_t *coords, W *elems) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    uint32_t s = rp[r], e = rp[r + 1];
+    uint32_t len = e - s < width ? e - s : width;
+    for (uint32_t j = 0; j < len; ++j) {
+      size_t off = (size_t)j * rows + r;
+      coords[off] = ci[s + j];
+      elems[off] = v[s + j];
+    }
+  }
+}
+
+template <typename W>
+static void ell_fill(Backend &be, const Matrix &src, uint32_t width, Matrix &dst) {
+  size_t slots = (size_t)src.rows * width;
+  dst.ell_coords.alloc(std::max<size_t>(slots, 1) * sizeof(uint32_t), be.stream);
+  dst.ell_elems.alloc(std::max<size_t>(slots, 1) * sizeof(W), be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(dst.ell_coords.ptr, 0, dst.ell_coords.bytes, be.stream));
+  VCLGB_CUDA(cudaMemsetAsync(dst.ell_elems.ptr, 0, dst.ell_elems.bytes, be.stream));
+  if (slots) {
+    int g = waves_grid(be, 256, 8, src.rows);
+    ell_fill_kernel<W><<<g, 256, 0, be.stream>>>(src.rows, width, src.row_ptr, src.col_idx,
+                                                 static_cast<const W *>(src.values),
+                                                 dst.ell_coords.as<uint32_t>(),
+                                                 dst.ell_elems.as<W>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+  }
+}
+
+static void copy_header(const Matrix &src, Matrix &dst, vclgbFormat f) {
+  dst.format = f;
+  dst.prec = src.prec;
+  dst.rows = src.rows;
+  dst.cols = src.cols;
+  dst.nnz = src.nnz;
+}
+
+std::unique_ptr<Matrix> convert_ell(Backend &be, const Matrix &csr) {
+  require(csr.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "conversion source must be CSR");
+  auto out = std::make_unique<Matrix>();
+  copy_header(csr, *out, VCLGB_ELL);
+  out->ell_width = csr.max_row_len;
+  if (csr.prec == VCLGB_FLOAT64)
+    ell_fill<uint64_t>(be, csr, out->ell_width, *out);
+  else
+    ell_fill<uint32_t>(be, csr, out->ell_width, *out);
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// SELL-C-sigma
+// ---------------------------------------------------------------------------
+// one block per window of sigma rows: rank = stable position in decreasing length
+__global__ void sell_sort_kernel(uint32_t rows, uint32_t sigma, const uint32_t *__restrict__ rp,
+                                 uint32_t *perm) {
+  extern __shared__ uint32_t lens[];
+  size_t w0 = (size_t)blockIdx.x * sigma;
+  uint32_t wn = (uint32_t)min((size_t)sigma, (size_t)rows - w0);
+  for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) lens[i] = rp[w0 + i + 1] - rp[w0 + i];
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) {
+    uint32_t li = lens[i], rank = 0;
+    for (uint32_t j = 0; j < wn; ++j) {
+      uint32_t lj = lens[j];
+      rank += (lj > li) || (lj == li && j < i);
+    }
+    perm[w0 + rank] = (uint32_t)(w0 + i);
+  }
+}
+
+__global__ void sell_width_kernel(uint32_t rows, uint32_t C, uint32_t nslices,
+                                  const uint32_t *__restrict__ rp,
+                                  const uint32_t *__restrict__ perm, uint32_t *cpb,
+                                  uint32_t *slots /* cpb*C, for the scan */) {
+  for (size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x; s < nslices;
+       s += (size_t)gridDim.x * blockDim.x) {
+    uint32_t w = 0;
+    for (uint32_t l = 0; l < C; ++l) {
+      size_t pos = s * C + l;
+      if (pos >= rows) break;
+      uint32_t r = perm ? perm[pos] : (uint32_t)pos;
+      w = max(w, rp[r + 1] - rp[r]);
+    }
+    cpb[s] = w;
+    slots[s] = w * C;
+  }
+}
+
+template <typename W>
+__global__ void sell_fill_kernel(uint32_t rows, uint32_t C, const uint32_t *__restrict__ rp,
+                                 const uint32_t *__restrict__ ci, const W *__restrict__ v,
+                                 const uint32_t *__restrict__ perm,
+                                 const uint32_t *__restrict__ start, uint32_t *cols, W *elems) {
+  for (size_t pos = (size_t)blockIdx.x * blockDim.x + threadIdx.x; pos < rows;
+       pos += (size_t)gridDim.x * blockDim.x) {
+    uint32_t s = (uint32_t)(pos / C), l = (uint32_t)(pos % C);
+    uint32_t r = perm ? perm[pos] : (uint32_t)pos;
+    uint32_t b = rp[r], e = rp[r + 1];
+    size_t base = (size_t)start[s] + l;
+    for (uint32_t j = 0; b + j < e; ++j) {
+      cols[base + (size_t)j * C] = ci[b + j];
+      elems[base + (size_t)j * C] = v[b + j];
+    }
+  }
+}
+
+std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C, uint32_t sigma) {
+  require(csr.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "conversion source must be CSR");
+  if (C == 0) C = 32;  // sliced_ell_matrix.hpp:146-147 default
+  if (sigma == 0) sigma = 1;
+  require(sigma <= 8192, VCLGB_INVALID_ARGUMENT, "sigma must be <= 8192");
+  auto out = std::make_unique<Matrix>();
+  copy_header(csr, *out, VCLGB_SELL);
+  out->C = C;
+  out->sigma = sigma;
+  uint32_t rows = csr.rows;
+  if (rows == 0) return out;
+  uint32_t nslices = (rows - 1) / C + 1;
+  out->num_slices = nslices;
+  const uint32_t *perm = nullptr;
+  if (sigma > 1) {
+    out->sell_perm.alloc((size_t)rows * sizeof(uint32_t), be.stream);
+    uint32_t nwin = (rows + sigma - 1) / sigma;
+    sell_sort_kernel<<<nwin, 256, sigma * sizeof(uint32_t), be.stream>>>(
+        rows, sigma, csr.row_ptr, out->sell_perm.as<uint32_t>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+    perm = out->sell_perm.as<uint32_t>();
+  }
+  out->sell_cpb.alloc((size_t)nslices * sizeof(uint32_t), be.stream);
+  out->sell_start.alloc(((size_t)nslices + 1) * sizeof(uint32_t), be.stream);
+  DevBuf slots((size_t)nslices * sizeof(uint32_t), be.stream);
+  int g = waves_grid(be, 256, 8, nslices);
+  sell_width_kernel<<<g, 256, 0, be.stream>>>(rows, C, nslices, csr.row_ptr, perm,
+                                              out->sell_cpb.as<uint32_t>(), slots.as<uint32_t>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  DevBuf start64(((size_t)nslices + 1) * sizeof(uint64_t), be.stream);
+  uint64_t total = exclusive_scan<uint32_t, uint64_t>(be, slots.as<uint32_t>(), nslices,
+                                                      start64.as<uint64_t>());
+  require(total < (1ull << 32), VCLGB_INVALID_ARGUMENT,
+          "SELL storage exceeds the 32-bit block_start of sliced_ell_matrix");
+  // narrow to u32 block_start (the reference IndexT)
+  exclusive_scan<uint32_t, uint32_t>(be, slots.as<uint32_t>(), nslices,
+                                     out->sell_start.as<uint32_t>());
+  out->sell_stored = total;
+  size_t vs = csr.vsize();
+  out->sell_cols.alloc(std::max<uint64_t>(total, 1) * sizeof(uint32_t), be.stream);
+  out->sell_elems.alloc(std::max<uint64_t>(total, 1) * vs, be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(out->sell_cols.ptr, 0, out->sell_cols.bytes, be.stream));
+  VCLGB_CUDA(cudaMemsetAsync(out->sell_elems.ptr, 0, out->sell_elems.bytes, be.stream));
+  int g2 = waves_grid(be, 256, 8, rows);
+  if (vs == 8)
+    sell_fill_kernel<uint64_t><<<g2, 256, 0, be.stream>>>(
+        rows, C, csr.row_ptr, csr.col_idx, static_cast<const uint64_t *>(csr.values), perm,
+        out->sell_start.as<uint32_t>(), out->sell_cols.as<uint32_t>(),
+        out->sell_elems.as<uint64_t>());
+  else
+    sell_fill_kernel<uint32_t><<<g2, 256, 0, be.stream>>>(
+        rows, C, csr.row_ptr, csr.col_idx, static_cast<const uint32_t *>(csr.values), perm,
+        out->sell_start.as<uint32_t>(), out->sell_cols.as<uint32_t>(),
+        out->sell_elems.as<uint32_t>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// HYB
+// ---------------------------------------------------------------------------
+__global__ void len_hist_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                unsigned long long *hist) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x)
+    atomicAdd(&hist[rp[r + 1] - rp[r]], 1ull);
+}
+
+__global__ void tail_len_kernel(uint32_t rows, uint32_t width, const uint32_t *__restrict__ rp,
+                                uint32_t *tlen) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    uint32_t len = rp[r + 1] - rp[r];
+    tlen[r] = len > width ? len - width : 0;
+  }
+}
+
+template <typename W>
+__global__ void tail_fill_kernel(uint32_t rows, uint32_t width, const uint32_t *__restrict__ rp,
+                                 const uint32_t *__restrict__ ci, const W *__restrict__ v,
+                                 const uint32_t *__restrict__ trp, uint32_t *tci, W *tv,
+                                 uint32_t *trow) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    uint32_t s = rp[r] + width, e = rp[r + 1];
+    uint32_t o = trp[r];
+    for (uint32_t k = s; k < e; ++k, ++o) {
+      tci[o] = ci[k];
+      tv[o] = v[k];
+      trow[o] = (uint32_t)r;
+    }
+  }
+}
+
+std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold) {
+  require(csr.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "conversion source must be CSR");
+  auto out = std::make_unique<Matrix>();
+  copy_header(csr, *out, VCLGB_HYB);
+  uint32_t rows = csr.rows, maxlen = csr.max_row_len;
+  // width rule of hyb_matrix.hpp:146-163, evaluated in the value precision
+  uint32_t width = maxlen;
+  if (rows > 0) {
+    DevBuf hist(((size_t)maxlen + 1) * sizeof(unsigned long long), be.stream);
+    VCLGB_CUDA(cudaMemsetAsync(hist.ptr, 0, hist.bytes, be.stream));
+    int g = waves_grid(be, 256, 8, rows);
+    len_hist_kernel<<<g, 256, 0, be.stream>>>(rows, csr.row_ptr, hist.as<unsigned long long>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+    std::vector<unsigned long long> h(maxlen + 1);
+    VCLGB_CUDA(cudaMemcpyAsync(h.data(), hist.ptr, hist.bytes, cudaMemcpyDeviceToHost, be.stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    unsigned long long sum = 0;
+    for (uint32_t ind = 0; ind <= maxlen; ++ind) {
+      sum += h[ind];
+      bool hit = csr.prec == VCLGB_FLOAT32
+                     ? (float)sum >= (float)threshold * (float)rows
+                     : (double)sum >= threshold * (double)rows;
+      if (hit) { width = ind; break; }
+    }
+  }
+  out->ell_width = width;
+  if (csr.prec == VCLGB_FLOAT64)
+    ell_fill<uint64_t>(be, csr, width, *out);
+  else
+    ell_fill<uint32_t>(be, csr, width, *out);
+  // tail: row_ptr by scan of the per-row overflow, then entries + COO rows
+  out->tail_rp.alloc(((size_t)rows + 1) * sizeof(uint32_t), be.stream);
+  DevBuf tlen(std::max<size_t>(rows, 1) * sizeof(uint32_t), be.stream);
+  uint64_t tnnz = 0;
+  if (rows > 0) {
+    int g = waves_grid(be, 256, 8, rows);
+    tail_len_kernel<<<g, 256, 0, be.stream>>>(rows, width, csr.row_ptr, tlen.as<uint32_t>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+    tnnz = exclusive_scan<uint32_t, uint32_t>(be, tlen.as<uint32_t>(), rows,
+                                              out->tail_rp.as<uint32_t>());
+  } else {
+    VCLGB_CUDA(cudaMemsetAsync(out->tail_rp.ptr, 0, sizeof(uint32_t), be.stream));
+  }
+  out->tail_nnz = tnnz;
+  size_t vs = csr.vsize();
+  size_t cap = std::max<uint64_t>(tnnz, 1);  // empty tail: one placeholder entry (hyb_matrix.hpp:213-217)
+  out->tail_ci.alloc(cap * sizeof(uint32_t), be.stream);
+  out->tail_v.alloc(cap * vs, be.stream);
+  out->tail_row.alloc(cap * sizeof(uint32_t), be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(out->tail_ci.ptr, 0, out->tail_ci.bytes, be.stream));
+  VCLGB_CUDA(cudaMemsetAsync(out->tail_v.ptr, 0, out->tail_v.bytes, be.stream));
+  if (tnnz > 0) {
+    int g = waves_grid(be, 256, 8, rows);
+    if (vs == 8)
+      tail_fill_kernel<uint64_t><<<g, 256, 0, be.stream>>>(
+          rows, width, csr.row_ptr, csr.col_idx, static_cast<const uint64_t *>(csr.values),
+          out->tail_rp.as<uint32_t>(), out->tail_ci.as<uint32_t>(), out->tail_v.as<uint64_t>(),
+          out->tail_row.as<uint32_t>());
+    else
+      tail_fill_kernel<uint32_t><<<g, 256, 0, be.stream>>>(
+          rows, width, csr.row_ptr, csr.col_idx, static_cast<const uint32_t *>(csr.values),
+          out->tail_rp.as<uint32_t>(), out->tail_ci.as<uint32_t>(), out->tail_v.as<uint32_t>(),
+          out->tail_row.as<uint32_t>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 copy (same format, same index arrays shared by value copy)
+// ---------------------------------------------------------------------------
+__global__ void d2f_kernel(size_t n, const double *__restrict__ in, float *out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+static void d2f(Backend &be, size_t n, const void *in, DevBuf &out) {
+  out.alloc(std::max<size_t>(n, 1) * sizeof(float), be.stream);
+  if (!n) return;
+  int g = waves_grid(be, 256, 8, n);
+  d2f_kernel<<<g, 256, 0, be.stream>>>(n, static_cast<const double *>(in), out.as<float>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
+std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m) {
+  require(m.prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "matrix is already FP32");
+  auto out = std::make_unique<Matrix>();
+  copy_header(m, *out, m.format);
+  out->prec = VCLGB_FLOAT32;
+  switch (m.format) {
+    case VCLGB_CSR:
+      out->row_ptr = m.row_ptr;
+      out->col_idx = m.col_idx;
+      d2f(be, m.nnz, m.values, out->own_values);
+      out->values = out->own_values.ptr;
+      out->num_bins = m.num_bins;
+      for (int i = 0; i < m.num_bins; ++i) out->bins[i] = m.bins[i];
+      out->max_row_len = m.max_row_len;
+      if (m.bin_rows.ptr) {
+        out->bin_rows.alloc(m.bin_rows.bytes, be.stream);
+        VCLGB_CUDA(cudaMemcpyAsync(out->bin_rows.ptr, m.bin_rows.ptr, m.bin_rows.bytes,
+                                   cudaMemcpyDeviceToDevice, be.stream));
+      }
+      break;
+    default:
+      throw Error(VCLGB_UNSUPPORTED, "FP32 copies are built from CSR matrices");
+  }
+  return out;
+}
+
+}  // namespace vclgb

@@ -1,0 +1,28 @@
+// formats.hpp -- declarations shared between the engine's translation units.
+#pragma once
+
+#include "vclgb_internal.hpp"
+
+namespace vclgb {
+
+std::unique_ptr<Matrix> convert_ell(Backend &be, const Matrix &csr);
+std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C, uint32_t sigma);
+std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold);
+std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m);
+void csr_row_blocks(Backend &be, Matrix &m);
+
+// preconditioners (precond.cu)
+std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A);
+std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_scheduling);
+// z = M^-1 z in place; skipped on the device when *skip_flag != 0
+void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);
+// diag(A) into a device buffer of the matrix precision; returns 1 in *zero_found
+// if a diagonal entry is zero (host-synchronising)
+void extract_diag(Backend &be, const Matrix &A, DevBuf &out, bool check_zero);
+
+// vector reductions (blas1.cu)
+void dot_launch(Backend &be, vclgbPrecision prec, uint64_t n, const void *x, int64_t xs,
+                int64_t xinc, const void *y, int64_t ys, int64_t yinc, void *d_result,
+                bool sqrt_result);
+
+}  // namespace vclgb

@@ -1,0 +1,400 @@
+// precond.cu -- Jacobi and ILU0 preconditioners.
+//
+// Jacobi: diag(A) by a device kernel (row_info SPARSE_ROW_DIAGONAL,
+// linalg/cuda/sparse_matrix_operations.hpp:53-119); apply z = r / diag is fused
+// into the solvers' update kernels.
+//
+// ILU0 (linalg/detail/ilu/ilu0.hpp): the elimination levels of L and U and
+// the per-level substitution lists follow level_scheduling_setup_impl
+// (detail/ilu/common.hpp:50-187) and are built from the pattern on the host,
+// as the reference does; the numeric factorisation then runs on the device,
+// one kernel per L level (rows of one level are independent), with the same
+// per-row IKJ operation order and no fused multiply-add, so the factors are
+// bit-identical to the reference's sequential host loop (ilu0.hpp:77-140).
+// The apply runs one substitution kernel per level
+// (linalg/cuda/misc_operations.hpp:41-83 semantics).
+#include <algorithm>
+#include <map>
+
+#include "formats.hpp"
+#include "vecpass.cuh"
+
+namespace vclgb {
+
+template <typename T>
+__global__ void diag_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                            const uint32_t *__restrict__ ci, const T *__restrict__ v, T *d,
+                            unsigned *zero_found) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    T val = 0;
+    for (uint32_t k = rp[r]; k < rp[r + 1]; ++k)
+      if (ci[k] == r) { val = v[k]; break; }
+    d[r] = val;
+    if (zero_found && val == T(0)) atomicOr(zero_found, 1u);
+  }
+}
+
+void extract_diag(Backend &be, const Matrix &A, DevBuf &out, bool check_zero) {
+  require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "diagonal extraction needs CSR");
+  out.alloc(std::max<size_t>(A.rows, 1) * A.vsize(), be.stream);
+  DevBuf flag(sizeof(unsigned), be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), be.stream));
+  int g = waves_grid(be, 256, 8, A.rows);
+  if (A.prec == VCLGB_FLOAT64)
+    diag_kernel<double><<<g, 256, 0, be.stream>>>(A.rows, A.row_ptr, A.col_idx,
+                                                  static_cast<const double *>(A.values),
+                                                  out.as<double>(), flag.as<unsigned>());
+  else
+    diag_kernel<float><<<g, 256, 0, be.stream>>>(A.rows, A.row_ptr, A.col_idx,
+                                                 static_cast<const float *>(A.values),
+                                                 out.as<float>(), flag.as<unsigned>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  if (check_zero) {
+    unsigned h = 0;
+    VCLGB_CUDA(cudaMemcpyAsync(&h, flag.ptr, sizeof(h), cudaMemcpyDeviceToHost, be.stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    if (h) throw Error(VCLGB_ZERO_ON_DIAGONAL, "zero on diagonal");
+  }
+}
+
+std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A) {
+  require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "jacobi_precond is built from CSR");
+  auto P = std::make_unique<Precond>();
+  P->kind = 1;
+  P->prec = A.prec;
+  P->rows = A.rows;
+  extract_diag(be, A, P->diag, true);
+  return P;
+}
+
+// ---------------------------------------------------------------------------
+// ILU0
+// ---------------------------------------------------------------------------
+// numeric factorisation of the rows of one level (thread per row)
+template <typename T>
+__device__ __forceinline__ T mul_rn(T a, T b);
+template <>
+__device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+template <>
+__device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T sub_rn(T a, T b);
+template <>
+__device__ __forceinline__ double sub_rn<double>(double a, double b) { return __dsub_rn(a, b); }
+template <>
+__device__ __forceinline__ float sub_rn<float>(float a, float b) { return __fsub_rn(a, b); }
+
+template <typename T>
+__global__ void ilu0_level_kernel(uint32_t count, const uint32_t *__restrict__ rows_of_level,
+                                  const uint32_t *__restrict__ rp,
+                                  const uint32_t *__restrict__ ci, T *lu) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t i = rows_of_level[t];
+    const uint32_t ib = rp[i], ie = rp[i + 1];
+    for (uint32_t bk = ib; bk < ie; ++bk) {
+      const uint32_t k = ci[bk];
+      if (k >= i) continue;
+      const uint32_t kb = rp[k], ke = rp[k + 1];
+      T a_kk = 0;
+      for (uint32_t q = kb; q < ke; ++q)
+        if (ci[q] == k) { a_kk = lu[q]; break; }
+      const T a_ik = lu[bk] / a_kk;
+      lu[bk] = a_ik;
+      for (uint32_t bj = ib; bj < ie; ++bj) {
+        const uint32_t j = ci[bj];
+        if (j <= k) continue;
+        T a_kj = 0;
+        for (uint32_t q = kb; q < ke; ++q)
+          if (ci[q] == j) { a_kj = lu[q]; break; }
+        lu[bj] = sub_rn(lu[bj], mul_rn(a_ik, a_kj));
+      }
+    }
+  }
+}
+
+// gather of the level-set values from the factors (U scaled by its diagonal)
+template <typename T>
+__global__ void level_vals_kernel(size_t nnz, const uint32_t *__restrict__ src,
+                                  const uint32_t *__restrict__ row_of_entry,
+                                  const T *__restrict__ lu, const T *__restrict__ udiag,
+                                  T *vals) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (size_t)gridDim.x * blockDim.x) {
+    T v = lu[src[k]];
+    if (udiag) v = v / udiag[row_of_entry[k]];
+    vals[k] = v;
+  }
+}
+
+// one level: vec[row] -= sum vals * vec[cols] (misc_operations.hpp substitute)
+template <typename T>
+__global__ void level_substitute_kernel(uint32_t r0, uint32_t r1,
+                                        const uint32_t *__restrict__ row_index,
+                                        const uint32_t *__restrict__ row_ptr,
+                                        const uint32_t *__restrict__ cols,
+                                        const T *__restrict__ vals, T *vec, const int *skip) {
+  if (skip && *skip) return;
+  for (size_t t = r0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < r1;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t row = row_index[t];
+    T s = vec[row];
+    for (uint32_t j = row_ptr[t]; j < row_ptr[t + 1]; ++j) s -= vec[cols[j]] * vals[j];
+    vec[row] = s;
+  }
+}
+
+template <typename T>
+__global__ void div_kernel(size_t n, T *vec, const T *__restrict__ d, const int *skip) {
+  if (skip && *skip) return;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    vec[i] = vec[i] / d[i];
+}
+
+// level structure of one triangle (host, from the pattern)
+struct LevelPlan {
+  std::vector<uint32_t> level_ptr, row_index, row_ptr, cols, src, row_of_entry;
+};
+
+static LevelPlan plan_levels(uint32_t n, const std::vector<uint32_t> &rp,
+                             const std::vector<uint32_t> &ci, bool upper,
+                             std::vector<uint32_t> *row_level_out) {
+  std::vector<uint32_t> lev(n, 0);
+  uint32_t maxlev = 0;
+  for (uint32_t r2 = 0; r2 < n; ++r2) {
+    uint32_t row = upper ? n - 1 - r2 : r2, e = 0;
+    for (uint32_t k = rp[row]; k < rp[row + 1]; ++k) {
+      uint32_t c = ci[k];
+      if ((!upper && c < row) || (upper && c > row)) e = std::max(e, lev[c]);
+    }
+    lev[row] = e + 1;
+    maxlev = std::max(maxlev, e + 1);
+  }
+  // bucket entries by the level of their column; rows ascending inside a level
+  std::vector<uint64_t> cnt_rows(maxlev + 2, 0), cnt_nnz(maxlev + 2, 0);
+  std::vector<uint32_t> seen(maxlev + 2, 0);
+  for (uint32_t row = 0; row < n; ++row)
+    for (uint32_t k = rp[row]; k < rp[row + 1]; ++k) {
+      uint32_t c = ci[k];
+      if ((!upper && c < row) || (upper && c > row)) {
+        uint32_t e = lev[c];
+        cnt_nnz[e] += 1;
+        if (seen[e] != row + 1) { seen[e] = row + 1; cnt_rows[e] += 1; }
+      }
+    }
+  LevelPlan p;
+  // per-level cursors
+  std::vector<uint64_t> row_off(maxlev + 2, 0), nnz_off(maxlev + 2, 0);
+  uint64_t ro = 0, no = 0;
+  p.level_ptr.push_back(0);
+  std::vector<int64_t> level_slot(maxlev + 2, -1);
+  for (uint32_t e = 1; e <= maxlev; ++e) {
+    if (cnt_rows[e] == 0) continue;
+    level_slot[e] = (int64_t)p.level_ptr.size() - 1;
+    row_off[e] = ro;
+    nnz_off[e] = no;
+    ro += cnt_rows[e];
+    no += cnt_nnz[e];
+    p.level_ptr.push_back((uint32_t)ro);
+  }
+  p.row_index.assign(ro, 0);
+  p.row_ptr.assign(ro + 1, 0);
+  p.cols.assign(no, 0);
+  p.src.assign(no, 0);
+  p.row_of_entry.assign(no, 0);
+  // rows are visited in ascending order, so each level's list stays sorted
+  std::vector<uint64_t> rcur(row_off), ncur(nnz_off);
+  std::fill(seen.begin(), seen.end(), 0);
+  for (uint32_t row = 0; row < n; ++row) {
+    for (uint32_t k = rp[row]; k < rp[row + 1]; ++k) {
+      uint32_t c = ci[k];
+      if (!((!upper && c < row) || (upper && c > row))) continue;
+      uint32_t e = lev[c];
+      if (seen[e] != row + 1) {
+        seen[e] = row + 1;
+        p.row_index[rcur[e]] = row;
+        rcur[e] += 1;
+      }
+      p.cols[ncur[e]] = c;
+      p.src[ncur[e]] = k;
+      p.row_of_entry[ncur[e]] = row;
+      ncur[e] += 1;
+    }
+    (void)level_slot;
+  }
+  // global row_ptr: entries of a level's row are contiguous and in row order
+  {
+    uint64_t pos = 0;
+    for (uint32_t e = 1; e <= maxlev; ++e) {
+      if (cnt_rows[e] == 0) continue;
+      uint64_t r0 = row_off[e], r1 = r0 + cnt_rows[e];
+      uint64_t k = nnz_off[e];
+      for (uint64_t t = r0; t < r1; ++t) {
+        p.row_ptr[t] = (uint32_t)k;
+        uint32_t row = p.row_index[t];
+        while (k < nnz_off[e] + cnt_nnz[e] && p.row_of_entry[k] == row) ++k;
+      }
+      pos = k;
+    }
+    p.row_ptr[ro] = (uint32_t)no;
+    (void)pos;
+  }
+  if (row_level_out) *row_level_out = std::move(lev);
+  return p;
+}
+
+template <typename X>
+static void upload(Backend &be, DevBuf &dst, const std::vector<X> &src) {
+  dst.alloc(std::max<size_t>(src.size(), 1) * sizeof(X), be.stream);
+  if (!src.empty())
+    VCLGB_CUDA(cudaMemcpyAsync(dst.ptr, src.data(), src.size() * sizeof(X),
+                               cudaMemcpyHostToDevice, be.stream));
+}
+
+template <typename T>
+static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
+  const uint32_t n = A.rows;
+  std::vector<uint32_t> rp(n + 1), ci(A.nnz);
+  VCLGB_CUDA(cudaMemcpyAsync(rp.data(), A.row_ptr, rp.size() * 4, cudaMemcpyDeviceToHost, be.stream));
+  if (A.nnz)
+    VCLGB_CUDA(cudaMemcpyAsync(ci.data(), A.col_idx, ci.size() * 4, cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  std::vector<uint32_t> levL;
+  LevelPlan L = plan_levels(n, rp, ci, false, &levL);
+  LevelPlan U = plan_levels(n, rp, ci, true, nullptr);
+
+  // factorisation order: rows grouped by their L level (ascending rows in a level)
+  uint32_t maxlev = 0;
+  for (uint32_t r = 0; r < n; ++r) maxlev = std::max(maxlev, levL[r]);
+  std::vector<uint32_t> lvl_cnt(maxlev + 2, 0);
+  for (uint32_t r = 0; r < n; ++r) lvl_cnt[levL[r]] += 1;
+  std::vector<uint32_t> lvl_off(maxlev + 2, 0);
+  for (uint32_t e = 1; e <= maxlev + 1; ++e) lvl_off[e] = lvl_off[e - 1] + lvl_cnt[e - 1];
+  std::vector<uint32_t> order(n), cur(lvl_off);
+  for (uint32_t r = 0; r < n; ++r) order[cur[levL[r]]++] = r;
+
+  P.lu.alloc(std::max<uint64_t>(A.nnz, 1) * sizeof(T), be.stream);
+  if (A.nnz)
+    VCLGB_CUDA(cudaMemcpyAsync(P.lu.ptr, A.values, A.nnz * sizeof(T), cudaMemcpyDeviceToDevice,
+                               be.stream));
+  DevBuf d_order;
+  upload(be, d_order, order);
+  for (uint32_t e = 1; e <= maxlev; ++e) {
+    uint32_t c = lvl_cnt[e];
+    if (!c) continue;
+    int g = waves_grid(be, 128, 16, c);
+    ilu0_level_kernel<T><<<g, 128, 0, be.stream>>>(c, d_order.as<uint32_t>() + lvl_off[e],
+                                                   A.row_ptr, A.col_idx, P.lu.as<T>());
+    be.launches++;
+  }
+  VCLGB_CHECK_LAUNCH();
+  // U diagonal of the factors
+  {
+    Matrix tmp;
+    tmp.format = VCLGB_CSR;
+    tmp.prec = A.prec;
+    tmp.rows = n;
+    tmp.cols = n;
+    tmp.nnz = A.nnz;
+    tmp.row_ptr = A.row_ptr;
+    tmp.col_idx = A.col_idx;
+    tmp.values = P.lu.ptr;
+    extract_diag(be, tmp, P.diag, false);
+  }
+  auto fill_tri = [&](LevelPlan &pl, Precond::Tri &tri, bool upper) {
+    tri.levels = (uint32_t)(pl.level_ptr.size() - 1);
+    tri.rows = pl.row_index.size();
+    tri.nnz = pl.cols.size();
+    tri.h_level_ptr = pl.level_ptr;
+    upload(be, tri.level_ptr, pl.level_ptr);
+    upload(be, tri.row_index, pl.row_index);
+    upload(be, tri.row_ptr, pl.row_ptr);
+    upload(be, tri.cols, pl.cols);
+    DevBuf src, roe;
+    upload(be, src, pl.src);
+    upload(be, roe, pl.row_of_entry);
+    tri.vals.alloc(std::max<uint64_t>(tri.nnz, 1) * sizeof(T), be.stream);
+    if (tri.nnz) {
+      int g = waves_grid(be, 256, 8, tri.nnz);
+      level_vals_kernel<T><<<g, 256, 0, be.stream>>>(tri.nnz, src.as<uint32_t>(),
+                                                     roe.as<uint32_t>(), P.lu.as<T>(),
+                                                     upper ? P.diag.as<T>() : nullptr,
+                                                     tri.vals.as<T>());
+      be.launches++;
+      VCLGB_CHECK_LAUNCH();
+    }
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // src/roe freed after use
+  };
+  fill_tri(L, P.L, false);
+  fill_tri(U, P.U, true);
+}
+
+std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_scheduling) {
+  require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "ilu0_precond is built from CSR");
+  require(A.rows == A.cols, VCLGB_INVALID_ARGUMENT, "ILU0 needs a square matrix");
+  auto P = std::make_unique<Precond>();
+  P->kind = 2;
+  P->prec = A.prec;
+  P->rows = A.rows;
+  P->nnz = A.nnz;
+  P->row_ptr = A.row_ptr;
+  P->col_idx = A.col_idx;
+  // the device apply is level-scheduled either way: without level scheduling the
+  // reference copies the vector to the host and solves sequentially
+  // (ilu0.hpp:229-236); both orders give the same substitution up to rounding
+  P->level_scheduling = level_scheduling;
+  if (A.prec == VCLGB_FLOAT64)
+    ilu0_build<double>(be, A, *P);
+  else
+    ilu0_build<float>(be, A, *P);
+  return P;
+}
+
+template <typename T>
+static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *skip) {
+  for (uint32_t L = 0; L < tri.levels; ++L) {
+    uint32_t r0 = tri.h_level_ptr[L], r1 = tri.h_level_ptr[L + 1];
+    int g = waves_grid(be, 128, 16, r1 - r0);
+    level_substitute_kernel<T><<<g, 128, 0, be.stream>>>(
+        r0, r1, tri.row_index.as<uint32_t>(), tri.row_ptr.as<uint32_t>(), tri.cols.as<uint32_t>(),
+        tri.vals.as<T>(), vec, skip);
+    be.launches++;
+  }
+  VCLGB_CHECK_LAUNCH();
+}
+
+void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag) {
+  if (P.kind == 1) {
+    int g = waves_grid(be, 256, 8, P.rows);
+    if (P.prec == VCLGB_FLOAT64)
+      div_kernel<double><<<g, 256, 0, be.stream>>>(P.rows, static_cast<double *>(d_vec),
+                                                   P.diag.as<double>(), skip_flag);
+    else
+      div_kernel<float><<<g, 256, 0, be.stream>>>(P.rows, static_cast<float *>(d_vec),
+                                                  P.diag.as<float>(), skip_flag);
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+    return;
+  }
+  // ILU0: L levels, divide by the U diagonal, U levels (ilu0.hpp:213-226)
+  int g = waves_grid(be, 256, 8, P.rows);
+  if (P.prec == VCLGB_FLOAT64) {
+    tri_apply<double>(be, P.L, static_cast<double *>(d_vec), skip_flag);
+    div_kernel<double><<<g, 256, 0, be.stream>>>(P.rows, static_cast<double *>(d_vec),
+                                                 P.diag.as<double>(), skip_flag);
+    be.launches++;
+    tri_apply<double>(be, P.U, static_cast<double *>(d_vec), skip_flag);
+  } else {
+    tri_apply<float>(be, P.L, static_cast<float *>(d_vec), skip_flag);
+    div_kernel<float><<<g, 256, 0, be.stream>>>(P.rows, static_cast<float *>(d_vec),
+                                                P.diag.as<float>(), skip_flag);
+    be.launches++;
+    tri_apply<float>(be, P.U, static_cast<float *>(d_vec), skip_flag);
+  }
+  VCLGB_CHECK_LAUNCH();
+}
+
+}  // namespace vclgb

@@ -1,0 +1,1069 @@
+// solvers.cu -- CG, BiCGStab, GMRES and the mixed-precision solvers with every
+// reduction, scalar recurrence and convergence test on the device.
+//
+// Each solver is a fixed sequence of fused kernels per iteration; scalars
+// live in a device state struct written by the last block of the kernel that
+// completes the reduction, and read by the next kernel.  The host only polls
+// the status word every check_every iterations (see run_iterations).
+#include <algorithm>
+#include <cmath>
+
+#include "formats.hpp"
+#include "vecpass.cuh"
+
+namespace vclgb {
+
+template <typename T>
+struct St {
+  T rr, ApAp, pAp, alpha, beta, omega;
+  T nrhs, nrhs2, ip, vnorm2;
+  T Ap_r0, s_s, r_r0, resnorm;
+  double tol, abs_tol, error;
+  unsigned iters, max_iters, last_restart, max_before_restart;
+  int done;
+  int restart;
+  int restart_skip;  // done || !restart (skip flag for the restart kernels)
+};
+
+template <typename T>
+__device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
+
+struct NoScal {};
+
+// ===========================================================================
+// pipelined CG (cg.hpp:128-187; fused kernels as in
+// host_based/iterative_operations.hpp:52-105 and 378-416)
+// ===========================================================================
+template <typename T>
+struct CgInit {
+  static constexpr int NDOT = 1;
+  const T *b; T *x, *r, *p; St<T> *st;
+  __device__ bool skip() const { return false; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T bi = b[i];
+    x[i] = T(0); r[i] = bi; p[i] = bi;
+    d[0] += bi * bi;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    T nrm = sqrt(s[0]);
+    st->nrhs2 = nrm * nrm;  // norm_2(residual)^2 as cg.hpp:149
+    st->rr = st->nrhs2;
+    st->iters = 0;
+    st->error = 0;
+    st->done = (st->nrhs2 <= T(st->abs_tol * st->abs_tol)) ? kConverged : kRunning;
+  }
+};
+
+template <typename T>
+struct EpiCgFirst {  // Ap = A p; alpha = rr/<p,Ap>; beta = (alpha^2 ||Ap||^2 - rr)/rr
+  static constexpr int NDOT = 2;
+  T *Ap; const T *p; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t r, T acc, T (&d)[2]) const {
+    Ap[r] = acc;
+    d[0] += acc * acc;
+    d[1] += p[r] * acc;
+  }
+  __device__ void finalize(const T (&s)[2]) const {
+    T rr = st->rr;
+    T alpha = rr / s[1];
+    T nap = sqrt(s[0]);
+    st->alpha = alpha;
+    st->beta = (alpha * alpha * nap * nap - rr) / rr;
+    if (st->max_iters == 0) {
+      st->done = kMaxIters;
+      st->error = sqrt(fabs((double)rr) / (double)st->nrhs2);
+    }
+  }
+};
+
+template <typename T>
+struct CgUpdate {  // x += a p; r -= a Ap; p = r + b p; <r,r>
+  static constexpr int NDOT = 1;
+  T *x, *p, *r; const T *Ap; St<T> *st;
+  struct S { T a, b; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->alpha, st->beta}; }
+  __device__ void apply(size_t i, S s, T (&d)[1]) const {
+    T vp = p[i], vr = r[i];
+    x[i] += s.a * vp;
+    vr -= s.a * Ap[i];
+    vp = vr + s.b * vp;
+    d[0] += vr * vr;
+    p[i] = vp;
+    r[i] = vr;
+  }
+  __device__ void finalize(const T (&s)[1]) const { st->rr = s[0]; }
+};
+
+template <typename T>
+struct EpiCg {  // Ap = A p, <Ap,Ap>, <p,Ap>; convergence test; next alpha/beta
+  static constexpr int NDOT = 2;
+  T *Ap; const T *p; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t r, T acc, T (&d)[2]) const {
+    Ap[r] = acc;
+    d[0] += acc * acc;
+    d[1] += p[r] * acc;
+  }
+  __device__ void finalize(const T (&s)[2]) const {
+    st->iters += 1;
+    T rr = st->rr;
+    double ratio = fabs((double)rr / (double)st->nrhs2);
+    if (ratio < st->tol * st->tol || fabs((double)rr) < st->abs_tol * st->abs_tol) {
+      st->done = kConverged;
+      st->error = sqrt(fabs((double)rr) / (double)st->nrhs2);
+      return;
+    }
+    T alpha = rr / s[1];
+    T beta = (alpha * alpha * s[0] - rr) / rr;
+    st->alpha = alpha;
+    st->beta = beta;
+    st->error = sqrt(fabs((double)rr) / (double)st->nrhs2);
+    if (!finite_(alpha) || !finite_(beta)) st->done = kBreakdown;
+    else if (st->iters >= st->max_iters) st->done = kMaxIters;
+  }
+};
+
+// ===========================================================================
+// preconditioned CG (cg.hpp:257-322)
+// ===========================================================================
+template <typename T>
+struct PcgInit {  // x = 0; r = b; z = b/d (or z = b); p = z; <r,z>
+  static constexpr int NDOT = 1;
+  const T *b, *dg; T *x, *r, *z, *p; St<T> *st;
+  bool jacobi;
+  __device__ bool skip() const { return false; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T bi = b[i];
+    x[i] = T(0); r[i] = bi;
+    if (jacobi) {
+      T zi = bi / dg[i];
+      p[i] = zi;
+      d[0] += bi * zi;
+    } else {
+      z[i] = bi;
+    }
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->iters = 0;
+    st->error = 0;
+    st->ip = s[0];
+    st->nrhs2 = s[0];
+    st->done = (fabs((double)s[0]) <= st->abs_tol * st->abs_tol) ? kConverged : kRunning;
+    if (st->done == kRunning && st->max_iters == 0) st->done = kMaxIters;
+  }
+};
+
+template <typename T>
+struct PcgInitFinish {  // generic preconditioner: p = z; <r,z>
+  static constexpr int NDOT = 1;
+  const T *r, *z; T *p; St<T> *st;
+  __device__ bool skip() const { return false; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T zi = z[i];
+    p[i] = zi;
+    d[0] += r[i] * zi;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->iters = 0;
+    st->error = 0;
+    st->ip = s[0];
+    st->nrhs2 = s[0];
+    st->done = (fabs((double)s[0]) <= st->abs_tol * st->abs_tol) ? kConverged : kRunning;
+    if (st->done == kRunning && st->max_iters == 0) st->done = kMaxIters;
+  }
+};
+
+template <typename T>
+struct EpiPcg {  // tmp = A p; alpha = ip / <tmp,p>
+  static constexpr int NDOT = 1;
+  T *tmp; const T *p; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t r, T acc, T (&d)[1]) const {
+    tmp[r] = acc;
+    d[0] += acc * p[r];
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->iters += 1;
+    st->alpha = st->ip / s[0];
+    if (!finite_(st->alpha)) st->done = kBreakdown;
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void pcg_check(St<T> *st, T new_ip) {
+  double ratio = (double)new_ip / (double)st->nrhs2;
+  st->error = sqrt(fabs(ratio));
+  if (fabs(ratio) < st->tol * st->tol || fabs((double)new_ip) < st->abs_tol * st->abs_tol) {
+    st->done = kConverged;
+    return;
+  }
+  st->beta = new_ip / st->ip;
+  st->ip = new_ip;
+  if (!finite_(st->beta)) st->done = kBreakdown;
+  else if (st->iters >= st->max_iters) st->done = kMaxIters;
+}
+
+template <typename T>
+struct PcgUpdate {  // x += a p; r -= a tmp; [z = r/d]; <r,z> (Jacobi) / z = r (generic)
+  static constexpr int NDOT = 1;
+  T *x, *r, *z; const T *p, *tmp, *dg; St<T> *st;
+  bool jacobi;
+  struct S { T a; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->alpha}; }
+  __device__ void apply(size_t i, S s, T (&d)[1]) const {
+    T vp = p[i];
+    x[i] += s.a * vp;
+    T vr = r[i] - s.a * tmp[i];
+    r[i] = vr;
+    if (jacobi) d[0] += vr * (vr / dg[i]);
+    else z[i] = vr;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    if (jacobi) pcg_check(st, s[0]);
+  }
+};
+
+template <typename T>
+struct PcgDot {  // generic preconditioner: <r,z> after z = M^-1 r
+  static constexpr int NDOT = 1;
+  const T *r, *z; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const { d[0] += r[i] * z[i]; }
+  __device__ void finalize(const T (&s)[1]) const { pcg_check(st, s[0]); }
+};
+
+template <typename T>
+struct PcgP {  // p = z + beta p, z = r/d (Jacobi) or z (generic)
+  static constexpr int NDOT = 0;
+  T *p; const T *r, *z, *dg; St<T> *st;
+  bool jacobi;
+  struct S { T b; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->beta}; }
+  __device__ void apply(size_t i, S s, T (&)[1]) const {
+    T zi = jacobi ? r[i] / dg[i] : z[i];
+    p[i] = zi + s.b * p[i];
+  }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
+// ===========================================================================
+// pipelined BiCGStab (bicgstab.hpp:96-215, host_based/iterative_operations.hpp:519-627)
+// ===========================================================================
+template <typename T>
+struct BicgInit {
+  static constexpr int NDOT = 1;
+  const T *b; T *x, *r, *p, *r0; St<T> *st;
+  __device__ bool skip() const { return false; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T bi = b[i];
+    x[i] = T(0); r[i] = bi; p[i] = bi; r0[i] = bi;
+    d[0] += bi * bi;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    T nrm = sqrt(s[0]);
+    st->nrhs = nrm;
+    st->resnorm = nrm;
+    st->r_r0 = nrm * nrm;
+    st->iters = 0;
+    st->error = 0;
+    st->done = ((double)nrm <= st->abs_tol) ? kConverged : kRunning;
+    if (st->done == kRunning && st->max_iters == 0) { st->done = kMaxIters; st->error = 1.0; }
+  }
+};
+
+template <typename T>
+struct EpiBicgAp {  // Ap = A p, <Ap, r0*>
+  static constexpr int NDOT = 1;
+  T *Ap; const T *r0; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t r, T acc, T (&d)[1]) const {
+    Ap[r] = acc;
+    d[0] += acc * r0[r];
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->iters += 1;
+    st->Ap_r0 = s[0];
+  }
+};
+
+template <typename T>
+struct BicgS {  // alpha = <r,r0*>/<Ap,r0*>; s = r - alpha Ap; <s,s>
+  static constexpr int NDOT = 1;
+  T *s_; const T *r, *Ap; St<T> *st;
+  struct S { T a; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->r_r0 / st->Ap_r0}; }
+  __device__ void apply(size_t i, S s, T (&d)[1]) const {
+    T v = r[i] - s.a * Ap[i];
+    d[0] += v * v;
+    s_[i] = v;
+  }
+  __device__ void finalize(const T (&s)[1]) const { st->s_s = s[0]; }
+};
+
+template <typename T>
+struct EpiBicgAs {  // As = A s, <As,As>, <s,As>, <As,r0*>; scalars; residual estimate
+  static constexpr int NDOT = 3;
+  T *As; const T *s_, *r0; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t r, T acc, T (&d)[3]) const {
+    As[r] = acc;
+    d[0] += acc * acc;
+    d[1] += s_[r] * acc;
+    d[2] += acc * r0[r];
+  }
+  __device__ void finalize(const T (&s)[3]) const {
+    T alpha = st->r_r0 / st->Ap_r0;
+    T beta = -s[2] / st->Ap_r0;
+    T omega = s[1] / s[0];
+    T rn = sqrt(st->s_s - T(2) * omega * s[1] + omega * omega * s[0]);
+    st->alpha = alpha;
+    st->beta = beta;
+    st->omega = omega;
+    st->resnorm = rn;
+    st->error = (double)rn / (double)st->nrhs;
+    if (fabs((double)rn / (double)st->nrhs) < st->tol || (double)rn < st->abs_tol) {
+      st->done = kConverged;  // leaves before the x update, as bicgstab.hpp:197-198
+    } else if (!finite_(alpha) || !finite_(omega) || !finite_(beta)) {
+      st->done = kBreakdown;
+    }
+  }
+};
+
+template <typename T>
+struct BicgUpdate {  // x += a p + w s; r = s - w As; p = r + b (p - w Ap); <r, r0*>
+  static constexpr int NDOT = 1;
+  T *x, *p, *r; const T *s_, *As, *Ap, *r0; St<T> *st;
+  struct S { T a, w, b; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->alpha, st->omega, st->beta}; }
+  __device__ void apply(size_t i, S c, T (&d)[1]) const {
+    T vp = p[i], vs = s_[i];
+    x[i] += c.a * vp + c.w * vs;
+    T vr = vs - c.w * As[i];
+    vp = vr + c.b * (vp - c.w * Ap[i]);
+    d[0] += vr * r0[i];
+    r[i] = vr;
+    p[i] = vp;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->r_r0 = s[0];
+    if (st->iters >= st->max_iters) st->done = kMaxIters;
+  }
+};
+
+// ===========================================================================
+// preconditioned BiCGStab (bicgstab.hpp:398-489)
+// ===========================================================================
+template <typename T>
+struct GbInit {  // x = 0; ||b||; restart at the first iteration
+  static constexpr int NDOT = 1;
+  const T *b; T *x; St<T> *st;
+  __device__ bool skip() const { return false; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T bi = b[i];
+    x[i] = T(0);
+    d[0] += bi * bi;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    T nrm = sqrt(s[0]);
+    st->nrhs = nrm;
+    st->resnorm = nrm;
+    st->iters = 0;
+    st->error = 0;
+    st->restart = 1;
+    st->done = ((double)nrm <= st->abs_tol) ? kConverged : kRunning;
+    if (st->done == kRunning && st->max_iters == 0) { st->done = kMaxIters; st->error = 1.0; }
+    st->restart_skip = st->done != kRunning;
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void gb_restart_done(St<T> *st, T rr) {
+  T nr = sqrt(rr);
+  st->ip = nr * nr;
+  st->restart = 0;
+  st->restart_skip = 1;
+  st->last_restart = st->iters;
+}
+
+template <typename T>
+struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0* = r; ||r||^2
+  static constexpr int NDOT = 1;
+  T *r, *p, *r0; const T *b, *dg; St<T> *st;
+  bool jacobi;
+  __device__ bool skip() const { return st->restart_skip != 0; }
+  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
+    T v = b[i] - acc;
+    if (jacobi) {
+      v = v / dg[i];
+      p[i] = v;
+      r0[i] = v;
+      d[0] += v * v;
+    }
+    r[i] = v;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    if (jacobi) gb_restart_done(st, s[0]);
+  }
+};
+
+template <typename T>
+struct GbRestartFinish {  // generic preconditioner: p = r0* = r (already M^-1 applied)
+  static constexpr int NDOT = 1;
+  T *p, *r0; const T *r; St<T> *st;
+  __device__ bool skip() const { return st->restart_skip != 0; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T v = r[i];
+    p[i] = v;
+    r0[i] = v;
+    d[0] += v * v;
+  }
+  __device__ void finalize(const T (&s)[1]) const { gb_restart_done(st, s[0]); }
+};
+
+template <typename T>
+struct EpiStore {  // y = acc (optionally / d)
+  static constexpr int NDOT = 0;
+  T *y; const T *dg; const int *flag;
+  __device__ bool skip() const { return flag && *flag != kRunning; }
+  __device__ void row(uint32_t i, T acc, T (&)[1]) const { y[i] = dg ? acc / dg[i] : acc; }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
+template <typename T>
+struct EpiGb1 {  // t0 = M^-1 A p (Jacobi fused); <t0, r0*> -> alpha
+  static constexpr int NDOT = 1;
+  T *t0; const T *dg, *r0; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
+    T v = acc / dg[i];
+    t0[i] = v;
+    d[0] += v * r0[i];
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->iters += 1;
+    st->alpha = st->ip / s[0];
+  }
+};
+
+template <typename T>
+struct GbDot1 {  // generic: <t0, r0*> -> alpha
+  static constexpr int NDOT = 1;
+  const T *t0, *r0; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const { d[0] += t0[i] * r0[i]; }
+  __device__ void finalize(const T (&s)[1]) const {
+    st->iters += 1;
+    st->alpha = st->ip / s[0];
+  }
+};
+
+template <typename T>
+struct GbS {  // s = r - alpha t0
+  static constexpr int NDOT = 0;
+  T *s_; const T *r, *t0; St<T> *st;
+  struct S { T a; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->alpha}; }
+  __device__ void apply(size_t i, S c, T (&)[1]) const { s_[i] = r[i] - c.a * t0[i]; }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
+template <typename T>
+__device__ __forceinline__ void gb_omega(St<T> *st, T t1t1, T t1s) {
+  T nt1 = sqrt(t1t1);
+  st->omega = t1s / (nt1 * nt1);
+}
+
+template <typename T>
+struct EpiGb2 {  // t1 = M^-1 A s (Jacobi fused); ||t1||^2, <t1,s> -> omega
+  static constexpr int NDOT = 2;
+  T *t1; const T *dg, *s_; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ void row(uint32_t i, T acc, T (&d)[2]) const {
+    T v = acc / dg[i];
+    t1[i] = v;
+    d[0] += v * v;
+    d[1] += v * s_[i];
+  }
+  __device__ void finalize(const T (&s)[2]) const { gb_omega(st, s[0], s[1]); }
+};
+
+template <typename T>
+struct GbDot2 {
+  static constexpr int NDOT = 2;
+  const T *t1, *s_; St<T> *st;
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[2]) const {
+    T v = t1[i];
+    d[0] += v * v;
+    d[1] += v * s_[i];
+  }
+  __device__ void finalize(const T (&s)[2]) const { gb_omega(st, s[0], s[1]); }
+};
+
+template <typename T>
+struct GbUpdate {  // x += a p + w s; r = s - w t1; ||r||, <r,r0*>; beta, restart test
+  static constexpr int NDOT = 2;
+  T *x, *r; const T *p, *s_, *t1, *r0; St<T> *st;
+  struct S { T a, w; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->alpha, st->omega}; }
+  __device__ void apply(size_t i, S c, T (&d)[2]) const {
+    T vs = s_[i];
+    x[i] += c.a * p[i] + c.w * vs;
+    T vr = vs - c.w * t1[i];
+    r[i] = vr;
+    d[0] += vr * vr;
+    d[1] += vr * r0[i];
+  }
+  __device__ void finalize(const T (&s)[2]) const {
+    T rn = sqrt(s[0]);
+    st->resnorm = rn;
+    st->error = (double)rn / (double)st->nrhs;
+    if ((double)rn / (double)st->nrhs < st->tol || (double)rn < st->abs_tol) {
+      st->done = kConverged;
+      st->restart_skip = 1;
+      return;
+    }
+    T new_ip = s[1];
+    T beta = new_ip / st->ip * st->alpha / st->omega;
+    st->beta = beta;
+    st->ip = new_ip;
+    unsigned i = st->iters - 1;
+    if ((new_ip >= T(0) && new_ip <= T(0)) || (st->omega >= T(0) && st->omega <= T(0)) ||
+        i - st->last_restart > st->max_before_restart) {
+      st->restart = 1;
+    }
+    if (!finite_(st->alpha) || !finite_(st->omega)) st->done = kBreakdown;
+    else if (st->iters >= st->max_iters) st->done = kMaxIters;
+    st->restart_skip = (st->done != kRunning) || !st->restart;
+  }
+};
+
+template <typename T>
+struct GbP {  // p = r + beta (p - omega t0)
+  static constexpr int NDOT = 0;
+  T *p; const T *r, *t0; St<T> *st;
+  struct S { T b, w; };
+  __device__ bool skip() const { return st->done != kRunning; }
+  __device__ S load() const { return {st->beta, st->omega}; }
+  __device__ void apply(size_t i, S c, T (&)[1]) const {
+    p[i] = r[i] + c.b * (p[i] - c.w * t0[i]);
+  }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
+// ===========================================================================
+// pipelined GMRES (gmres.hpp:181-367, host_based/iterative_operations.hpp:734-935)
+// ===========================================================================
+constexpr int kGmresMaxK = 64;
+
+template <typename T>
+struct Gm {  // GMRES device state
+  T nrhs, rho0, rho, vnorm2;
+  T R[kGmresMaxK * kGmresMaxK];
+  T xi[kGmresMaxK];
+  T h[kGmresMaxK];
+  T coef[kGmresMaxK];
+  int kk;             // number of update coefficients
+  unsigned restart_count, max_restarts;
+  double tol, abs_tol, error;
+  unsigned iters;
+  unsigned K;
+  int done;
+};
+
+template <typename T>
+struct GmInit {
+  static constexpr int NDOT = 1;
+  const T *b; T *x, *r; Gm<T> *g;
+  __device__ bool skip() const { return false; }
+  __device__ NoScal load() const { return {}; }
+  __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
+    T bi = b[i];
+    x[i] = T(0);
+    r[i] = bi;
+    d[0] += bi * bi;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    g->nrhs = sqrt(s[0]);
+    g->rho0 = g->nrhs;
+    g->rho = T(1);
+    g->iters = 0;
+    g->error = 0;
+    g->restart_count = 0;
+    g->done = kRunning;
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void gm_cycle_check(Gm<T> *g) {
+  // gmres.hpp:226-233 (the restart bound ends the loop after the last cycle)
+  if ((double)g->rho0 <= g->abs_tol) { g->done = kConverged; return; }
+  g->rho = T(1);
+  if ((double)(g->rho0 / g->nrhs) < g->tol || (double)g->rho0 < g->abs_tol) {
+    g->done = kConverged;
+    return;
+  }
+  if (g->restart_count > g->max_restarts) g->done = kMaxIters;
+}
+
+template <typename T>
+struct GmCheckFirst {
+  Gm<T> *g;
+  __device__ void operator()() const { gm_cycle_check(g); }
+};
+
+template <typename T>
+struct EpiGmResid {  // r = b - A x; rho0 = ||r||
+  static constexpr int NDOT = 1;
+  T *r; const T *b; Gm<T> *g;
+  __device__ bool skip() const { return g->done != kRunning; }
+  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
+    T v = b[i] - acc;
+    r[i] = v;
+    d[0] += v * v;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    g->rho0 = sqrt(s[0]);
+    gm_cycle_check(g);
+  }
+};
+
+template <typename T>
+struct GmScaleR {  // r /= rho0 (the reference scales before its convergence test)
+  static constexpr int NDOT = 0;
+  T *r; Gm<T> *g;
+  struct S { T inv; };
+  __device__ bool skip() const { return false; }
+  __device__ S load() const { return {g->rho0}; }
+  __device__ void apply(size_t i, S c, T (&)[1]) const { r[i] /= c.inv; }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
+template <typename T>
+struct EpiGmV {  // v_k = A src, ||v_k||^2 (used for k = 0)
+  static constexpr int NDOT = 1;
+  T *vk; Gm<T> *g;
+  __device__ bool skip() const { return g->done != kRunning; }
+  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
+    vk[i] = acc;
+    d[0] += acc * acc;
+  }
+  __device__ void finalize(const T (&s)[1]) const { g->vnorm2 = s[0]; }
+};
+
+// classical Gram-Schmidt stage 1: h_j = <v_j, v_k>, j < k, one pass over the
+// rows reading each basis vector once (a tall-skinny GEMV)
+template <typename T, int KB>
+__global__ void __launch_bounds__(256)
+    gmres_multidot_kernel(size_t n, int k, const T *__restrict__ V, size_t ld, Gm<T> *g,
+                          T *partials, unsigned *counter) {
+  if (g->done != kRunning) return;
+  __shared__ T red[KB * 8];
+  __shared__ bool am_last;
+  const T *vk = V + (size_t)k * ld;
+  T acc[KB];
+#pragma unroll
+  for (int j = 0; j < KB; ++j) acc[j] = T(0);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    T v = vk[i];
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < k) acc[j] += V[(size_t)j * ld + i] * v;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < KB; ++j) {
+    if (j < k) {
+      T t = warp_sum(acc[j]);
+      if (lane == 0) red[j * 8 + warp] = t;
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    T t = 0;
+    for (int w = 0; w < 8; ++w) t += red[j * 8 + w];
+    partials[(size_t)j * gridDim.x + blockIdx.x] = t;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  // last block: one warp per dot, fixed order
+  for (int j = warp; j < k; j += 8) {
+    T t = 0;
+    for (unsigned b = lane; b < gridDim.x; b += 32)
+      t += ((volatile T *)partials)[(size_t)j * gridDim.x + b];
+    t = warp_sum(t);
+    if (lane == 0) {
+      g->h[j] = t;
+      g->R[j + (size_t)k * g->K] = t;
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0;
+}
+
+// stage 2 for k basis vectors: v_k -= sum_j h_j v_j; ||v_k||^2
+template <typename T, int KB>
+__global__ void __launch_bounds__(256)
+    gmres_orth_kernel(size_t n, int k, T *__restrict__ V, size_t ld, Gm<T> *g, T *partials,
+                      unsigned *counter) {
+  if (g->done != kRunning) return;
+  __shared__ T hs[KB];
+  __shared__ T smem[16];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = g->h[j];
+  __syncthreads();
+  T *vk = V + (size_t)k * ld;
+  T d[1] = {T(0)};
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    T v = vk[i];
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < k) v -= hs[j] * V[(size_t)j * ld + i];
+    d[0] += v * v;
+    vk[i] = v;
+  }
+  T s[1];
+  if (grid_reduce<1>(d, partials, counter, smem, s)) g->vnorm2 = s[0];
+}
+
+template <typename T>
+struct GmNormalize {  // R(k,k) = ||v_k||; v_k /= ||v_k||; xi_k = <r, v_k>
+  static constexpr int NDOT = 1;
+  T *vk; const T *r; Gm<T> *g; int k;
+  struct S { T nv; };
+  __device__ bool skip() const { return g->done != kRunning; }
+  __device__ S load() const { return {sqrt(g->vnorm2)}; }
+  __device__ void apply(size_t i, S c, T (&d)[1]) const {
+    T v = vk[i] / c.nv;
+    d[0] += r[i] * v;
+    vk[i] = v;
+  }
+  __device__ void finalize(const T (&s)[1]) const {
+    g->xi[k] = s[0];
+    g->R[k + (size_t)k * g->K] = sqrt(g->vnorm2);
+  }
+};
+
+// the host part of a restart cycle (gmres.hpp:287-345) as one device thread
+template <typename T>
+struct GmCycleEnd {
+  Gm<T> *g;
+  __device__ void operator()() const {
+    if (g->done != kRunning) { g->kk = 0; return; }
+    const unsigned K = g->K;
+    unsigned k = K, full_k = K;
+    for (unsigned i = 0; i < k; ++i)
+      if (fabs((double)g->R[i + i * k]) < g->tol * (double)g->R[0]) { k = i; break; }
+    T rho = g->rho;
+    for (unsigned i = 0; i < k; ++i) {
+      g->iters += 1;
+      T xi = g->xi[i];
+      if (xi >= rho || xi <= -rho) { k = i; break; }
+      rho *= sin(acos(xi / rho));
+    }
+    g->rho = rho;
+    T eta[kGmresMaxK];
+    for (unsigned i = 0; i < K; ++i) eta[i] = g->xi[i];
+    for (int i2 = (int)k - 1; i2 > -1; --i2) {
+      unsigned i = (unsigned)i2;
+      for (unsigned j = i + 1; j < k; ++j) eta[i] -= g->R[i + j * full_k] * eta[j];
+      eta[i] /= g->R[i + i * full_k];
+    }
+    for (unsigned i = 0; i < k; ++i) g->coef[i] = g->rho0 * eta[i];
+    g->kk = (int)k;
+    g->error = fabs((double)(rho * g->rho0 / g->nrhs));
+    g->restart_count += 1;
+  }
+};
+
+template <typename T>
+struct GmUpdateX {  // x += c0 r + sum_{j>=1} c_j v_{j-1}
+  static constexpr int NDOT = 0;
+  T *x; const T *r, *V; size_t ld; Gm<T> *g;
+  struct S { int kk; };
+  __device__ bool skip() const { return g->done != kRunning || g->kk == 0; }
+  __device__ S load() const { return {g->kk}; }
+  __device__ void apply(size_t i, S c, T (&)[1]) const {
+    T v = x[i] + g->coef[0] * r[i];
+    for (int j = 1; j < c.kk; ++j) v += g->coef[j] * V[(size_t)(j - 1) * ld + i];
+    x[i] = v;
+  }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
+// ===========================================================================
+// host drivers
+// ===========================================================================
+struct Workspace {
+  DevBuf buf;
+  std::vector<size_t> offs;
+  size_t total = 0;
+  size_t add(size_t bytes) {
+    size_t o = total;
+    total += (bytes + 255) / 256 * 256;
+    offs.push_back(o);
+    return o;
+  }
+  void commit(Backend &be) {
+    buf.alloc(std::max<size_t>(total, 256), be.stream);
+    VCLGB_CUDA(cudaMemsetAsync(buf.ptr, 0, buf.bytes, be.stream));
+  }
+  template <typename X> X *at(size_t off) const { return reinterpret_cast<X *>(buf.as<char>() + off); }
+};
+
+static uint32_t auto_check_every(const vclgbSolverTag *tag, uint32_t rows) {
+  if (tag->check_every) return tag->check_every;
+  if (rows < (1u << 16)) return 32;
+  if (rows < (1u << 20)) return 16;
+  return 8;
+}
+
+template <typename T>
+static void set_tag_outputs(Backend &be, const St<T> *d_st, vclgbSolverTag *tag) {
+  St<T> h;
+  VCLGB_CUDA(cudaMemcpyAsync(&h, d_st, sizeof(h), cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  tag->iters = h.iters;
+  tag->error = h.error;
+  tag->status = h.done == kConverged ? VCLGB_SUCCESS
+              : h.done == kMaxIters  ? VCLGB_NOT_CONVERGED
+                                     : VCLGB_BREAKDOWN;
+}
+
+template <typename T>
+static St<T> make_state(const vclgbSolverTag *tag) {
+  St<T> s;
+  std::memset(&s, 0, sizeof(s));
+  s.tol = tag->tol;
+  s.abs_tol = tag->abs_tol;
+  s.max_iters = tag->max_iters;
+  s.max_before_restart = tag->max_iters_before_restart;
+  return s;
+}
+
+static bool diag_needed(const Precond *P) { return P && P->kind == 1; }
+
+template <typename T>
+void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, const Precond *P) {
+  const uint32_t n = A.rows;
+  require(A.rows == A.cols, VCLGB_INVALID_ARGUMENT, "CG needs a square matrix");
+  Workspace ws;
+  size_t o_st = ws.add(sizeof(St<T>));
+  size_t o_part = ws.add(8 * kMaxSpmvGrid * sizeof(T));
+  size_t o_cnt = ws.add(64);
+  size_t vb = std::max<size_t>(n, 1) * sizeof(T);
+  size_t o_r = ws.add(vb), o_p = ws.add(vb), o_q = ws.add(vb), o_z = ws.add(vb);
+  size_t o_hyb = ws.add(hyb_scratch_bytes(A));
+  ws.commit(be);
+  St<T> *st = ws.at<St<T>>(o_st);
+  St<T> h0 = make_state<T>(tag);
+  VCLGB_CUDA(cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, be.stream));
+  Reduction red{ws.at<void>(o_part), ws.at<unsigned>(o_cnt)};
+  T *r = ws.at<T>(o_r), *p = ws.at<T>(o_p), *q = ws.at<T>(o_q), *z = ws.at<T>(o_z);
+  void *hyb = ws.at<void>(o_hyb);
+  const int *done = &st->done;
+  uint32_t every = auto_check_every(tag, n);
+  uint32_t chunks = tag->max_iters / every + 2;
+
+  if (!P) {
+    // pipelined CG
+    vec_pass<T>(be, n, CgInit<T>{b, x, r, p, st}, red);
+    spmv_launch<T>(be, A, p, 0, 1, EpiCgFirst<T>{q, p, st}, red, q, 0, 1, T(1), T(0), done, hyb);
+    run_iterations(be, done, chunks, every, true, [&]() {
+      vec_pass<T>(be, n, CgUpdate<T>{x, p, r, q, st}, red);
+      spmv_launch<T>(be, A, p, 0, 1, EpiCg<T>{q, p, st}, red, q, 0, 1, T(1), T(0), done, hyb);
+    });
+  } else {
+    const bool jac = diag_needed(P);
+    const T *dg = jac ? P->diag.as<T>() : nullptr;
+    vec_pass<T>(be, n, PcgInit<T>{b, dg, x, r, z, p, st, jac}, red);
+    if (!jac) {
+      precond_apply(be, *P, z, nullptr);
+      vec_pass<T>(be, n, PcgInitFinish<T>{r, z, p, st}, red);
+    }
+    run_iterations(be, done, chunks, every, true, [&]() {
+      spmv_launch<T>(be, A, p, 0, 1, EpiPcg<T>{q, p, st}, red, q, 0, 1, T(1), T(0), done, hyb);
+      vec_pass<T>(be, n, PcgUpdate<T>{x, r, z, p, q, dg, st, jac}, red);
+      if (!jac) {
+        precond_apply(be, *P, z, done);
+        vec_pass<T>(be, n, PcgDot<T>{r, z, st}, red);
+      }
+      vec_pass<T>(be, n, PcgP<T>{p, r, z, dg, st, jac}, red);
+    });
+  }
+  set_tag_outputs(be, st, tag);
+}
+
+template <typename T>
+void bicgstab_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag,
+                    const Precond *P) {
+  const uint32_t n = A.rows;
+  require(A.rows == A.cols, VCLGB_INVALID_ARGUMENT, "BiCGStab needs a square matrix");
+  Workspace ws;
+  size_t o_st = ws.add(sizeof(St<T>));
+  size_t o_part = ws.add(8 * kMaxSpmvGrid * sizeof(T));
+  size_t o_cnt = ws.add(64);
+  size_t vb = std::max<size_t>(n, 1) * sizeof(T);
+  size_t o_r = ws.add(vb), o_p = ws.add(vb), o_r0 = ws.add(vb), o_Ap = ws.add(vb),
+         o_s = ws.add(vb), o_As = ws.add(vb);
+  size_t o_hyb = ws.add(hyb_scratch_bytes(A));
+  ws.commit(be);
+  St<T> *st = ws.at<St<T>>(o_st);
+  St<T> h0 = make_state<T>(tag);
+  VCLGB_CUDA(cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, be.stream));
+  Reduction red{ws.at<void>(o_part), ws.at<unsigned>(o_cnt)};
+  T *r = ws.at<T>(o_r), *p = ws.at<T>(o_p), *r0 = ws.at<T>(o_r0), *Ap = ws.at<T>(o_Ap),
+    *s = ws.at<T>(o_s), *As = ws.at<T>(o_As);
+  void *hyb = ws.at<void>(o_hyb);
+  const int *done = &st->done;
+  uint32_t every = auto_check_every(tag, n);
+  uint32_t chunks = tag->max_iters / every + 2;
+
+  if (!P) {
+    vec_pass<T>(be, n, BicgInit<T>{b, x, r, p, r0, st}, red);
+    run_iterations(be, done, chunks, every, true, [&]() {
+      spmv_launch<T>(be, A, p, 0, 1, EpiBicgAp<T>{Ap, r0, st}, red, Ap, 0, 1, T(1), T(0), done, hyb);
+      vec_pass<T>(be, n, BicgS<T>{s, r, Ap, st}, red);
+      spmv_launch<T>(be, A, s, 0, 1, EpiBicgAs<T>{As, s, r0, st}, red, As, 0, 1, T(1), T(0), done, hyb);
+      vec_pass<T>(be, n, BicgUpdate<T>{x, p, r, s, As, Ap, r0, st}, red);
+    });
+  } else {
+    const bool jac = diag_needed(P);
+    const T *dg = jac ? P->diag.as<T>() : nullptr;
+    // t0 -> Ap, t1 -> As
+    vec_pass<T>(be, n, GbInit<T>{b, x, st}, red);
+    const int *rskip = &st->restart_skip;
+    run_iterations(be, done, chunks, every, true, [&]() {
+      spmv_launch<T>(be, A, x, 0, 1, EpiGbRestart<T>{r, p, r0, b, dg, st, jac}, red, r, 0, 1,
+                     T(1), T(0), rskip, hyb);
+      if (!jac) {
+        precond_apply(be, *P, r, rskip);
+        vec_pass<T>(be, n, GbRestartFinish<T>{p, r0, r, st}, red);
+        spmv_launch<T>(be, A, p, 0, 1, EpiStore<T>{Ap, nullptr, done}, red, Ap, 0, 1, T(1), T(0), done, hyb);
+        precond_apply(be, *P, Ap, done);
+        vec_pass<T>(be, n, GbDot1<T>{Ap, r0, st}, red);
+      } else {
+        spmv_launch<T>(be, A, p, 0, 1, EpiGb1<T>{Ap, dg, r0, st}, red, Ap, 0, 1, T(1), T(0), done, hyb);
+      }
+      vec_pass<T>(be, n, GbS<T>{s, r, Ap, st}, red);
+      if (!jac) {
+        spmv_launch<T>(be, A, s, 0, 1, EpiStore<T>{As, nullptr, done}, red, As, 0, 1, T(1), T(0), done, hyb);
+        precond_apply(be, *P, As, done);
+        vec_pass<T>(be, n, GbDot2<T>{As, s, st}, red);
+      } else {
+        spmv_launch<T>(be, A, s, 0, 1, EpiGb2<T>{As, dg, s, st}, red, As, 0, 1, T(1), T(0), done, hyb);
+      }
+      vec_pass<T>(be, n, GbUpdate<T>{x, r, p, s, As, r0, st}, red);
+      vec_pass<T>(be, n, GbP<T>{p, r, Ap, st}, red);
+    });
+  }
+  set_tag_outputs(be, st, tag);
+}
+
+template <typename T>
+void gmres_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag) {
+  const uint32_t n = A.rows;
+  const uint32_t K = tag->krylov_dim ? tag->krylov_dim : 20;
+  require(A.rows == A.cols, VCLGB_INVALID_ARGUMENT, "GMRES needs a square matrix");
+  require(K <= (uint32_t)kGmresMaxK, VCLGB_INVALID_ARGUMENT, "krylov_dim must be <= 64");
+  Workspace ws;
+  size_t o_g = ws.add(sizeof(Gm<T>));
+  size_t o_part = ws.add((size_t)kGmresMaxK * kMaxSpmvGrid * sizeof(T));
+  size_t o_cnt = ws.add(64);
+  size_t ld = ((size_t)std::max<uint32_t>(n, 1) + 31) / 32 * 32;
+  size_t o_r = ws.add(ld * sizeof(T));
+  size_t o_V = ws.add(ld * K * sizeof(T));
+  size_t o_hyb = ws.add(hyb_scratch_bytes(A));
+  ws.commit(be);
+  Gm<T> *g = ws.at<Gm<T>>(o_g);
+  {
+    Gm<T> h;
+    std::memset(&h, 0, sizeof(h));
+    h.K = K;
+    h.tol = tag->tol;
+    h.abs_tol = tag->abs_tol;
+    unsigned mr = tag->max_iters / K;
+    if (mr > 0 && mr * K == tag->max_iters) mr -= 1;  // gmres_tag::max_restarts
+    h.max_restarts = mr;
+    VCLGB_CUDA(cudaMemcpyAsync(g, &h, sizeof(h), cudaMemcpyHostToDevice, be.stream));
+  }
+  Reduction red{ws.at<void>(o_part), ws.at<unsigned>(o_cnt)};
+  T *r = ws.at<T>(o_r), *V = ws.at<T>(o_V);
+  void *hyb = ws.at<void>(o_hyb);
+  const int *done = &g->done;
+  vec_pass<T>(be, n, GmInit<T>{b, x, r, g}, red);
+  scalar_step(be, GmCheckFirst<T>{g});
+  vec_pass<T>(be, n, GmScaleR<T>{r, g}, red);
+  bool first = true;
+  auto cycle = [&]() {
+    if (!first) {
+      spmv_launch<T>(be, A, x, 0, 1, EpiGmResid<T>{r, b, g}, red, r, 0, 1, T(1), T(0), done, hyb);
+      vec_pass<T>(be, n, GmScaleR<T>{r, g}, red);
+    }
+    for (uint32_t k = 0; k < K; ++k) {
+      T *vk = V + (size_t)k * ld;
+      const T *src = k == 0 ? r : V + (size_t)(k - 1) * ld;
+      spmv_launch<T>(be, A, src, 0, 1, EpiGmV<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done, hyb);
+      if (k > 0) {
+        int grid = vec_grid(be, n);
+        T *part = static_cast<T *>(red.partials);
+#define VCLGB_GM_CASE(KB)                                                                          \
+  gmres_multidot_kernel<T, KB><<<grid, 256, 0, be.stream>>>(n, (int)k, V, ld, g, part, red.counter); \
+  gmres_orth_kernel<T, KB><<<grid, 256, 0, be.stream>>>(n, (int)k, V, ld, g, part, red.counter)
+        if (k <= 8) { VCLGB_GM_CASE(8); }
+        else if (k <= 16) { VCLGB_GM_CASE(16); }
+        else if (k <= 32) { VCLGB_GM_CASE(32); }
+        else { VCLGB_GM_CASE(64); }
+#undef VCLGB_GM_CASE
+        be.launches += 2;
+        VCLGB_CHECK_LAUNCH();
+      }
+      vec_pass<T>(be, n, GmNormalize<T>{vk, r, g, (int)k}, red);
+    }
+    scalar_step(be, GmCycleEnd<T>{g});
+    vec_pass<T>(be, n, GmUpdateX<T>{x, r, V, ld, g}, red);
+  };
+  // first cycle (no residual recomputation), then captured cycles
+  cycle();
+  first = false;
+  uint32_t max_cycles = tag->max_iters / K + 3;
+  run_iterations(be, done, max_cycles, 1, true, cycle);
+  Gm<T> h;
+  VCLGB_CUDA(cudaMemcpyAsync(&h, g, sizeof(h), cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  tag->iters = h.iters;
+  tag->error = h.error;
+  tag->status = h.done == kConverged ? VCLGB_SUCCESS
+              : h.done == kMaxIters  ? VCLGB_NOT_CONVERGED
+                                     : VCLGB_BREAKDOWN;
+}
+
+template void cg_solve<double>(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, const Precond *);
+template void cg_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *, const Precond *);
+template void bicgstab_solve<double>(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, const Precond *);
+template void bicgstab_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *, const Precond *);
+template void gmres_solve<double>(Backend &, Matrix &, const double *, double *, vclgbSolverTag *);
+template void gmres_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *);
+
+}  // namespace vclgb

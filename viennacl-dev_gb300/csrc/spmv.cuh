@@ -1,0 +1,457 @@
+// spmv.cuh -- SpMV kernels for CSR (adaptive, row-length bins), ELL, SELL-C-sigma
+// and HYB (ELL + COO tail with a warp-segmented reduction).
+//
+// Every kernel hands each finished row to an epilogue object E:
+//   static constexpr int NDOT;                    number of fused dot products
+//   bool skip() const;                            grid-uniform early exit
+//   void row(uint32_t r, T acc, T (&dots)[..])    store the row, add to dots
+//   void finalize(const T (&sums)[..]) const;     last block, thread 0
+// so the pipelined solvers fuse "Ap = A p" with their reductions, as the
+// reference's pipelined_*_prod kernels do (linalg/cuda/iterative_operations.hpp),
+// but finish the reduction and the scalar recurrences on the device.
+#pragma once
+
+#include "vclgb_internal.hpp"
+
+namespace vclgb {
+
+constexpr int kSpmvThreads = 256;
+
+// epilogue: y = alpha*acc + beta*y (linalg/cuda/sparse_matrix_operations.hpp prod_impl)
+template <typename T>
+struct EpiAxpby {
+  static constexpr int NDOT = 0;
+  T alpha, beta;
+  T *y;
+  int64_t ys, yinc;
+  __device__ __forceinline__ bool skip() const { return false; }
+  __device__ __forceinline__ void row(uint32_t r, T acc, T (&)[1]) const {
+    T *p = y + ys + (int64_t)r * yinc;
+    *p = (beta != T(0)) ? alpha * acc + beta * *p : alpha * acc;
+  }
+  __device__ __forceinline__ void finalize(const T (&)[1]) const {}
+};
+
+// same, with an early-exit flag (solver converged)
+template <typename T>
+struct EpiAxpbySkip : EpiAxpby<T> {
+  const int *flag;
+  __device__ __forceinline__ bool skip() const { return flag && *flag; }
+};
+
+template <int N>
+struct DotArr { static constexpr int n = N > 0 ? N : 1; };
+
+// ---------------------------------------------------------------------------
+// adaptive CSR
+// ---------------------------------------------------------------------------
+struct BinTable {
+  int n;
+  CsrBin b[kMaxBins];
+};
+
+template <typename T>
+struct CsrView {
+  const uint32_t *rp;
+  const uint32_t *ci;
+  const T *v;
+  uint32_t rows;
+};
+
+// rows of one bin, LANES threads per row, U rows per group per step; the
+// warp's groups take consecutive rows so that each load instruction of the
+// warp touches one contiguous stretch of the value/column arrays.
+template <int LANES, int U, typename T, class E>
+__device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__restrict__ x,
+                                               int64_t xs, int64_t xinc, uint32_t count,
+                                               const uint32_t *__restrict__ list, const E &epi,
+                                               T (&dots)[DotArr<E::NDOT>::n]) {
+  constexpr int GPW = 32 / LANES;  // groups per warp
+  const uint32_t lane = threadIdx.x & (LANES - 1);
+  const uint32_t gw = (threadIdx.x & 31) / LANES;
+  const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  constexpr uint32_t ROWS_PER_WARP = GPW * U;
+  for (size_t wb = warp * ROWS_PER_WARP; wb < count; wb += nwarps * ROWS_PER_WARP) {
+    uint32_t row[U], s[U], e[U];
+    T acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      size_t idx = wb + (size_t)u * GPW + gw;
+      bool ok = idx < count;
+      row[u] = ok ? (list ? __ldg(list + idx) : (uint32_t)idx) : 0xffffffffu;
+      s[u] = ok ? __ldg(A.rp + row[u]) : 0u;
+      e[u] = ok ? __ldg(A.rp + row[u] + 1) : 0u;
+    }
+    // first chunk of every row: loads of all U rows are issued together
+    uint32_t c[U];
+    T vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      uint32_t k = s[u] + lane;
+      bool ok = k < e[u];
+      c[u] = ok ? __ldg(A.ci + k) : 0u;
+      vv[u] = ok ? __ldg(A.v + k) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      uint32_t k = s[u] + lane;
+      acc[u] = (k < e[u]) ? vv[u] * __ldg(x + xs + (int64_t)c[u] * xinc) : T(0);
+    }
+    // remaining chunks (rows longer than LANES)
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      for (uint32_t k = s[u] + lane + LANES; k < e[u]; k += LANES)
+        acc[u] += __ldg(A.v + k) * __ldg(x + xs + (int64_t)__ldg(A.ci + k) * xinc);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      T t = group_sum<LANES>(acc[u]);
+      if (lane == 0 && row[u] != 0xffffffffu) epi.row(row[u], t, dots);
+    }
+  }
+}
+
+// one block per row (rows longer than a warp can stream efficiently)
+template <typename T, class E>
+__device__ __forceinline__ void csr_rows_block(const CsrView<T> &A, const T *__restrict__ x,
+                                               int64_t xs, int64_t xinc, uint32_t count,
+                                               const uint32_t *__restrict__ list, const E &epi,
+                                               T (&dots)[DotArr<E::NDOT>::n], T *smem) {
+  for (size_t i = blockIdx.x; i < count; i += gridDim.x) {
+    uint32_t row = list ? __ldg(list + i) : (uint32_t)i;
+    uint32_t s = __ldg(A.rp + row), e = __ldg(A.rp + row + 1);
+    T acc[1] = {T(0)};
+    for (uint32_t k = s + threadIdx.x; k < e; k += blockDim.x)
+      acc[0] += __ldg(A.v + k) * __ldg(x + xs + (int64_t)__ldg(A.ci + k) * xinc);
+    block_sum<1>(acc, smem);
+    if (threadIdx.x == 0) epi.row(row, acc[0], dots);
+    __syncthreads();
+  }
+}
+
+template <typename T, class E>
+__global__ void __launch_bounds__(kSpmvThreads)
+    csr_adaptive_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc,
+                        BinTable bins, const uint32_t *__restrict__ bin_rows, E epi,
+                        T *partials, unsigned *counter) {
+  if (epi.skip()) return;
+  __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
+  T dots[DotArr<E::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  for (int b = 0; b < bins.n; ++b) {
+    const CsrBin bin = bins.b[b];
+    const uint32_t *list = bin.identity ? nullptr : bin_rows + bin.offset;
+    switch (bin.lanes) {
+      case 1: csr_rows_group<1, 4>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 2: csr_rows_group<2, 4>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 4: csr_rows_group<4, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 8: csr_rows_group<8, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 16: csr_rows_group<16, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 32: csr_rows_group<32, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      default: csr_rows_block(A, x, xs, xinc, bin.count, list, epi, dots, smem); break;
+    }
+  }
+  if constexpr (E::NDOT > 0) {
+    T sums[E::NDOT];
+    if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ELL: thread per row, column-major slots (ell_matrix.hpp layout); explicit
+// zeros are skipped like the reference kernels do.
+// ---------------------------------------------------------------------------
+template <typename T, class E>
+__global__ void __launch_bounds__(kSpmvThreads)
+    ell_kernel(uint32_t rows, uint32_t width, const uint32_t *__restrict__ coords,
+               const T *__restrict__ elems, const T *__restrict__ x, int64_t xs, int64_t xinc,
+               E epi, T *partials, unsigned *counter) {
+  if (epi.skip()) return;
+  __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
+  T dots[DotArr<E::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    T acc = 0;
+    uint32_t j = 0;
+    for (; j + 4 <= width; j += 4) {
+      T val[4];
+      uint32_t col[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        size_t off = (size_t)(j + q) * rows + r;
+        val[q] = __ldg(elems + off);
+        col[q] = __ldg(coords + off);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (val[q] != T(0)) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+    }
+    for (; j < width; ++j) {
+      size_t off = (size_t)j * rows + r;
+      T val = __ldg(elems + off);
+      if (val != T(0)) acc += val * __ldg(x + xs + (int64_t)__ldg(coords + off) * xinc);
+    }
+    epi.row((uint32_t)r, acc, dots);
+  }
+  if constexpr (E::NDOT > 0) {
+    T sums[E::NDOT];
+    if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SELL-C-sigma: thread per stored row position; slice s, lane l; element j of
+// the position at block_start[s] + j*C + l (sliced_ell_matrix.hpp layout).
+// ---------------------------------------------------------------------------
+template <typename T, class E>
+__global__ void __launch_bounds__(kSpmvThreads)
+    sell_kernel(uint32_t rows, uint32_t C, const uint32_t *__restrict__ cpb,
+                const uint32_t *__restrict__ start, const uint32_t *__restrict__ cols,
+                const T *__restrict__ elems, const uint32_t *__restrict__ perm,
+                const T *__restrict__ x, int64_t xs, int64_t xinc, E epi, T *partials,
+                unsigned *counter) {
+  if (epi.skip()) return;
+  __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
+  T dots[DotArr<E::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  for (size_t pos = (size_t)blockIdx.x * blockDim.x + threadIdx.x; pos < rows;
+       pos += (size_t)gridDim.x * blockDim.x) {
+    uint32_t s = (uint32_t)(pos / C), l = (uint32_t)(pos % C);
+    uint32_t w = __ldg(cpb + s);
+    size_t base = (size_t)__ldg(start + s) + l;
+    T acc = 0;
+    uint32_t j = 0;
+    for (; j + 4 <= w; j += 4) {
+      T val[4];
+      uint32_t col[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        size_t off = base + (size_t)(j + q) * C;
+        val[q] = __ldg(elems + off);
+        col[q] = __ldg(cols + off);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (val[q] != T(0)) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+    }
+    for (; j < w; ++j) {
+      size_t off = base + (size_t)j * C;
+      T val = __ldg(elems + off);
+      if (val != T(0)) acc += val * __ldg(x + xs + (int64_t)__ldg(cols + off) * xinc);
+    }
+    uint32_t row = perm ? __ldg(perm + pos) : (uint32_t)pos;
+    epi.row(row, acc, dots);
+  }
+  if constexpr (E::NDOT > 0) {
+    T sums[E::NDOT];
+    if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// HYB tail: COO entries (row-sorted) in chunks of 32*K per warp.  Products are
+// combined with a warp-segmented scan; segments that lie wholly inside a chunk
+// are added to y directly, the first and last segment of every chunk go to a
+// carry array that hyb_tail_fixup adds in chunk order (deterministic).
+// ---------------------------------------------------------------------------
+constexpr int kTailK = 8;                       // steps of 32 entries per warp chunk
+constexpr int kTailChunk = 32 * kTailK;
+
+template <typename T>
+__global__ void __launch_bounds__(kSpmvThreads)
+    hyb_tail_kernel(uint64_t tnnz, const uint32_t *__restrict__ trow,
+                    const uint32_t *__restrict__ tcol, const T *__restrict__ tval,
+                    const T *__restrict__ x, int64_t xs, int64_t xinc, T alpha, T *y, int64_t ys,
+                    int64_t yinc, uint32_t *carry_row, T *carry_val, const int *skip_flag) {
+  if (skip_flag && *skip_flag) return;
+  const uint32_t INV = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t nchunks = (tnnz + kTailChunk - 1) / kTailChunk;
+  const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t ch = warp; ch < nchunks; ch += nwarps) {
+    const size_t c0 = ch * kTailChunk;
+    const size_t c1 = c0 + kTailChunk < tnnz ? c0 + kTailChunk : tnnz;
+    const uint32_t first_row = __ldg(trow + c0);
+    const uint32_t last_row = __ldg(trow + c1 - 1);
+    T run = 0;             // inclusive sum at the last entry of the previous step
+    uint32_t run_row = INV;
+    for (size_t k0 = c0; k0 < c1; k0 += 32) {
+      const size_t k = k0 + lane;
+      const bool ok = k < c1;
+      const uint32_t r = ok ? __ldg(trow + k) : INV;
+      T p = ok ? __ldg(tval + k) * __ldg(x + xs + (int64_t)__ldg(tcol + k) * xinc) : T(0);
+      if (lane == 0 && r == run_row) p += run;
+      // segmented inclusive scan (rows are sorted, so equal row <=> same segment)
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        T q = __shfl_up_sync(0xffffffffu, p, o);
+        uint32_t qr = __shfl_up_sync(0xffffffffu, r, o);
+        if ((int)lane >= o && qr == r) p += q;
+      }
+      uint32_t nr = __shfl_down_sync(0xffffffffu, r, 1);
+      if (lane == 31) nr = (k + 1 < c1) ? __ldg(trow + k + 1) : INV;
+      if (ok && nr != r) {  // last entry of row r inside this chunk
+        if (r == first_row) {
+          carry_row[2 * ch] = r;
+          carry_val[2 * ch] = p;
+        } else if (r == last_row) {
+          carry_row[2 * ch + 1] = r;
+          carry_val[2 * ch + 1] = p;
+        } else {
+          T *py = y + ys + (int64_t)r * yinc;
+          *py += alpha * p;
+        }
+      }
+      const int lastlane = (int)((c1 - k0 < 32 ? c1 - k0 : 32) - 1);
+      run = __shfl_sync(0xffffffffu, p, lastlane);
+      run_row = __shfl_sync(0xffffffffu, r, lastlane);
+    }
+    if (lane == 0 && first_row == last_row) carry_row[2 * ch + 1] = INV;
+  }
+}
+
+// Adds the carries of the tail chunks: the chunk in which a row's tail starts
+// owns the row and sums the continuation carries of the following chunks in
+// order.  carry[2c] = first segment of chunk c, carry[2c+1] = last segment
+// (0xffffffff when the chunk holds a single row).
+template <typename T>
+__global__ void hyb_tail_fixup(size_t nchunks, const uint32_t *__restrict__ carry_row,
+                               const T *__restrict__ carry_val, T alpha, T *y, int64_t ys,
+                               int64_t yinc, const int *skip_flag) {
+  if (skip_flag && *skip_flag) return;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
+       c += (size_t)gridDim.x * blockDim.x) {
+    for (int which = 0; which < 2; ++which) {
+      uint32_t r = carry_row[2 * c + which];
+      if (r == 0xffffffffu) continue;
+      if (which == 0 && c > 0) {
+        // continuation of a row owned by an earlier chunk?
+        uint32_t pl = carry_row[2 * (c - 1) + 1];
+        uint32_t pf = carry_row[2 * (c - 1)];
+        uint32_t prev_last = (pl != 0xffffffffu) ? pl : pf;
+        if (prev_last == r) continue;
+      }
+      T total = carry_val[2 * c + which];
+      for (size_t d = c + 1; d < nchunks; ++d) {
+        if (carry_row[2 * d] != r) break;
+        total += carry_val[2 * d];
+        if (carry_row[2 * d + 1] != 0xffffffffu) break;  // row ends inside chunk d
+      }
+      T *py = y + ys + (int64_t)r * yinc;
+      *py += alpha * total;
+    }
+  }
+}
+
+// epilogue pass over an already computed product (HYB in the solvers)
+template <typename T, class E>
+__global__ void __launch_bounds__(kSpmvThreads)
+    epilogue_pass_kernel(uint32_t rows, const T *__restrict__ y, E epi, T *partials,
+                         unsigned *counter) {
+  if (epi.skip()) return;
+  __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
+  T dots[DotArr<E::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x)
+    epi.row((uint32_t)r, y[r], dots);
+  if constexpr (E::NDOT > 0) {
+    T sums[E::NDOT];
+    if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host-side dispatch
+// ---------------------------------------------------------------------------
+struct Reduction {
+  void *partials = nullptr;  // >= 3 * grid entries of T
+  unsigned *counter = nullptr;
+};
+
+// grid of the SpMV kernels (also the number of partials per dot)
+inline int spmv_grid(const Backend &be, const Matrix &m) {
+  size_t work = m.format == VCLGB_SELL || m.format == VCLGB_ELL ? m.rows : (m.rows + 3) / 4;
+  if (m.format == VCLGB_CSR && m.nnz / 8 > work) work = m.nnz / 8;
+  return waves_grid(be, kSpmvThreads, 8, work < 1 ? 1 : work);
+}
+constexpr int kMaxSpmvGrid = 152 * 8 * 2;
+
+template <typename T, class E>
+void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t xinc, const E &epi,
+                 const Reduction &red, T *y_for_hyb = nullptr, int64_t ys = 0, int64_t yinc = 1,
+                 T alpha = T(1), T beta = T(0), const int *skip_flag = nullptr,
+                 void *hyb_scratch = nullptr) {
+  int grid = spmv_grid(be, m);
+  T *partials = static_cast<T *>(red.partials);
+  switch (m.format) {
+    case VCLGB_CSR: {
+      CsrView<T> A{m.row_ptr, m.col_idx, static_cast<const T *>(m.values), m.rows};
+      BinTable bt;
+      bt.n = m.num_bins;
+      for (int i = 0; i < m.num_bins; ++i) bt.b[i] = m.bins[i];
+      csr_adaptive_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+          A, x, xs, xinc, bt, m.bin_rows.as<uint32_t>(), epi, partials, red.counter);
+      break;
+    }
+    case VCLGB_ELL:
+      ell_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+          m.rows, m.ell_width, m.ell_coords.as<uint32_t>(), m.ell_elems.as<T>(), x, xs, xinc,
+          epi, partials, red.counter);
+      break;
+    case VCLGB_SELL:
+      sell_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+          m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
+          m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
+          m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, x, xs, xinc, epi, partials,
+          red.counter);
+      break;
+    case VCLGB_HYB: {
+      // y = alpha*ELL*x + beta*y, then y += alpha*tail*x, then the epilogue pass
+      EpiAxpbySkip<T> sp;
+      sp.alpha = alpha; sp.beta = beta; sp.y = y_for_hyb; sp.ys = ys; sp.yinc = yinc;
+      sp.flag = skip_flag;
+      ell_kernel<T, EpiAxpbySkip<T>><<<grid, kSpmvThreads, 0, be.stream>>>(
+          m.rows, m.ell_width, m.ell_coords.as<uint32_t>(), m.ell_elems.as<T>(), x, xs, xinc,
+          sp, partials, red.counter);
+      if (m.tail_nnz > 0) {
+        size_t nchunks = (m.tail_nnz + kTailChunk - 1) / kTailChunk;
+        uint32_t *carry_row = static_cast<uint32_t *>(hyb_scratch);
+        T *carry_val = reinterpret_cast<T *>(static_cast<char *>(hyb_scratch) +
+                                             ((2 * nchunks * sizeof(uint32_t) + 15) / 16) * 16);
+        int g = waves_grid(be, kSpmvThreads, 8, nchunks * 32);
+        hyb_tail_kernel<T><<<g, kSpmvThreads, 0, be.stream>>>(
+            m.tail_nnz, m.tail_row.as<uint32_t>(), m.tail_ci.as<uint32_t>(), m.tail_v.as<T>(),
+            x, xs, xinc, alpha, y_for_hyb, ys, yinc, carry_row, carry_val, skip_flag);
+        int g2 = (int)((nchunks + 255) / 256);
+        hyb_tail_fixup<T><<<g2, 256, 0, be.stream>>>(nchunks, carry_row, carry_val, alpha,
+                                                      y_for_hyb, ys, yinc, skip_flag);
+        be.launches += 2;
+      }
+      if constexpr (E::NDOT > 0) {
+        epilogue_pass_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            m.rows, y_for_hyb, epi, partials, red.counter);
+        be.launches++;
+      }
+      break;
+    }
+  }
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
+// scratch bytes the HYB tail needs (carry arrays)
+inline size_t hyb_scratch_bytes(const Matrix &m) {
+  if (m.format != VCLGB_HYB || m.tail_nnz == 0) return 0;
+  size_t nchunks = (m.tail_nnz + kTailChunk - 1) / kTailChunk;
+  return ((2 * nchunks * sizeof(uint32_t) + 15) / 16) * 16 + 2 * nchunks * 8 + 16;
+}
+
+}  // namespace vclgb

@@ -1,0 +1,293 @@
+// vclgb_internal.hpp -- shared host/device definitions of the GB300 sparse engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/vclgb.h"
+
+namespace vclgb {
+
+// ---------------------------------------------------------------------------
+// errors: every C entry point catches these and turns them into a status.
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  vclgbStatus status;
+  Error(vclgbStatus s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+#define VCLGB_CUDA(call)                                                                  \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      if (e_ == cudaErrorMemoryAllocation)                                                \
+        throw ::vclgb::Error(VCLGB_OUT_OF_MEMORY, std::string(#call) + ": " +             \
+                                                      cudaGetErrorString(e_));            \
+      throw ::vclgb::Error(VCLGB_CUDA_ERROR,                                              \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));           \
+    }                                                                                     \
+  } while (0)
+
+#define VCLGB_CHECK_LAUNCH() VCLGB_CUDA(cudaGetLastError())
+
+inline void require(bool ok, vclgbStatus s, const char *msg) {
+  if (!ok) throw Error(s, msg);
+}
+
+// ---------------------------------------------------------------------------
+// device memory owned by the engine (stream-ordered pool allocations)
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf() = default;
+  DevBuf(size_t b, cudaStream_t s) { alloc(b, s); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept { *this = std::move(o); }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      ptr = o.ptr; bytes = o.bytes; stream = o.stream;
+      o.ptr = nullptr; o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t b, cudaStream_t s) {
+    release();
+    stream = s;
+    bytes = b;
+    if (b) VCLGB_CUDA(cudaMallocAsync(&ptr, b, s));
+  }
+  void release() noexcept {
+    if (ptr) cudaFreeAsync(ptr, stream);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// ---------------------------------------------------------------------------
+// backend
+// ---------------------------------------------------------------------------
+struct Backend {
+  int device = 0;
+  int num_sms = 152;
+  int max_threads_per_sm = 2048;
+  size_t max_smem_per_block = 48 * 1024;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string last_error;
+  uint64_t launches = 0;
+  // pinned host word the solvers poll (convergence / status)
+  int *host_flags = nullptr;
+  // persistent reduction scratch for the vector reductions
+  DevBuf red_partials;
+  DevBuf red_counter;
+};
+
+// grid size for grid-stride kernels: a whole number of waves on the 152 SMs
+inline int waves_grid(const Backend &be, int threads, int blocks_per_sm_cap, size_t work_items,
+                      int items_per_thread = 1) {
+  int per_sm = be.max_threads_per_sm / threads;
+  if (per_sm > blocks_per_sm_cap) per_sm = blocks_per_sm_cap;
+  if (per_sm < 1) per_sm = 1;
+  size_t full = (size_t)be.num_sms * per_sm;
+  size_t need = (work_items + (size_t)threads * items_per_thread - 1) /
+                ((size_t)threads * items_per_thread);
+  if (need < 1) need = 1;
+  return (int)(need < full ? need : full);
+}
+
+// ---------------------------------------------------------------------------
+// matrices
+// ---------------------------------------------------------------------------
+// Row-length bins of the adaptive CSR kernel: rows of one bin are handled by
+// groups of `lanes` threads (1..32) or, for lanes == 0, one block per row.
+struct CsrBin {
+  uint32_t lanes;      // 1,2,4,8,16,32 or 0 (= block per row)
+  uint32_t count;      // rows in the bin
+  uint32_t offset;     // offset into the bin row list (unused when identity)
+  uint32_t identity;   // 1: the bin is rows [0, count) in order (no row list)
+};
+
+constexpr int kMaxBins = 8;
+
+struct Matrix {
+  vclgbFormat format = VCLGB_CSR;
+  vclgbPrecision prec = VCLGB_FLOAT64;
+  uint32_t rows = 0, cols = 0;
+  uint64_t nnz = 0;
+  size_t vsize() const { return prec == VCLGB_FLOAT64 ? 8 : 4; }
+
+  // CSR (borrowed or owned)
+  const uint32_t *row_ptr = nullptr;
+  const uint32_t *col_idx = nullptr;
+  const void *values = nullptr;
+  DevBuf own_row_ptr, own_col_idx, own_values;
+  // adaptive-CSR analysis
+  int num_bins = 0;
+  CsrBin bins[kMaxBins];
+  DevBuf bin_rows;          // concatenated row lists of non-identity bins
+  uint32_t max_row_len = 0;
+  // reference row blocks (generate_row_block_information), built on demand
+  DevBuf row_blocks;
+  uint32_t num_row_blocks = 0;
+  bool row_blocks_built = false;
+
+  // ELL / HYB-ELL part: coords[item*rows + row], elems[...]
+  uint32_t ell_width = 0;
+  DevBuf ell_coords, ell_elems;
+
+  // SELL-C-sigma
+  uint32_t C = 32, sigma = 1, num_slices = 0;
+  uint64_t sell_stored = 0;
+  DevBuf sell_cpb, sell_start, sell_cols, sell_elems, sell_perm;
+
+  // HYB tail: reference CSR arrays + COO rows for the segmented kernel
+  uint64_t tail_nnz = 0;     // real tail entries (0 if empty)
+  DevBuf tail_rp, tail_ci, tail_v, tail_row;
+
+  // cached FP32 copy used by the mixed-precision solvers
+  std::unique_ptr<Matrix> f32_copy;
+  // cached FP32 copy of D^-1/2 A D^-1/2 and D^-1/2 (FP64) for refined CG
+  std::unique_ptr<Matrix> f32_scaled;
+  DevBuf inv_sqrt_diag;
+  // diagonal (FP64 or FP32), built on demand for Jacobi
+  DevBuf diag;
+  bool diag_built = false;
+};
+
+struct Precond {
+  int kind = 0;  // 1 jacobi, 2 ilu0
+  vclgbPrecision prec = VCLGB_FLOAT64;
+  uint32_t rows = 0;
+  DevBuf diag;   // jacobi: diag(A); ilu0: U diagonal
+  // ILU0
+  bool level_scheduling = true;
+  uint64_t nnz = 0;
+  DevBuf lu;                // factors in A's pattern
+  const uint32_t *row_ptr = nullptr, *col_idx = nullptr;  // A's pattern (borrowed)
+  struct Tri {
+    uint32_t levels = 0;
+    uint64_t rows = 0, nnz = 0;
+    std::vector<uint32_t> h_level_ptr;
+    DevBuf level_ptr, row_index, row_ptr, cols, vals;
+  } L, U;
+};
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int LANES, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = LANES / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block reduction of NV values per thread.  Result valid in
+// thread 0.  smem must hold NV * (blockDim.x/32) values.
+template <int NV, typename T>
+__device__ __forceinline__ void block_sum(T (&v)[NV], T *smem) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) smem[i * nw + warp] = v[i];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      T t = lane < nw ? smem[i * nw + lane] : T(0);
+      v[i] = warp_sum(t);
+    }
+  }
+}
+
+// Grid-level two-stage reduction: every block writes NV partials, the last
+// block to arrive sums all partials in a fixed order (deterministic) and
+// returns true in thread 0 with the sums in out[].  counter is reset.
+template <int NV, typename T>
+__device__ __forceinline__ bool grid_reduce(T (&v)[NV], T *partials, unsigned *counter, T *smem,
+                                            T (&out)[NV]) {
+  block_sum<NV>(v, smem);
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) partials[(size_t)i * gridDim.x + blockIdx.x] = v[i];
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  T acc[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    T s = 0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+      s += ((volatile T *)partials)[(size_t)i * gridDim.x + b];
+    acc[i] = s;
+  }
+  block_sum<NV>(acc, smem);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = acc[i];
+    *counter = 0;
+  }
+  return threadIdx.x == 0;
+}
+#endif
+
+// C-ABI plumbing
+template <typename F>
+vclgbStatus guarded(Backend *be, F &&f) {
+  try {
+    f();
+    return VCLGB_SUCCESS;
+  } catch (const Error &e) {
+    if (be) be->last_error = e.what();
+    return e.status;
+  } catch (const std::bad_alloc &) {
+    if (be) be->last_error = "host allocation failed";
+    return VCLGB_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    if (be) be->last_error = e.what();
+    return VCLGB_GENERIC_FAILURE;
+  } catch (...) {
+    if (be) be->last_error = "unknown failure";
+    return VCLGB_GENERIC_FAILURE;
+  }
+}
+
+inline Backend *B(vclgbBackend h) { return reinterpret_cast<Backend *>(h); }
+inline Matrix *M(vclgbMatrix h) { return reinterpret_cast<Matrix *>(h); }
+inline Precond *P(vclgbPrecond h) { return reinterpret_cast<Precond *>(h); }
+
+// implemented in the .cu files
+void csr_analyse(Backend &be, Matrix &m);
+void csr_validate(Backend &be, const Matrix &m);
+
+}  // namespace vclgb

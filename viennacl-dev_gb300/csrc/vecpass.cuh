@@ -1,0 +1,111 @@
+// vecpass.cuh -- one generic grid-stride vector kernel with an optional fused
+// deterministic reduction, and the iteration runner used by every solver.
+#pragma once
+
+#include "spmv.cuh"
+
+namespace vclgb {
+
+constexpr int kVecThreads = 256;
+
+// F: NDOT, skip(), apply(i, dots), finalize(sums)
+template <typename T, class F>
+__global__ void __launch_bounds__(kVecThreads)
+    vec_pass_kernel(size_t n, F f, T *partials, unsigned *counter) {
+  if (f.skip()) return;
+  __shared__ T smem[4 * (kVecThreads / 32) + 8];
+  T dots[DotArr<F::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<F::NDOT>::n; ++i) dots[i] = T(0);
+  const auto sc = f.load();  // per-thread copy of the step's device scalars
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // two independent elements per step for memory-level parallelism
+  for (; i + stride < n; i += 2 * stride) {
+    f.apply(i, sc, dots);
+    f.apply(i + stride, sc, dots);
+  }
+  if (i < n) f.apply(i, sc, dots);
+  if constexpr (F::NDOT > 0) {
+    T sums[F::NDOT];
+    if (grid_reduce<F::NDOT>(dots, partials, counter, smem, sums)) f.finalize(sums);
+  }
+}
+
+inline int vec_grid(const Backend &be, size_t n) { return waves_grid(be, kVecThreads, 8, n, 4); }
+
+template <typename T, class F>
+void vec_pass(Backend &be, size_t n, const F &f, const Reduction &red) {
+  vec_pass_kernel<T, F><<<vec_grid(be, n), kVecThreads, 0, be.stream>>>(
+      n, f, static_cast<T *>(red.partials), red.counter);
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
+// a single-thread device step (scalar bookkeeping between passes)
+template <class F>
+__global__ void scalar_step_kernel(F f) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) f();
+}
+template <class F>
+void scalar_step(Backend &be, const F &f) {
+  scalar_step_kernel<F><<<1, 32, 0, be.stream>>>(f);
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
+// solver status words (device)
+enum : int { kRunning = 0, kConverged = 1, kMaxIters = 2, kBreakdown = 3 };
+
+// Launches `one_iteration` (which enqueues the kernels of one solver
+// iteration and returns how many it launched) in chunks of check_every
+// iterations, captured once into a CUDA graph and replayed; after every
+// chunk the host reads the device status word.  Kernels of a finished solve
+// return at their first instruction, so overshooting is harmless.
+template <class F>
+void run_iterations(Backend &be, const int *d_done, uint32_t max_chunks_hint, uint32_t check_every,
+                    bool use_graph, F &&one_iteration) {
+  if (check_every == 0) check_every = 16;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t per_chunk = 0;
+  if (use_graph) {
+    cudaGraph_t graph = nullptr;
+    VCLGB_CUDA(cudaStreamBeginCapture(be.stream, cudaStreamCaptureModeThreadLocal));
+    uint64_t before = be.launches;
+    try {
+      for (uint32_t i = 0; i < check_every; ++i) one_iteration();
+    } catch (...) {
+      cudaStreamEndCapture(be.stream, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    per_chunk = be.launches - before;
+    be.launches = before;
+    VCLGB_CUDA(cudaStreamEndCapture(be.stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    VCLGB_CUDA(e);
+  }
+  uint64_t chunks = 0;
+  const uint64_t limit = (uint64_t)max_chunks_hint + 4;
+  for (;;) {
+    if (exec) {
+      VCLGB_CUDA(cudaGraphLaunch(exec, be.stream));
+      be.launches += per_chunk;
+    } else {
+      for (uint32_t i = 0; i < check_every; ++i) one_iteration();
+    }
+    VCLGB_CUDA(cudaMemcpyAsync(be.host_flags, d_done, sizeof(int), cudaMemcpyDeviceToHost,
+                               be.stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    ++chunks;
+    if (*be.host_flags != kRunning) break;
+    if (chunks > limit) {
+      if (exec) cudaGraphExecDestroy(exec);
+      throw Error(VCLGB_TIMEOUT, "solver did not report completion within its iteration bound");
+    }
+  }
+  if (exec) VCLGB_CUDA(cudaGraphExecDestroy(exec));
+}
+
+}  // namespace vclgb

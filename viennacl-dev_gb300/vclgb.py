@@ -1,0 +1,499 @@
+"""Python mirror of ViennaCL's sparse/solver API on top of the GB300 engine.
+
+Names, argument meaning and results follow the reference so tests and
+benchmarks read like ViennaCL code:
+
+    A = compressed_matrix(row_ptr, cols, values, nrows, ncols)   # viennacl/compressed_matrix.hpp
+    E = ell_matrix(A); S = sliced_ell_matrix(A, 32, 256); H = hyb_matrix(A)
+    y = prod(A, x)                                               # viennacl/linalg/prod.hpp
+    x = solve(A, b, cg_tag(1e-8, 2000), jacobi_precond(A))       # viennacl/linalg/cg.hpp
+    tag.iters(), tag.error()
+
+Every call goes through the C ABI of include/vclgb.h (libvclgb.so) with raw
+device pointers; PyTorch only provides device memory and the current stream.
+There is no CPU fallback: importing this module without the built library,
+or using it without a CUDA device, raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libvclgb.so")
+
+SUCCESS, GENERIC_FAILURE, INVALID_ARGUMENT, INVALID_MATRIX, OUT_OF_MEMORY, CUDA_ERROR, \
+    NOT_CONVERGED, BREAKDOWN, ZERO_ON_DIAGONAL, TIMEOUT, UNSUPPORTED = range(11)
+STATUS_NAMES = ["SUCCESS", "GENERIC_FAILURE", "INVALID_ARGUMENT", "INVALID_MATRIX",
+                "OUT_OF_MEMORY", "CUDA_ERROR", "NOT_CONVERGED", "BREAKDOWN",
+                "ZERO_ON_DIAGONAL", "TIMEOUT", "UNSUPPORTED"]
+FLOAT32, FLOAT64 = 0, 1
+CSR, ELL, SELL, HYB = 0, 1, 2, 3
+
+
+class VclgbError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES)
+                                     else status, msg))
+        self.status = status
+
+
+class MatrixInfo(ctypes.Structure):
+    _fields_ = [("format", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("rows", ctypes.c_uint32), ("cols", ctypes.c_uint32),
+                ("nnz", ctypes.c_uint64), ("stored", ctypes.c_uint64),
+                ("ell_width", ctypes.c_uint32), ("slice_height", ctypes.c_uint32),
+                ("sigma", ctypes.c_uint32), ("num_slices", ctypes.c_uint32),
+                ("tail_nnz", ctypes.c_uint64), ("num_bins", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class SolverTag(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("abs_tol", ctypes.c_double),
+                ("max_iters", ctypes.c_uint32), ("krylov_dim", ctypes.c_uint32),
+                ("max_iters_before_restart", ctypes.c_uint32), ("check_every", ctypes.c_uint32),
+                ("iters", ctypes.c_uint32), ("status", ctypes.c_uint32),
+                ("error", ctypes.c_double)]
+
+
+class Ilu0Info(ctypes.Structure):
+    _fields_ = [("num_levels_L", ctypes.c_uint32), ("num_levels_U", ctypes.c_uint32),
+                ("rows_L", ctypes.c_uint64), ("rows_U", ctypes.c_uint64),
+                ("nnz_L", ctypes.c_uint64), ("nnz_U", ctypes.c_uint64)]
+
+
+_lib = None
+_P = ctypes.c_void_p
+_U32, _U64, _I64, _I32, _D, _F = (ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64,
+                                 ctypes.c_int, ctypes.c_double, ctypes.c_float)
+
+# exported symbol -> (restype, argtypes); mirrors include/vclgb.h
+SIGNATURES = {
+    "vclgbVersion": (ctypes.c_char_p, []),
+    "vclgbBackendCreate": (_I32, [ctypes.POINTER(_P), _P]),
+    "vclgbBackendDestroy": (_I32, [ctypes.POINTER(_P)]),
+    "vclgbBackendSetStream": (_I32, [_P, _P]),
+    "vclgbBackendSynchronize": (_I32, [_P]),
+    "vclgbBackendLastError": (ctypes.c_char_p, [_P]),
+    "vclgbBackendLaunchCount": (_U64, [_P]),
+    "vclgbCsrCreate": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, _P, ctypes.POINTER(_P)]),
+    "vclgbMatrixToEll": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "vclgbMatrixToSell": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
+    "vclgbMatrixToHyb": (_I32, [_P, _P, _D, ctypes.POINTER(_P)]),
+    "vclgbMatrixToFloat32": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "vclgbMatrixDestroy": (_I32, [ctypes.POINTER(_P)]),
+    "vclgbMatrixGetInfo": (_I32, [_P, ctypes.POINTER(MatrixInfo)]),
+    "vclgbMatrixExport": (_I32, [_P, _P, _I32, _P]),
+    "vclgbCsrRowBlockCount": (_I32, [_P, _P, ctypes.POINTER(_U32)]),
+    "vclgbSpmv": (_I32, [_P, _P, _D, _P, _I64, _I64, _D, _P, _I64, _I64]),
+    "vclgbDot": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, _P]),
+    "vclgbNorm2": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P]),
+    "vclgbJacobiCreate": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "vclgbIlu0Create": (_I32, [_P, _P, _I32, ctypes.POINTER(_P)]),
+    "vclgbPrecondApply": (_I32, [_P, _P, _P]),
+    "vclgbPrecondDestroy": (_I32, [ctypes.POINTER(_P)]),
+    "vclgbIlu0GetInfo": (_I32, [_P, ctypes.POINTER(Ilu0Info)]),
+    "vclgbIlu0Export": (_I32, [_P, _P, _I32, _P]),
+    "vclgbSolverTagInit": (None, [ctypes.POINTER(SolverTag), _I32]),
+    "vclgbSolveCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
+    "vclgbSolveBiCGStab": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
+    "vclgbSolveGMRES": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag)]),
+    "vclgbSolveMixedCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _F]),
+    "vclgbSolveRefinedCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _D, _U32,
+                                   ctypes.POINTER(_U32)]),
+}
+
+
+def load_library(path=_LIB_PATH):
+    """Loads libvclgb.so and declares every C-ABI signature (no GPU needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libvclgb.so is not built (run __graft_entry__.build()): %s" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
+    return torch
+
+
+_backend = None
+
+
+class Backend:
+    """ViennaCLBackend: one stream, device scalars, error messages."""
+
+    def __init__(self, stream=None):
+        lib = load_library()
+        torch = _torch()
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        h = _P()
+        self._check_raw(lib.vclgbBackendCreate(ctypes.byref(h), _P(stream)), None)
+        self.h = h
+        self.lib = lib
+
+    def _check_raw(self, st, h):
+        if st != SUCCESS:
+            msg = load_library().vclgbBackendLastError(h).decode() if h else ""
+            raise VclgbError(st, msg)
+
+    def check(self, st, allow=()):
+        if st != SUCCESS and st not in allow:
+            raise VclgbError(st, self.lib.vclgbBackendLastError(self.h).decode())
+        return st
+
+    def synchronize(self):
+        self.check(self.lib.vclgbBackendSynchronize(self.h))
+
+    def launches(self):
+        return int(self.lib.vclgbBackendLaunchCount(self.h))
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.vclgbBackendDestroy(ctypes.byref(self.h))
+        except Exception:
+            pass
+
+
+def backend():
+    """The process-wide default backend (created on first use)."""
+    global _backend
+    if _backend is None:
+        _backend = Backend()
+    return _backend
+
+
+def _dtype_prec(dtype):
+    torch = _torch()
+    if dtype == torch.float64:
+        return FLOAT64
+    if dtype == torch.float32:
+        return FLOAT32
+    raise TypeError("only float32/float64 are supported")
+
+
+def _dev(a, dtype):
+    """numpy/torch -> contiguous CUDA tensor of dtype."""
+    torch = _torch()
+    if isinstance(a, np.ndarray):
+        a = torch.from_numpy(np.ascontiguousarray(a))
+    return a.to(device="cuda", dtype=dtype).contiguous()
+
+
+def _ptr(t):
+    return _P(t.data_ptr()) if t is not None and t.numel() else _P(0)
+
+
+class _Matrix:
+    fmt = None
+
+    def __init__(self):
+        self.h = None
+        self.be = None
+        self._keep = []
+
+    def info(self):
+        inf = MatrixInfo()
+        self.be.check(self.be.lib.vclgbMatrixGetInfo(self.h, ctypes.byref(inf)))
+        return inf
+
+    def size1(self):
+        return self.info().rows
+
+    def size2(self):
+        return self.info().cols
+
+    def nnz(self):
+        return self.info().nnz
+
+    @property
+    def dtype(self):
+        torch = _torch()
+        return torch.float64 if self.info().precision == FLOAT64 else torch.float32
+
+    def export(self, which, count, dtype):
+        torch = _torch()
+        out = torch.empty(max(int(count), 1), dtype=dtype, device="cuda")
+        self.be.check(self.be.lib.vclgbMatrixExport(self.be.h, self.h, which, _ptr(out)))
+        return out[:int(count)]
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.be.lib.vclgbMatrixDestroy(ctypes.byref(self.h))
+        except Exception:
+            pass
+
+
+class compressed_matrix(_Matrix):
+    """viennacl::compressed_matrix wrapping device CSR arrays (uint32 indices)."""
+    fmt = CSR
+
+    def __init__(self, row_ptr, cols, values, nrows=None, ncols=None, dtype=None, be=None):
+        super().__init__()
+        torch = _torch()
+        self.be = be or backend()
+        if dtype is None:
+            dtype = values.dtype if isinstance(values, torch.Tensor) else (
+                torch.float64 if np.asarray(values).dtype == np.float64 else torch.float32)
+            if isinstance(values, np.ndarray):
+                dtype = torch.float64 if values.dtype == np.float64 else torch.float32
+        rp = _dev(np.asarray(row_ptr, dtype=np.uint32).view(np.int32)
+                  if not isinstance(row_ptr, torch.Tensor) else row_ptr, torch.int32)
+        ci = _dev(np.asarray(cols, dtype=np.uint32).view(np.int32)
+                  if not isinstance(cols, torch.Tensor) else cols, torch.int32)
+        va = _dev(values, dtype)
+        n = int(nrows if nrows is not None else rp.numel() - 1)
+        m = int(ncols if ncols is not None else n)
+        self.row_ptr, self.cols, self.values = rp, ci, va
+        h = _P()
+        self.be.check(self.be.lib.vclgbCsrCreate(self.be.h, _dtype_prec(dtype), n, m, int(va.numel()),
+                                                 _ptr(rp), _ptr(ci), _ptr(va), ctypes.byref(h)))
+        self.h = h
+
+    def row_blocks(self):
+        torch = _torch()
+        c = _U32()
+        self.be.check(self.be.lib.vclgbCsrRowBlockCount(self.be.h, self.h, ctypes.byref(c)))
+        return self.export(3, c.value + 1, torch.int32)
+
+
+class _Converted(_Matrix):
+    def __init__(self, src, fn, *args):
+        super().__init__()
+        if not isinstance(src, compressed_matrix):
+            raise TypeError("conversions start from a compressed_matrix")
+        self.be = src.be
+        self._src = src  # the CSR arrays stay alive with the converted matrix
+        h = _P()
+        self.be.check(fn(self.be.h, src.h, *args, ctypes.byref(h)))
+        self.h = h
+
+
+class ell_matrix(_Converted):
+    """viennacl::ell_matrix built on the GPU from a compressed_matrix."""
+    fmt = ELL
+
+    def __init__(self, csr):
+        super().__init__(csr, load_library().vclgbMatrixToEll)
+
+
+class sliced_ell_matrix(_Converted):
+    """viennacl::sliced_ell_matrix (SELL-C-sigma) built on the GPU."""
+    fmt = SELL
+
+    def __init__(self, csr, rows_per_block=32, sigma=1):
+        super().__init__(csr, load_library().vclgbMatrixToSell, int(rows_per_block), int(sigma))
+
+
+class hyb_matrix(_Converted):
+    """viennacl::hyb_matrix built on the GPU (csr_threshold as hyb_matrix.hpp:44)."""
+    fmt = HYB
+
+    def __init__(self, csr, csr_threshold=0.8):
+        super().__init__(csr, load_library().vclgbMatrixToHyb, float(csr_threshold))
+
+
+def prod(A, x, alpha=1.0, y=None, beta=0.0, x_start=0, x_stride=1, y_start=0, y_stride=1,
+         y_size=None):
+    """linalg::prod_impl(A, x, alpha, y, beta): y = alpha*A*x + beta*y on the GPU."""
+    torch = _torch()
+    dt = A.dtype
+    x = x if (isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == dt) else _dev(x, dt)
+    if y is None:
+        y = torch.empty(y_size or A.size1(), dtype=dt, device="cuda")
+    A.be.check(A.be.lib.vclgbSpmv(A.be.h, A.h, float(alpha), _ptr(x), x_start, x_stride,
+                                  float(beta), _ptr(y), y_start, y_stride))
+    return y
+
+
+def inner_prod(x, y, be=None):
+    """linalg::inner_prod -> device scalar (0-d tensor)."""
+    torch = _torch()
+    be = be or backend()
+    out = torch.empty((), dtype=x.dtype, device="cuda")
+    be.check(be.lib.vclgbDot(be.h, _dtype_prec(x.dtype), x.numel(), _ptr(x), 0, 1, _ptr(y), 0, 1,
+                             _ptr(out)))
+    return out
+
+
+def norm_2(x, be=None):
+    """linalg::norm_2 -> device scalar (0-d tensor)."""
+    torch = _torch()
+    be = be or backend()
+    out = torch.empty((), dtype=x.dtype, device="cuda")
+    be.check(be.lib.vclgbNorm2(be.h, _dtype_prec(x.dtype), x.numel(), _ptr(x), 0, 1, _ptr(out)))
+    return out
+
+
+# ---- tags -------------------------------------------------------------------
+class _Tag:
+    kind = 0
+
+    def __init__(self, tol, max_iterations, krylov_dim=0, max_before_restart=0, check_every=0):
+        self.t = SolverTag()
+        load_library().vclgbSolverTagInit(ctypes.byref(self.t), self.kind)
+        self.t.tol = tol
+        self.t.max_iters = max_iterations
+        if krylov_dim:
+            self.t.krylov_dim = krylov_dim
+        if max_before_restart:
+            self.t.max_iters_before_restart = max_before_restart
+        self.t.check_every = check_every
+
+    def tolerance(self):
+        return self.t.tol
+
+    def abs_tolerance(self, v=None):
+        if v is not None and v >= 0:
+            self.t.abs_tol = v
+        return self.t.abs_tol
+
+    def max_iterations(self):
+        return self.t.max_iters
+
+    def iters(self):
+        return self.t.iters
+
+    def error(self):
+        return self.t.error
+
+    def status(self):
+        return self.t.status
+
+
+class cg_tag(_Tag):
+    kind = 0
+
+    def __init__(self, tol=1e-8, max_iterations=300, check_every=0):
+        super().__init__(tol, max_iterations, check_every=check_every)
+
+
+class bicgstab_tag(_Tag):
+    kind = 1
+
+    def __init__(self, tol=1e-8, max_iters=400, max_iters_before_restart=200, check_every=0):
+        super().__init__(tol, max_iters, max_before_restart=max_iters_before_restart,
+                         check_every=check_every)
+
+
+class gmres_tag(_Tag):
+    kind = 2
+
+    def __init__(self, tol=1e-10, max_iterations=300, krylov_dim=20):
+        super().__init__(tol, max_iterations, krylov_dim=krylov_dim)
+
+
+class mixed_precision_cg_tag(_Tag):
+    kind = 0
+
+    def __init__(self, tol=1e-8, max_iterations=300, inner_tol=1e-2):
+        super().__init__(tol, max_iterations)
+        self.inner_tol = inner_tol
+
+
+class refined_cg_tag(_Tag):
+    """FP64 iterative refinement around FP32 Jacobi-PCG inner solves (new form)."""
+    kind = 0
+
+    def __init__(self, tol=1e-10, max_iterations=100000, inner_tol=1e-4, max_outer=30):
+        super().__init__(tol, max_iterations)
+        self.inner_tol = inner_tol
+        self.max_outer = max_outer
+        self.outer = 0
+
+
+# ---- preconditioners ----------------------------------------------------------
+class _Precond:
+    def __init__(self, A, fn, *args):
+        self.be = A.be
+        self._A = A
+        h = _P()
+        self.be.check(fn(self.be.h, A.h, *args, ctypes.byref(h)))
+        self.h = h
+
+    def apply(self, vec):
+        self.be.check(self.be.lib.vclgbPrecondApply(self.be.h, self.h, _ptr(vec)))
+        return vec
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.be.lib.vclgbPrecondDestroy(ctypes.byref(self.h))
+        except Exception:
+            pass
+
+
+class jacobi_precond(_Precond):
+    """jacobi_precond<compressed_matrix>(A, jacobi_tag())."""
+
+    def __init__(self, A, tag=None):
+        super().__init__(A, load_library().vclgbJacobiCreate)
+
+
+class ilu0_precond(_Precond):
+    """ilu0_precond<compressed_matrix>(A, ilu0_tag(use_level_scheduling))."""
+
+    def __init__(self, A, use_level_scheduling=True):
+        super().__init__(A, load_library().vclgbIlu0Create, 1 if use_level_scheduling else 0)
+
+    def info(self):
+        inf = Ilu0Info()
+        self.be.check(self.be.lib.vclgbIlu0GetInfo(self.h, ctypes.byref(inf)))
+        return inf
+
+    def levels(self):
+        return self.info().num_levels_L
+
+    def export(self, which, count, dtype):
+        torch = _torch()
+        out = torch.empty(max(int(count), 1), dtype=dtype, device="cuda")
+        self.be.check(self.be.lib.vclgbIlu0Export(self.be.h, self.h, which, _ptr(out)))
+        return out[:int(count)]
+
+
+def solve(A, b, tag, precond=None, x=None):
+    """linalg::solve(A, b, tag[, precond]) -> x (device tensor).
+
+    Raises on failures other than NOT_CONVERGED/BREAKDOWN, which the reference
+    reports only through tag.iters()/tag.error(); those are in tag.status()."""
+    torch = _torch()
+    dt = A.dtype
+    b = b if (isinstance(b, torch.Tensor) and b.is_cuda and b.dtype == dt) else _dev(b, dt)
+    if x is None:
+        x = torch.empty(A.size1(), dtype=dt, device="cuda")
+    be, lib = A.be, A.be.lib
+    t = ctypes.byref(tag.t)
+    ok = (NOT_CONVERGED, BREAKDOWN)
+    if isinstance(tag, refined_cg_tag):
+        outer = _U32()
+        be.check(lib.vclgbSolveRefinedCG(be.h, A.h, _ptr(b), _ptr(x), t, tag.inner_tol,
+                                         tag.max_outer, ctypes.byref(outer)), ok)
+        tag.outer = outer.value
+    elif isinstance(tag, mixed_precision_cg_tag):
+        be.check(lib.vclgbSolveMixedCG(be.h, A.h, _ptr(b), _ptr(x), t, tag.inner_tol), ok)
+    elif isinstance(tag, cg_tag):
+        be.check(lib.vclgbSolveCG(be.h, A.h, _ptr(b), _ptr(x), t,
+                                  precond.h if precond else _P(0)), ok)
+    elif isinstance(tag, bicgstab_tag):
+        be.check(lib.vclgbSolveBiCGStab(be.h, A.h, _ptr(b), _ptr(x), t,
+                                        precond.h if precond else _P(0)), ok)
+    elif isinstance(tag, gmres_tag):
+        if precond is not None:
+            raise VclgbError(UNSUPPORTED, "GMRES is provided without a preconditioner")
+        be.check(lib.vclgbSolveGMRES(be.h, A.h, _ptr(b), _ptr(x), t), ok)
+    else:
+        raise TypeError("unknown solver tag")
+    return x
