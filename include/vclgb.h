@@ -240,6 +240,50 @@ VCLGB_API vclgbStatus vclgbSolveRefinedCG(vclgbBackend be, vclgbMatrix A, const 
                                           void *d_x, vclgbSolverTag *tag, double inner_tol,
                                           uint32_t max_outer, uint32_t *outer_iters);
 
+/* ---- batched solves (no reference counterpart) ----------------------------
+ * Many independent systems, given as the diagonal blocks of one FP64
+ * block-diagonal CSR matrix A: system k owns rows [sys_ptr[k], sys_ptr[k+1])
+ * and every entry of those rows lies in the same column range (checked:
+ * VCLGB_INVALID_MATRIX otherwise).  method[k] = 0 runs the pipelined CG of
+ * cg.hpp:128-187, 1 the pipelined BiCGStab of bicgstab.hpp:96-215, each with
+ * the reference's stopping test.  One persistent launch solves the batch:
+ * CTAs pull whole systems from a device work queue, largest first, and each
+ * system stops on its own convergence test.  The batch keeps a pointer to A
+ * (destroy the batch first).  h_* arrays are host arrays of num_systems. */
+typedef struct vclgbBatch_st *vclgbBatch;
+VCLGB_API vclgbStatus vclgbBatchCreate(vclgbBackend be, vclgbMatrix A, uint32_t num_systems,
+                                       const uint32_t *h_sys_ptr, const int32_t *h_methods,
+                                       vclgbBatch *out);
+/* Autotunes block size (128/256/512) and lanes per row (1/2/4/8) on every
+ * eighth system; block/lanes (optional) receive the choice. */
+VCLGB_API vclgbStatus vclgbBatchTune(vclgbBackend be, vclgbBatch batch, const void *d_b,
+                                     int32_t *block, int32_t *lanes);
+/* Solves all systems to relative tolerance tol (x overwritten, initial guess
+ * 0).  Per-system iterations, status (vclgbStatus) and residual estimate are
+ * written to the optional host arrays.  Returns VCLGB_SUCCESS when every
+ * system converged, VCLGB_NOT_CONVERGED otherwise. */
+VCLGB_API vclgbStatus vclgbBatchSolve(vclgbBackend be, vclgbBatch batch, const void *d_b,
+                                      void *d_x, double tol, uint32_t max_iters,
+                                      uint32_t *h_iters, int32_t *h_status, double *h_error);
+VCLGB_API vclgbStatus vclgbBatchDestroy(vclgbBatch *batch);
+
+/* ---- adjoint (backward) solve (no reference counterpart) ------------------
+ * For x = A^-1 b (the forward solve) and dL/dx: solves A^T lambda = dL/dx with
+ * solver 0 = CG, 1 = BiCGStab, 2 = GMRES (tag as for the forward solvers;
+ * precond: NULL or a Jacobi preconditioner of A, which is also one of A^T),
+ * writes dL/db = lambda (length rows) and, if d_dLdA != NULL, the gradient
+ * on the sparsity pattern dL/dA_ij = -lambda_i x_j (length nnz, in A's entry
+ * order).  symmetric != 0 uses A itself; otherwise A^T is built once on the
+ * device with a map to A's entries and cached on A. */
+VCLGB_API vclgbStatus vclgbSolveAdjoint(vclgbBackend be, vclgbMatrix A, int solver,
+                                        vclgbPrecond precond, const void *d_x,
+                                        const void *d_dLdx, void *d_dLdb, void *d_dLdA,
+                                        vclgbSolverTag *tag, int symmetric);
+/* The cached transpose of A (built on first use): 0 row_ptr u32[cols+1],
+ * 1 cols u32[nnz], 2 values T[nnz], 3 map u32[nnz] (A entry of each A^T entry). */
+VCLGB_API vclgbStatus vclgbTransposeExport(vclgbBackend be, vclgbMatrix A, int which,
+                                           void *d_dst);
+
 #ifdef __cplusplus
 }
 #endif

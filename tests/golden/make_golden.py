@@ -103,6 +103,30 @@ def main():
     save("mixed_cg_laplace2d.npz", rp=rp, ci=ci, v=v, b=b, tol=1e-8, max_iters=3000,
          inner_tol=1e-2, x=r["x"], iters=r["iters"], error=r["error"])
 
+    # adjoint: forward solve and the transpose solve A^T lambda = x - x_t with the
+    # reference host backend (Jacobi-BiCGStab for the nonsymmetric case -- the
+    # host GMRES stagnates below 1e-12 on it because of its stage-1 defect --
+    # and Jacobi-PCG for the SPD diffusion case); dL/dA = -lambda_i x_j
+    rp, ci, v = gen.convdiff2d(20, 18, peclet=10.0, shift=0.1)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 21)
+    xt = np.random.default_rng(22).uniform(0.0, 1.0, n)
+    x = oracle.run_ref("bicgstab", rp, ci, v, args=(1e-14, 3000, "jacobi"), b=b)["x"]
+    trp, tci, tv, mp = oracle.transpose(n, n, rp, ci, v)
+    lam = oracle.run_ref("bicgstab", trp, tci, tv, args=(1e-14, 3000, "jacobi"), b=x - xt)["x"]
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    save("adjoint_convdiff.npz", rp=rp, ci=ci, v=v, b=b, xt=xt, x=x, lam=lam,
+         dLdA=-lam[rows] * x[ci], trp=trp, tci=tci, tv=tv, map=mp)
+    rp, ci, v, _ = gen.diffusion2d_edges(24, contrast=1e3, seed=4)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 23)
+    xt = np.random.default_rng(24).uniform(0.0, 1.0, n)
+    x = oracle.run_ref("cg", rp, ci, v, args=(1e-13, 5000, "jacobi"), b=b)["x"]
+    lam = oracle.run_ref("cg", rp, ci, v, args=(1e-13, 5000, "jacobi"), b=x - xt)["x"]
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    save("adjoint_diffusion2d.npz", rp=rp, ci=ci, v=v, b=b, xt=xt, x=x, lam=lam,
+         dLdA=-lam[rows] * x[ci])
+
     # ILU0 factors, level sets (L and U) and the level-scheduled apply
     rp, ci, v = gen.convdiff2d(23, 19, peclet=5.0, shift=0.2)
     n = len(rp) - 1

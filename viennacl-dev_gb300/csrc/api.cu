@@ -14,6 +14,17 @@ void gmres_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *);
 void mixed_cg_solve(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, float);
 void refined_cg_solve(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, double,
                       uint32_t, uint32_t *);
+struct Batch;
+Batch *batch_create(Backend &, const Matrix &, uint32_t, const uint32_t *, const int32_t *);
+void batch_tune(Backend &, Batch &, const double *);
+bool batch_solve(Backend &, Batch &, const double *, double *, double, uint32_t, uint32_t *,
+                 int32_t *, double *);
+void batch_config(const Batch &, int *, int *);
+void batch_destroy(Batch *);
+template <typename T>
+void adjoint_solve(Backend &, Matrix &, int, const Precond *, const T *, const T *, T *, T *,
+                   vclgbSolverTag *, bool);
+void transpose_export(Backend &, Matrix &, int, void *);
 }  // namespace vclgb
 
 using namespace vclgb;
@@ -279,14 +290,19 @@ VCLGB_API vclgbStatus vclgbSpmv(vclgbBackend h, vclgbMatrix A, double alpha, con
     DevBuf hyb;
     if (m.format == VCLGB_HYB && m.tail_nnz) hyb.alloc(hyb_scratch_bytes(m), be->stream);
     if (m.prec == VCLGB_FLOAT64) {
-      EpiAxpby<double> e{alpha, beta, static_cast<double *>(y), ys, yinc};
-      spmv_launch<double>(*be, m, static_cast<const double *>(x), xs, xinc, e, red,
-                          static_cast<double *>(y), ys, yinc, alpha, beta, nullptr, hyb.ptr);
+      with_axpby_mode(alpha, beta, [&](auto mode) {
+        EpiAxpbyM<double, decltype(mode)::value> e{alpha, beta, static_cast<double *>(y), ys,
+                                                   yinc};
+        spmv_launch<double>(*be, m, static_cast<const double *>(x), xs, xinc, e, red,
+                            static_cast<double *>(y), ys, yinc, alpha, beta, nullptr, hyb.ptr);
+      });
     } else {
-      EpiAxpby<float> e{(float)alpha, (float)beta, static_cast<float *>(y), ys, yinc};
-      spmv_launch<float>(*be, m, static_cast<const float *>(x), xs, xinc, e, red,
-                         static_cast<float *>(y), ys, yinc, (float)alpha, (float)beta, nullptr,
-                         hyb.ptr);
+      const float af = (float)alpha, bf = (float)beta;
+      with_axpby_mode(af, bf, [&](auto mode) {
+        EpiAxpbyM<float, decltype(mode)::value> e{af, bf, static_cast<float *>(y), ys, yinc};
+        spmv_launch<float>(*be, m, static_cast<const float *>(x), xs, xinc, e, red,
+                           static_cast<float *>(y), ys, yinc, af, bf, nullptr, hyb.ptr);
+      });
     }
   });
 }
@@ -438,6 +454,85 @@ VCLGB_API vclgbStatus vclgbSolveRefinedCG(vclgbBackend h, vclgbMatrix A, const v
     refined_cg_solve(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag,
                      inner_tol, max_outer, outer_iters);
   });
+}
+
+// ---------------------------------------------------------------------------
+VCLGB_API vclgbStatus vclgbBatchCreate(vclgbBackend h, vclgbMatrix A, uint32_t nsys,
+                                       const uint32_t *h_sys_ptr, const int32_t *h_methods,
+                                       vclgbBatch *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    Batch *bt = batch_create(*be, *M(A), nsys, h_sys_ptr, h_methods);
+    *out = reinterpret_cast<vclgbBatch>(bt);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbBatchTune(vclgbBackend h, vclgbBatch bt, const void *b, int32_t *block,
+                                     int32_t *lanes) {
+  if (!h || !bt || !b) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    Batch &batch = *reinterpret_cast<Batch *>(bt);
+    batch_tune(*be, batch, static_cast<const double *>(b));
+    int bb = 0, ll = 0;
+    batch_config(batch, &bb, &ll);
+    if (block) *block = bb;
+    if (lanes) *lanes = ll;
+  });
+}
+
+VCLGB_API vclgbStatus vclgbBatchSolve(vclgbBackend h, vclgbBatch bt, const void *b, void *x,
+                                      double tol, uint32_t max_iters, uint32_t *h_iters,
+                                      int32_t *h_status, double *h_error) {
+  if (!h || !bt || !b || !x) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  Batch &batch = *reinterpret_cast<Batch *>(bt);
+  bool all = false;
+  vclgbStatus s = guarded(be, [&]() {
+    all = batch_solve(*be, batch, static_cast<const double *>(b), static_cast<double *>(x), tol,
+                      max_iters, h_iters, h_status, h_error);
+  });
+  if (s != VCLGB_SUCCESS) return s;
+  return all ? VCLGB_SUCCESS : VCLGB_NOT_CONVERGED;
+}
+
+VCLGB_API vclgbStatus vclgbBatchDestroy(vclgbBatch *bt) {
+  if (!bt || !*bt) return VCLGB_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  batch_destroy(reinterpret_cast<Batch *>(*bt));
+  *bt = nullptr;
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbSolveAdjoint(vclgbBackend h, vclgbMatrix A, int solver, vclgbPrecond P,
+                                        const void *x, const void *dLdx, void *dLdb, void *dLdA,
+                                        vclgbSolverTag *tag, int symmetric) {
+  if (!h || !A || !x || !dLdx || !dLdb || !tag) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  vclgbStatus s = guarded(be, [&]() {
+    Matrix &m = *M(A);
+    const Precond *pc = P ? vclgb::P(P) : nullptr;
+    if (m.prec == VCLGB_FLOAT64)
+      adjoint_solve<double>(*be, m, solver, pc, static_cast<const double *>(x),
+                            static_cast<const double *>(dLdx), static_cast<double *>(dLdb),
+                            static_cast<double *>(dLdA), tag, symmetric != 0);
+    else
+      adjoint_solve<float>(*be, m, solver, pc, static_cast<const float *>(x),
+                           static_cast<const float *>(dLdx), static_cast<float *>(dLdb),
+                           static_cast<float *>(dLdA), tag, symmetric != 0);
+  });
+  if (s != VCLGB_SUCCESS) {
+    tag->status = s;
+    return s;
+  }
+  return (vclgbStatus)tag->status;
+}
+
+VCLGB_API vclgbStatus vclgbTransposeExport(vclgbBackend h, vclgbMatrix A, int which, void *dst) {
+  if (!h || !A || !dst) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { transpose_export(*be, *M(A), which, dst); });
 }
 
 }  // extern "C"

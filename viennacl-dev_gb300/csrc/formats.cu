@@ -113,6 +113,10 @@ uint64_t exclusive_scan(Backend &be, const In *in, size_t n, Out *out) {
   return total;
 }
 
+uint64_t extern_scan_u32(Backend &be, const uint32_t *in, size_t n, uint32_t *out) {
+  return exclusive_scan<uint32_t, uint32_t>(be, in, n, out);
+}
+
 // ---------------------------------------------------------------------------
 // validation
 // ---------------------------------------------------------------------------
@@ -147,14 +151,16 @@ void csr_validate(Backend &be, const Matrix &m) {
 // ---------------------------------------------------------------------------
 // row-length analysis for the adaptive CSR kernel
 // ---------------------------------------------------------------------------
-// bin of a row: 0..5 = 1,2,4,8,16,32 lanes per row, 6 = one block per row
+// bin of a row: 0..5 = 1,2,4,8,16,32 lanes per row (each lane issues up to 8
+// loads per round, so bin q covers rows of up to 8 << q entries in one round),
+// 6 = one block per row for rows longer than 4096
 __device__ __host__ inline int lane_bin(uint32_t len) {
-  if (len <= 1) return 0;
-  if (len <= 2) return 1;
-  if (len <= 4) return 2;
-  if (len <= 8) return 3;
-  if (len <= 16) return 4;
-  if (len <= 1024) return 5;
+  if (len <= 8) return 0;
+  if (len <= 16) return 1;
+  if (len <= 32) return 2;
+  if (len <= 64) return 3;
+  if (len <= 128) return 4;
+  if (len <= 4096) return 5;
   return 6;
 }
 constexpr int kLaneBins = 7;
@@ -255,7 +261,7 @@ void csr_analyse(Backend &be, Matrix &m) {
   m.num_bins = 0;
   if (m.rows == 0) return;
   // near-uniform rows (stencils): one bin over all rows in order, no row list
-  if (maxlen <= 1024 && (double)maxlen <= 2.0 * avg + 1.0) {
+  if (maxlen <= 4096 && (double)maxlen <= 2.0 * avg + 1.0) {
     CsrBin b;
     b.lanes = kBinLanes[lane_bin(maxlen)];
     b.count = m.rows;

@@ -10,6 +10,8 @@ std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C,
 std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold);
 std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m);
 void csr_row_blocks(Backend &be, Matrix &m);
+// out[0..n) = exclusive scan of in, out[n] = total; returns the total (host-synchronising)
+uint64_t extern_scan_u32(Backend &be, const uint32_t *in, size_t n, uint32_t *out);
 
 // preconditioners (precond.cu)
 std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A);

@@ -60,10 +60,12 @@ struct McInit {
 struct EpiMc1 {  // tmp = A32 p; alpha = inner_ip / <tmp,p>
   static constexpr int NDOT = 1;
   float *tmp; const float *p; McSt *st;
+  struct Pre { float p; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t r, float acc, float (&d)[1]) const {
+  __device__ Pre pre(uint32_t r) const { return {p[r]}; }
+  __device__ void row(uint32_t r, float acc, const Pre &v, float (&d)[1]) const {
     tmp[r] = acc;
-    d[0] += acc * p[r];
+    d[0] += acc * v.p;
   }
   __device__ void finalize(const float (&s)[1]) const {
     st->iters += 1;
@@ -115,9 +117,11 @@ struct McAddX {  // x += x32
 struct EpiMcRes {  // res = b - A x (FP64); <res,res>; outer test
   static constexpr int NDOT = 1;
   double *res; const double *b; McSt *st;
+  struct Pre { double b; };
   __device__ bool skip() const { return st->restart_skip != 0; }
-  __device__ void row(uint32_t r, double acc, double (&d)[1]) const {
-    double v = b[r] - acc;
+  __device__ Pre pre(uint32_t r) const { return {b[r]}; }
+  __device__ void row(uint32_t r, double acc, const Pre &pv, double (&d)[1]) const {
+    double v = pv.b - acc;
     res[r] = v;
     d[0] += v * v;
   }
@@ -313,9 +317,11 @@ struct IrUpdate {  // x += ||r|| D^-1/2 y
 struct EpiIrResid {  // r = b - A x; ||r||^2
   static constexpr int NDOT = 1;
   double *r; const double *b; double *out;
+  struct Pre { double b; };
   __device__ bool skip() const { return false; }
-  __device__ void row(uint32_t i, double acc, double (&d)[1]) const {
-    double v = b[i] - acc;
+  __device__ Pre pre(uint32_t i) const { return {b[i]}; }
+  __device__ void row(uint32_t i, double acc, const Pre &pv, double (&d)[1]) const {
+    double v = pv.b - acc;
     r[i] = v;
     d[0] += v * v;
   }

@@ -59,11 +59,13 @@ template <typename T>
 struct EpiCgFirst {  // Ap = A p; alpha = rr/<p,Ap>; beta = (alpha^2 ||Ap||^2 - rr)/rr
   static constexpr int NDOT = 2;
   T *Ap; const T *p; St<T> *st;
+  struct Pre { T p; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t r, T acc, T (&d)[2]) const {
+  __device__ Pre pre(uint32_t r) const { return {p[r]}; }
+  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[2]) const {
     Ap[r] = acc;
     d[0] += acc * acc;
-    d[1] += p[r] * acc;
+    d[1] += v.p * acc;
   }
   __device__ void finalize(const T (&s)[2]) const {
     T rr = st->rr;
@@ -101,11 +103,13 @@ template <typename T>
 struct EpiCg {  // Ap = A p, <Ap,Ap>, <p,Ap>; convergence test; next alpha/beta
   static constexpr int NDOT = 2;
   T *Ap; const T *p; St<T> *st;
+  struct Pre { T p; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t r, T acc, T (&d)[2]) const {
+  __device__ Pre pre(uint32_t r) const { return {p[r]}; }
+  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[2]) const {
     Ap[r] = acc;
     d[0] += acc * acc;
-    d[1] += p[r] * acc;
+    d[1] += v.p * acc;
   }
   __device__ void finalize(const T (&s)[2]) const {
     st->iters += 1;
@@ -182,10 +186,12 @@ template <typename T>
 struct EpiPcg {  // tmp = A p; alpha = ip / <tmp,p>
   static constexpr int NDOT = 1;
   T *tmp; const T *p; St<T> *st;
+  struct Pre { T p; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t r, T acc, T (&d)[1]) const {
+  __device__ Pre pre(uint32_t r) const { return {p[r]}; }
+  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[1]) const {
     tmp[r] = acc;
-    d[0] += acc * p[r];
+    d[0] += acc * v.p;
   }
   __device__ void finalize(const T (&s)[1]) const {
     st->iters += 1;
@@ -284,10 +290,12 @@ template <typename T>
 struct EpiBicgAp {  // Ap = A p, <Ap, r0*>
   static constexpr int NDOT = 1;
   T *Ap; const T *r0; St<T> *st;
+  struct Pre { T r0; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t r, T acc, T (&d)[1]) const {
+  __device__ Pre pre(uint32_t r) const { return {r0[r]}; }
+  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[1]) const {
     Ap[r] = acc;
-    d[0] += acc * r0[r];
+    d[0] += acc * v.r0;
   }
   __device__ void finalize(const T (&s)[1]) const {
     st->iters += 1;
@@ -314,12 +322,14 @@ template <typename T>
 struct EpiBicgAs {  // As = A s, <As,As>, <s,As>, <As,r0*>; scalars; residual estimate
   static constexpr int NDOT = 3;
   T *As; const T *s_, *r0; St<T> *st;
+  struct Pre { T s, r0; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t r, T acc, T (&d)[3]) const {
+  __device__ Pre pre(uint32_t r) const { return {s_[r], r0[r]}; }
+  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[3]) const {
     As[r] = acc;
     d[0] += acc * acc;
-    d[1] += s_[r] * acc;
-    d[2] += acc * r0[r];
+    d[1] += v.s * acc;
+    d[2] += acc * v.r0;
   }
   __device__ void finalize(const T (&s)[3]) const {
     T alpha = st->r_r0 / st->Ap_r0;
@@ -402,11 +412,13 @@ struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0
   static constexpr int NDOT = 1;
   T *r, *p, *r0; const T *b, *dg; St<T> *st;
   bool jacobi;
+  struct Pre { T b, d; };
   __device__ bool skip() const { return st->restart_skip != 0; }
-  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
-    T v = b[i] - acc;
+  __device__ Pre pre(uint32_t i) const { return {b[i], jacobi ? dg[i] : T(1)}; }
+  __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
+    T v = pv.b - acc;
     if (jacobi) {
-      v = v / dg[i];
+      v = v / pv.d;
       p[i] = v;
       r0[i] = v;
       d[0] += v * v;
@@ -437,8 +449,12 @@ template <typename T>
 struct EpiStore {  // y = acc (optionally / d)
   static constexpr int NDOT = 0;
   T *y; const T *dg; const int *flag;
+  struct Pre { T d; };
   __device__ bool skip() const { return flag && *flag != kRunning; }
-  __device__ void row(uint32_t i, T acc, T (&)[1]) const { y[i] = dg ? acc / dg[i] : acc; }
+  __device__ Pre pre(uint32_t i) const { return {dg ? dg[i] : T(1)}; }
+  __device__ void row(uint32_t i, T acc, const Pre &v, T (&)[1]) const {
+    y[i] = dg ? acc / v.d : acc;
+  }
   __device__ void finalize(const T (&)[1]) const {}
 };
 
@@ -446,11 +462,13 @@ template <typename T>
 struct EpiGb1 {  // t0 = M^-1 A p (Jacobi fused); <t0, r0*> -> alpha
   static constexpr int NDOT = 1;
   T *t0; const T *dg, *r0; St<T> *st;
+  struct Pre { T d, r0; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
-    T v = acc / dg[i];
+  __device__ Pre pre(uint32_t i) const { return {dg[i], r0[i]}; }
+  __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
+    T v = acc / pv.d;
     t0[i] = v;
-    d[0] += v * r0[i];
+    d[0] += v * pv.r0;
   }
   __device__ void finalize(const T (&s)[1]) const {
     st->iters += 1;
@@ -492,12 +510,14 @@ template <typename T>
 struct EpiGb2 {  // t1 = M^-1 A s (Jacobi fused); ||t1||^2, <t1,s> -> omega
   static constexpr int NDOT = 2;
   T *t1; const T *dg, *s_; St<T> *st;
+  struct Pre { T d, s; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ void row(uint32_t i, T acc, T (&d)[2]) const {
-    T v = acc / dg[i];
+  __device__ Pre pre(uint32_t i) const { return {dg[i], s_[i]}; }
+  __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[2]) const {
+    T v = acc / pv.d;
     t1[i] = v;
     d[0] += v * v;
-    d[1] += v * s_[i];
+    d[1] += v * pv.s;
   }
   __device__ void finalize(const T (&s)[2]) const { gb_omega(st, s[0], s[1]); }
 };
@@ -633,9 +653,11 @@ template <typename T>
 struct EpiGmResid {  // r = b - A x; rho0 = ||r||
   static constexpr int NDOT = 1;
   T *r; const T *b; Gm<T> *g;
+  struct Pre { T b; };
   __device__ bool skip() const { return g->done != kRunning; }
-  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
-    T v = b[i] - acc;
+  __device__ Pre pre(uint32_t i) const { return {b[i]}; }
+  __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
+    T v = pv.b - acc;
     r[i] = v;
     d[0] += v * v;
   }
@@ -660,8 +682,9 @@ template <typename T>
 struct EpiGmV {  // v_k = A src, ||v_k||^2 (used for k = 0)
   static constexpr int NDOT = 1;
   T *vk; Gm<T> *g;
+  VCLGB_NO_PRE
   __device__ bool skip() const { return g->done != kRunning; }
-  __device__ void row(uint32_t i, T acc, T (&d)[1]) const {
+  __device__ void row(uint32_t i, T acc, const Pre &, T (&d)[1]) const {
     vk[i] = acc;
     d[0] += acc * acc;
   }

@@ -4,7 +4,12 @@
 // Every kernel hands each finished row to an epilogue object E:
 //   static constexpr int NDOT;                    number of fused dot products
 //   bool skip() const;                            grid-uniform early exit
-//   void row(uint32_t r, T acc, T (&dots)[..])    store the row, add to dots
+//   Pre pre(uint32_t r) const;                    per-row operands of the
+//                                                 epilogue (y, p, b, diag ...),
+//                                                 loaded before the row's
+//                                                 products so the loads overlap
+//   void row(uint32_t r, T acc, const Pre &, T (&dots)[..])
+//                                                 store the row, add to dots
 //   void finalize(const T (&sums)[..]) const;     last block, thread 0
 // so the pipelined solvers fuse "Ap = A p" with their reductions, as the
 // reference's pipelined_*_prod kernels do (linalg/cuda/iterative_operations.hpp),
@@ -17,24 +22,57 @@ namespace vclgb {
 
 constexpr int kSpmvThreads = 256;
 
-// epilogue: y = alpha*acc + beta*y (linalg/cuda/sparse_matrix_operations.hpp prod_impl)
-template <typename T>
-struct EpiAxpby {
+#define VCLGB_NO_PRE                                                    \
+  struct Pre {};                                                        \
+  __device__ __forceinline__ Pre pre(uint32_t) const { return {}; }
+
+// GB300 executes FP64 arithmetic at a small fraction of its FP32 rate, and an
+// FP64 SpMV keeps that pipe busy with its one FMA per entry.  Everything else
+// a kernel does per row or per entry is therefore kept off the FP64 pipe:
+// the alpha/beta cases are resolved on the host (MODE), and padding zeros are
+// recognised by an integer test of the value's bits.
+__device__ __forceinline__ bool nonzero_bits(double v) {
+  return (__double_as_longlong(v) << 1) != 0;  // +0.0 and -0.0 are zero
+}
+__device__ __forceinline__ bool nonzero_bits(float v) { return (__float_as_int(v) << 1) != 0; }
+
+// epilogue: y = alpha*acc + beta*y (linalg/cuda/sparse_matrix_operations.hpp prod_impl).
+// MODE 0: alpha == 1, beta == 0; MODE 1: beta == 0; MODE 2: general (y read).
+template <typename T, int MODE>
+struct EpiAxpbyM {
   static constexpr int NDOT = 0;
   T alpha, beta;
   T *y;
   int64_t ys, yinc;
+  struct Pre { T yold; };
   __device__ __forceinline__ bool skip() const { return false; }
-  __device__ __forceinline__ void row(uint32_t r, T acc, T (&)[1]) const {
-    T *p = y + ys + (int64_t)r * yinc;
-    *p = (beta != T(0)) ? alpha * acc + beta * *p : alpha * acc;
+  __device__ __forceinline__ Pre pre(uint32_t r) const {
+    if constexpr (MODE == 2) return {y[ys + (int64_t)r * yinc]};
+    else return {T(0)};
+  }
+  __device__ __forceinline__ void row(uint32_t r, T acc, const Pre &pv, T (&)[1]) const {
+    T out;
+    if constexpr (MODE == 0) out = acc;
+    else if constexpr (MODE == 1) out = alpha * acc;
+    else out = alpha * acc + beta * pv.yold;
+    y[ys + (int64_t)r * yinc] = out;
   }
   __device__ __forceinline__ void finalize(const T (&)[1]) const {}
 };
+template <typename T>
+using EpiAxpby = EpiAxpbyM<T, 2>;
+
+// calls f(std::integral_constant<int, MODE>) for the alpha/beta case at hand
+template <typename T, class F>
+void with_axpby_mode(T alpha, T beta, F &&f) {
+  if (beta != T(0)) f(std::integral_constant<int, 2>{});
+  else if (alpha != T(1)) f(std::integral_constant<int, 1>{});
+  else f(std::integral_constant<int, 0>{});
+}
 
 // same, with an early-exit flag (solver converged)
-template <typename T>
-struct EpiAxpbySkip : EpiAxpby<T> {
+template <typename T, int MODE>
+struct EpiAxpbySkip : EpiAxpbyM<T, MODE> {
   const int *flag;
   __device__ __forceinline__ bool skip() const { return flag && *flag; }
 };
@@ -58,10 +96,16 @@ struct CsrView {
   uint32_t rows;
 };
 
-// rows of one bin, LANES threads per row, U rows per group per step; the
-// warp's groups take consecutive rows so that each load instruction of the
-// warp touches one contiguous stretch of the value/column arrays.
-template <int LANES, int U, typename T, class E>
+// Rows of one bin, LANES threads per row.  Each lane takes up to kMpl entries
+// of its row per round (lane, lane+LANES, ...) and issues every value, index
+// and x load of the round before the first multiply, so a warp keeps
+// 2*kMpl*32 independent loads in flight.  For rows of at most 8 entries
+// (stencils) LANES = 1: one thread per row, no shuffles.  The warp's groups
+// take consecutive rows, so the warp reads one contiguous stretch of the
+// value and index arrays.
+constexpr int kMpl = 8;
+
+template <int LANES, typename T, class E>
 __device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__restrict__ x,
                                                int64_t xs, int64_t xinc, uint32_t count,
                                                const uint32_t *__restrict__ list, const E &epi,
@@ -71,44 +115,31 @@ __device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__r
   const uint32_t gw = (threadIdx.x & 31) / LANES;
   const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-  constexpr uint32_t ROWS_PER_WARP = GPW * U;
-  for (size_t wb = warp * ROWS_PER_WARP; wb < count; wb += nwarps * ROWS_PER_WARP) {
-    uint32_t row[U], s[U], e[U];
-    T acc[U];
+  for (size_t wb = warp * GPW; wb < count; wb += nwarps * GPW) {
+    const size_t idx = wb + gw;
+    const bool ok = idx < count;
+    const uint32_t row = ok ? (list ? __ldg(list + idx) : (uint32_t)idx) : 0xffffffffu;
+    const uint32_t s = ok ? __ldg(A.rp + row) : 0u;
+    const uint32_t e = ok ? __ldg(A.rp + row + 1) : 0u;
+    typename E::Pre pv{};
+    if (ok && lane == 0) pv = epi.pre(row);
+    T acc = T(0);
+    for (uint32_t k0 = s + lane; k0 < e; k0 += kMpl * LANES) {
+      uint32_t c[kMpl];
+      T vv[kMpl];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      size_t idx = wb + (size_t)u * GPW + gw;
-      bool ok = idx < count;
-      row[u] = ok ? (list ? __ldg(list + idx) : (uint32_t)idx) : 0xffffffffu;
-      s[u] = ok ? __ldg(A.rp + row[u]) : 0u;
-      e[u] = ok ? __ldg(A.rp + row[u] + 1) : 0u;
-    }
-    // first chunk of every row: loads of all U rows are issued together
-    uint32_t c[U];
-    T vv[U];
+      for (int j = 0; j < kMpl; ++j) {
+        const uint32_t k = k0 + j * LANES;
+        const bool in = k < e;
+        c[j] = in ? __ldg(A.ci + k) : 0u;
+        vv[j] = in ? __ldg(A.v + k) : T(0);
+      }
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      uint32_t k = s[u] + lane;
-      bool ok = k < e[u];
-      c[u] = ok ? __ldg(A.ci + k) : 0u;
-      vv[u] = ok ? __ldg(A.v + k) : T(0);
+      for (int j = 0; j < kMpl; ++j)
+        if (k0 + j * LANES < e) acc += vv[j] * __ldg(x + xs + (int64_t)c[j] * xinc);
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      uint32_t k = s[u] + lane;
-      acc[u] = (k < e[u]) ? vv[u] * __ldg(x + xs + (int64_t)c[u] * xinc) : T(0);
-    }
-    // remaining chunks (rows longer than LANES)
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      for (uint32_t k = s[u] + lane + LANES; k < e[u]; k += LANES)
-        acc[u] += __ldg(A.v + k) * __ldg(x + xs + (int64_t)__ldg(A.ci + k) * xinc);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      T t = group_sum<LANES>(acc[u]);
-      if (lane == 0 && row[u] != 0xffffffffu) epi.row(row[u], t, dots);
-    }
+    if constexpr (LANES > 1) acc = group_sum<LANES>(acc);
+    if (lane == 0 && ok) epi.row(row, acc, pv, dots);
   }
 }
 
@@ -121,16 +152,20 @@ __device__ __forceinline__ void csr_rows_block(const CsrView<T> &A, const T *__r
   for (size_t i = blockIdx.x; i < count; i += gridDim.x) {
     uint32_t row = list ? __ldg(list + i) : (uint32_t)i;
     uint32_t s = __ldg(A.rp + row), e = __ldg(A.rp + row + 1);
+    typename E::Pre pv{};
+    if (threadIdx.x == 0) pv = epi.pre(row);
     T acc[1] = {T(0)};
     for (uint32_t k = s + threadIdx.x; k < e; k += blockDim.x)
       acc[0] += __ldg(A.v + k) * __ldg(x + xs + (int64_t)__ldg(A.ci + k) * xinc);
     block_sum<1>(acc, smem);
-    if (threadIdx.x == 0) epi.row(row, acc[0], dots);
+    if (threadIdx.x == 0) epi.row(row, acc[0], pv, dots);
     __syncthreads();
   }
 }
 
-template <typename T, class E>
+// FIXED > 0: the matrix is one identity bin of FIXED lanes per row (stencils),
+// compiled without the bin dispatch; FIXED == 0: the general binned kernel.
+template <int FIXED, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     csr_adaptive_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc,
                         BinTable bins, const uint32_t *__restrict__ bin_rows, E epi,
@@ -140,16 +175,19 @@ __global__ void __launch_bounds__(kSpmvThreads)
   T dots[DotArr<E::NDOT>::n];
 #pragma unroll
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  if constexpr (FIXED > 0) {
+    csr_rows_group<FIXED>(A, x, xs, xinc, A.rows, nullptr, epi, dots);
+  } else
   for (int b = 0; b < bins.n; ++b) {
     const CsrBin bin = bins.b[b];
     const uint32_t *list = bin.identity ? nullptr : bin_rows + bin.offset;
     switch (bin.lanes) {
-      case 1: csr_rows_group<1, 4>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 2: csr_rows_group<2, 4>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 4: csr_rows_group<4, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 8: csr_rows_group<8, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 16: csr_rows_group<16, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 32: csr_rows_group<32, 2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 1: csr_rows_group<1>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 2: csr_rows_group<2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 4: csr_rows_group<4>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 8: csr_rows_group<8>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 16: csr_rows_group<16>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 32: csr_rows_group<32>(A, x, xs, xinc, bin.count, list, epi, dots); break;
       default: csr_rows_block(A, x, xs, xinc, bin.count, list, epi, dots, smem); break;
     }
   }
@@ -163,7 +201,33 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // ELL: thread per row, column-major slots (ell_matrix.hpp layout); explicit
 // zeros are skipped like the reference kernels do.
 // ---------------------------------------------------------------------------
-template <typename T, class E>
+// W > 0: the width is a compile-time constant (fully unrolled, every load of
+// the row issued up front); W == 0: runtime width in rounds of 8.
+template <int W, typename T>
+__device__ __forceinline__ T ell_row(size_t r, uint32_t rows, uint32_t width,
+                                     const uint32_t *__restrict__ coords,
+                                     const T *__restrict__ elems, const T *__restrict__ x,
+                                     int64_t xs, int64_t xinc) {
+  constexpr int R = W > 0 ? W : 8;
+  T acc = 0;
+  for (uint32_t j0 = 0; j0 < (W > 0 ? (uint32_t)W : width); j0 += R) {
+    T val[R];
+    uint32_t col[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const bool in = W > 0 || j0 + q < width;
+      const size_t off = (size_t)(j0 + q) * rows + r;
+      val[q] = in ? __ldg(elems + off) : T(0);
+      col[q] = in ? __ldg(coords + off) : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+      if (nonzero_bits(val[q])) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+  }
+  return acc;
+}
+
+template <int W, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     ell_kernel(uint32_t rows, uint32_t width, const uint32_t *__restrict__ coords,
                const T *__restrict__ elems, const T *__restrict__ x, int64_t xs, int64_t xinc,
@@ -175,27 +239,9 @@ __global__ void __launch_bounds__(kSpmvThreads)
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
        r += (size_t)gridDim.x * blockDim.x) {
-    T acc = 0;
-    uint32_t j = 0;
-    for (; j + 4 <= width; j += 4) {
-      T val[4];
-      uint32_t col[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        size_t off = (size_t)(j + q) * rows + r;
-        val[q] = __ldg(elems + off);
-        col[q] = __ldg(coords + off);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (val[q] != T(0)) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
-    }
-    for (; j < width; ++j) {
-      size_t off = (size_t)j * rows + r;
-      T val = __ldg(elems + off);
-      if (val != T(0)) acc += val * __ldg(x + xs + (int64_t)__ldg(coords + off) * xinc);
-    }
-    epi.row((uint32_t)r, acc, dots);
+    const typename E::Pre pv = epi.pre((uint32_t)r);
+    T acc = ell_row<W>(r, rows, width, coords, elems, x, xs, xinc);
+    epi.row((uint32_t)r, acc, pv, dots);
   }
   if constexpr (E::NDOT > 0) {
     T sums[E::NDOT];
@@ -207,7 +253,33 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // SELL-C-sigma: thread per stored row position; slice s, lane l; element j of
 // the position at block_start[s] + j*C + l (sliced_ell_matrix.hpp layout).
 // ---------------------------------------------------------------------------
-template <typename T, class E>
+// one stored row position: element j at base + j*C, rounds of 8 loads
+template <typename T>
+__device__ __forceinline__ T sell_row(size_t base, uint32_t w, uint32_t C,
+                                      const uint32_t *__restrict__ cols,
+                                      const T *__restrict__ elems, const T *__restrict__ x,
+                                      int64_t xs, int64_t xinc) {
+  T acc = 0;
+  for (uint32_t j0 = 0; j0 < w; j0 += 8) {
+    T val[8];
+    uint32_t col[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const bool in = j0 + q < w;
+      const size_t off = base + (size_t)(j0 + q) * C;
+      val[q] = in ? __ldg(elems + off) : T(0);
+      col[q] = in ? __ldg(cols + off) : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (nonzero_bits(val[q])) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+  }
+  return acc;
+}
+
+// WARP: C is a multiple of 32 and each warp takes 32 consecutive positions of
+// one slice (no division per thread); otherwise thread per position.
+template <bool WARP, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     sell_kernel(uint32_t rows, uint32_t C, const uint32_t *__restrict__ cpb,
                 const uint32_t *__restrict__ start, const uint32_t *__restrict__ cols,
@@ -219,33 +291,30 @@ __global__ void __launch_bounds__(kSpmvThreads)
   T dots[DotArr<E::NDOT>::n];
 #pragma unroll
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
-  for (size_t pos = (size_t)blockIdx.x * blockDim.x + threadIdx.x; pos < rows;
-       pos += (size_t)gridDim.x * blockDim.x) {
-    uint32_t s = (uint32_t)(pos / C), l = (uint32_t)(pos % C);
-    uint32_t w = __ldg(cpb + s);
-    size_t base = (size_t)__ldg(start + s) + l;
-    T acc = 0;
-    uint32_t j = 0;
-    for (; j + 4 <= w; j += 4) {
-      T val[4];
-      uint32_t col[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        size_t off = base + (size_t)(j + q) * C;
-        val[q] = __ldg(elems + off);
-        col[q] = __ldg(cols + off);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (val[q] != T(0)) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+  if constexpr (WARP) {
+    const uint32_t lane = threadIdx.x & 31, per = C >> 5;
+    const uint32_t nsub = (rows + 31) >> 5;  // 32-position chunks
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nsub;
+         q += (gridDim.x * blockDim.x) >> 5) {
+      const uint32_t s = q / per, l = (q - s * per) * 32 + lane;
+      const uint32_t pos = q * 32 + lane;
+      const uint32_t row = pos < rows ? (perm ? __ldg(perm + pos) : pos) : 0u;
+      typename E::Pre pv{};
+      if (pos < rows) pv = epi.pre(row);
+      const T acc = sell_row(__ldg(start + s) + (size_t)l, __ldg(cpb + s), C, cols, elems, x,
+                             xs, xinc);
+      if (pos < rows) epi.row(row, acc, pv, dots);
     }
-    for (; j < w; ++j) {
-      size_t off = base + (size_t)j * C;
-      T val = __ldg(elems + off);
-      if (val != T(0)) acc += val * __ldg(x + xs + (int64_t)__ldg(cols + off) * xinc);
+  } else {
+    for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < rows;
+         pos += gridDim.x * blockDim.x) {
+      const uint32_t s = pos / C, l = pos - s * C;
+      const uint32_t row = perm ? __ldg(perm + pos) : pos;
+      const typename E::Pre pv = epi.pre(row);
+      const T acc = sell_row(__ldg(start + s) + (size_t)l, __ldg(cpb + s), C, cols, elems, x,
+                             xs, xinc);
+      epi.row(row, acc, pv, dots);
     }
-    uint32_t row = perm ? __ldg(perm + pos) : (uint32_t)pos;
-    epi.row(row, acc, dots);
   }
   if constexpr (E::NDOT > 0) {
     T sums[E::NDOT];
@@ -361,7 +430,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
        r += (size_t)gridDim.x * blockDim.x)
-    epi.row((uint32_t)r, y[r], dots);
+    epi.row((uint32_t)r, y[r], epi.pre((uint32_t)r), dots);
   if constexpr (E::NDOT > 0) {
     T sums[E::NDOT];
     if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
@@ -385,6 +454,27 @@ inline int spmv_grid(const Backend &be, const Matrix &m) {
 constexpr int kMaxSpmvGrid = 152 * 8 * 2;
 
 template <typename T, class E>
+void ell_launch(Backend &be, int grid, const Matrix &m, const T *x, int64_t xs, int64_t xinc,
+                const E &epi, T *partials, unsigned *counter) {
+#define VCLGB_ELL(W)                                                                          \
+  ell_kernel<W, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(                                  \
+      m.rows, m.ell_width, m.ell_coords.as<uint32_t>(), m.ell_elems.as<T>(), x, xs, xinc, epi, \
+      partials, counter)
+  switch (m.ell_width) {
+    case 1: VCLGB_ELL(1); break;
+    case 2: VCLGB_ELL(2); break;
+    case 3: VCLGB_ELL(3); break;
+    case 4: VCLGB_ELL(4); break;
+    case 5: VCLGB_ELL(5); break;
+    case 6: VCLGB_ELL(6); break;
+    case 7: VCLGB_ELL(7); break;
+    case 8: VCLGB_ELL(8); break;
+    default: VCLGB_ELL(0); break;
+  }
+#undef VCLGB_ELL
+}
+
+template <typename T, class E>
 void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t xinc, const E &epi,
                  const Reduction &red, T *y_for_hyb = nullptr, int64_t ys = 0, int64_t yinc = 1,
                  T alpha = T(1), T beta = T(0), const int *skip_flag = nullptr,
@@ -397,30 +487,47 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
       BinTable bt;
       bt.n = m.num_bins;
       for (int i = 0; i < m.num_bins; ++i) bt.b[i] = m.bins[i];
-      csr_adaptive_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-          A, x, xs, xinc, bt, m.bin_rows.as<uint32_t>(), epi, partials, red.counter);
+      const bool single = m.num_bins == 1 && m.bins[0].identity;
+      if (single && m.bins[0].lanes == 1)
+        csr_adaptive_kernel<1, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            A, x, xs, xinc, bt, nullptr, epi, partials, red.counter);
+      else if (single && m.bins[0].lanes == 2)
+        csr_adaptive_kernel<2, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            A, x, xs, xinc, bt, nullptr, epi, partials, red.counter);
+      else if (single && m.bins[0].lanes == 4)
+        csr_adaptive_kernel<4, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            A, x, xs, xinc, bt, nullptr, epi, partials, red.counter);
+      else
+        csr_adaptive_kernel<0, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            A, x, xs, xinc, bt, m.bin_rows.as<uint32_t>(), epi, partials, red.counter);
       break;
     }
     case VCLGB_ELL:
-      ell_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-          m.rows, m.ell_width, m.ell_coords.as<uint32_t>(), m.ell_elems.as<T>(), x, xs, xinc,
-          epi, partials, red.counter);
+      ell_launch<T, E>(be, grid, m, x, xs, xinc, epi, partials, red.counter);
       break;
     case VCLGB_SELL:
-      sell_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-          m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
-          m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
-          m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, x, xs, xinc, epi, partials,
-          red.counter);
+      if (m.C % 32 == 0)
+        sell_kernel<true, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
+            m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
+            m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, x, xs, xinc, epi, partials,
+            red.counter);
+      else
+        sell_kernel<false, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+            m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
+            m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
+            m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, x, xs, xinc, epi, partials,
+            red.counter);
       break;
     case VCLGB_HYB: {
       // y = alpha*ELL*x + beta*y, then y += alpha*tail*x, then the epilogue pass
-      EpiAxpbySkip<T> sp;
-      sp.alpha = alpha; sp.beta = beta; sp.y = y_for_hyb; sp.ys = ys; sp.yinc = yinc;
-      sp.flag = skip_flag;
-      ell_kernel<T, EpiAxpbySkip<T>><<<grid, kSpmvThreads, 0, be.stream>>>(
-          m.rows, m.ell_width, m.ell_coords.as<uint32_t>(), m.ell_elems.as<T>(), x, xs, xinc,
-          sp, partials, red.counter);
+      with_axpby_mode(alpha, beta, [&](auto mode) {
+        EpiAxpbySkip<T, decltype(mode)::value> sp;
+        sp.alpha = alpha; sp.beta = beta; sp.y = y_for_hyb; sp.ys = ys; sp.yinc = yinc;
+        sp.flag = skip_flag;
+        ell_launch<T, EpiAxpbySkip<T, decltype(mode)::value>>(be, grid, m, x, xs, xinc, sp,
+                                                              partials, red.counter);
+      });
       if (m.tail_nnz > 0) {
         size_t nchunks = (m.tail_nnz + kTailChunk - 1) / kTailChunk;
         uint32_t *carry_row = static_cast<uint32_t *>(hyb_scratch);

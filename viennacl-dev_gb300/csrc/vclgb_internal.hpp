@@ -122,6 +122,8 @@ struct CsrBin {
 
 constexpr int kMaxBins = 8;
 
+struct Transposed;  // adjoint.cu: A^T and its entry map
+
 struct Matrix {
   vclgbFormat format = VCLGB_CSR;
   vclgbPrecision prec = VCLGB_FLOAT64;
@@ -162,6 +164,8 @@ struct Matrix {
   // cached FP32 copy of D^-1/2 A D^-1/2 and D^-1/2 (FP64) for refined CG
   std::unique_ptr<Matrix> f32_scaled;
   DevBuf inv_sqrt_diag;
+  // cached transpose for the adjoint solve
+  std::shared_ptr<Transposed> transposed;
   // diagonal (FP64 or FP32), built on demand for Jacobi
   DevBuf diag;
   bool diag_built = false;

@@ -63,7 +63,18 @@ class Ilu0Info(ctypes.Structure):
 
 
 _lib = None
+_exiting = False  # set at interpreter exit: destructors then leave cleanup to process teardown
 _P = ctypes.c_void_p
+
+
+def _mark_exit():
+    global _exiting
+    _exiting = True
+
+
+import atexit  # noqa: E402
+
+atexit.register(_mark_exit)
 _U32, _U64, _I64, _I32, _D, _F = (ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64,
                                  ctypes.c_int, ctypes.c_double, ctypes.c_float)
 
@@ -101,6 +112,14 @@ SIGNATURES = {
     "vclgbSolveMixedCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _F]),
     "vclgbSolveRefinedCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _D, _U32,
                                    ctypes.POINTER(_U32)]),
+    "vclgbBatchCreate": (_I32, [_P, _P, _U32, _P, _P, ctypes.POINTER(_P)]),
+    "vclgbBatchTune": (_I32, [_P, _P, _P, ctypes.POINTER(ctypes.c_int32),
+                              ctypes.POINTER(ctypes.c_int32)]),
+    "vclgbBatchSolve": (_I32, [_P, _P, _P, _P, _D, _U32, _P, _P, _P]),
+    "vclgbBatchDestroy": (_I32, [ctypes.POINTER(_P)]),
+    "vclgbSolveAdjoint": (_I32, [_P, _P, _I32, _P, _P, _P, _P, _P, ctypes.POINTER(SolverTag),
+                                 _I32]),
+    "vclgbTransposeExport": (_I32, [_P, _P, _I32, _P]),
 }
 
 
@@ -160,6 +179,8 @@ class Backend:
         return int(self.lib.vclgbBackendLaunchCount(self.h))
 
     def __del__(self):
+        if _exiting:
+            return
         try:
             if getattr(self, "h", None):
                 self.lib.vclgbBackendDestroy(ctypes.byref(self.h))
@@ -230,6 +251,8 @@ class _Matrix:
         return out[:int(count)]
 
     def __del__(self):
+        if _exiting:
+            return
         try:
             if self.h:
                 self.be.lib.vclgbMatrixDestroy(ctypes.byref(self.h))
@@ -429,6 +452,8 @@ class _Precond:
         return vec
 
     def __del__(self):
+        if _exiting:
+            return
         try:
             if self.h:
                 self.be.lib.vclgbPrecondDestroy(ctypes.byref(self.h))
@@ -497,3 +522,77 @@ def solve(A, b, tag, precond=None, x=None):
     else:
         raise TypeError("unknown solver tag")
     return x
+
+
+# ---- batched solves (no reference counterpart) ---------------------------------
+class Batch:
+    """Independent systems = diagonal blocks of one block-diagonal CSR matrix.
+    methods[k]: 0 = pipelined CG, 1 = pipelined BiCGStab."""
+
+    def __init__(self, A, sys_ptr, methods):
+        self.be = A.be
+        self._A = A
+        self.sys_ptr = np.ascontiguousarray(sys_ptr, dtype=np.uint32)
+        self.methods = np.ascontiguousarray(methods, dtype=np.int32)
+        self.nsys = len(self.methods)
+        h = _P()
+        self.be.check(self.be.lib.vclgbBatchCreate(
+            self.be.h, A.h, self.nsys, self.sys_ptr.ctypes.data_as(_P),
+            self.methods.ctypes.data_as(_P), ctypes.byref(h)))
+        self.h = h
+
+    def tune(self, b):
+        blk, ln = ctypes.c_int32(), ctypes.c_int32()
+        self.be.check(self.be.lib.vclgbBatchTune(self.be.h, self.h, _ptr(b), ctypes.byref(blk),
+                                                 ctypes.byref(ln)))
+        return blk.value, ln.value
+
+    def solve(self, b, tol=1e-10, max_iters=10000, x=None):
+        torch = _torch()
+        b = b if (isinstance(b, torch.Tensor) and b.is_cuda) else _dev(b, torch.float64)
+        if x is None:
+            x = torch.empty_like(b)
+        it = np.zeros(self.nsys, np.uint32)
+        st = np.zeros(self.nsys, np.int32)
+        er = np.zeros(self.nsys, np.float64)
+        self.be.check(self.be.lib.vclgbBatchSolve(self.be.h, self.h, _ptr(b), _ptr(x), float(tol),
+                                                  int(max_iters), it.ctypes.data_as(_P),
+                                                  st.ctypes.data_as(_P), er.ctypes.data_as(_P)),
+                      (NOT_CONVERGED,))
+        return x, it, st, er
+
+    def __del__(self):
+        if _exiting:
+            return
+        try:
+            if self.h:
+                self.be.lib.vclgbBatchDestroy(ctypes.byref(self.h))
+        except Exception:
+            pass
+
+
+# ---- adjoint (backward) solve ---------------------------------------------------
+_SOLVER_IDS = {"cg": 0, "bicgstab": 1, "gmres": 2}
+
+
+def solve_adjoint(A, x, dLdx, tag, solver="cg", precond=None, symmetric=False, want_dA=True):
+    """Backward of x = A^-1 b: returns (dL/db, dL/dA on A's pattern or None)."""
+    torch = _torch()
+    dt = A.dtype
+    x = x if (isinstance(x, torch.Tensor) and x.is_cuda) else _dev(x, dt)
+    dLdx = dLdx if (isinstance(dLdx, torch.Tensor) and dLdx.is_cuda) else _dev(dLdx, dt)
+    lam = torch.empty(A.size1(), dtype=dt, device="cuda")
+    gA = torch.empty(max(A.nnz(), 1), dtype=dt, device="cuda") if want_dA else None
+    A.be.check(A.be.lib.vclgbSolveAdjoint(A.be.h, A.h, _SOLVER_IDS[solver],
+                                          precond.h if precond else _P(0), _ptr(x), _ptr(dLdx),
+                                          _ptr(lam), _ptr(gA) if want_dA else _P(0),
+                                          ctypes.byref(tag.t), 1 if symmetric else 0),
+               (NOT_CONVERGED, BREAKDOWN))
+    return lam, (gA[:A.nnz()] if want_dA else None)
+
+
+def transpose_export(A, which, count, dtype):
+    torch = _torch()
+    out = torch.empty(max(int(count), 1), dtype=dtype, device="cuda")
+    A.be.check(A.be.lib.vclgbTransposeExport(A.be.h, A.h, which, _ptr(out)))
+    return out[:int(count)]

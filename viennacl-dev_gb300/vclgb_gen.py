@@ -227,3 +227,45 @@ def convdiff2d(nx, ny=None, peclet=10.0, shift=0.0):
 
 def rhs_uniform(n, seed, lo=-1.0, hi=1.0):
     return np.random.default_rng(seed).uniform(lo, hi, n)
+
+
+def batch_systems(count=4096, lo=500, hi=20000, seed=3):
+    """Independent systems for the batched solver, as one block-diagonal CSR.
+
+    Sizes n_k are drawn log-uniform in [lo, hi] and rounded to a near-square
+    grid nx*ny.  Even k: SPD 2D 5-point Laplacian plus a diagonal shift
+    U[0.01, 1] (solved with CG); odd k: nonsymmetric upwind convection-diffusion
+    with Peclet number U[0.1, 50] (solved with BiCGStab).  Returns
+    (rp, ci, v, sys_ptr, methods, b) with b ~ U[-1, 1]."""
+    rng = np.random.default_rng(seed)
+    target = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    shifts = rng.uniform(0.01, 1.0, count)
+    pecl = rng.uniform(0.1, 50.0, count)
+    rps, cis, vs, sizes, methods = [], [], [], [], []
+    row0 = 0
+    nnz0 = 0
+    for k in range(count):
+        nx = max(2, int(round(np.sqrt(target[k]))))
+        ny = max(2, int(round(target[k] / nx)))
+        if k % 2 == 0:
+            rp, ci, v = laplace2d(nx, ny)
+            v = v.copy()
+            v[ci.astype(np.int64) == np.repeat(np.arange(nx * ny), np.diff(rp.astype(np.int64)))] += shifts[k]
+            methods.append(0)
+        else:
+            rp, ci, v = convdiff2d(nx, ny, peclet=pecl[k])
+            methods.append(1)
+        n = nx * ny
+        rps.append(rp[:-1].astype(np.int64) + nnz0)
+        cis.append(ci.astype(np.int64) + row0)
+        vs.append(v)
+        sizes.append(n)
+        row0 += n
+        nnz0 += int(rp[-1])
+    rp = np.concatenate(rps + [np.array([nnz0])]).astype(np.uint32)
+    ci = np.concatenate(cis).astype(np.uint32)
+    v = np.concatenate(vs)
+    sys_ptr = np.zeros(count + 1, np.uint32)
+    sys_ptr[1:] = np.cumsum(sizes)
+    b = rng.uniform(-1.0, 1.0, row0)
+    return rp, ci, v, sys_ptr, np.array(methods, np.int32), b
