@@ -284,6 +284,38 @@ VCLGB_API vclgbStatus vclgbSolveAdjoint(vclgbBackend be, vclgbMatrix A, int solv
 VCLGB_API vclgbStatus vclgbTransposeExport(vclgbBackend be, vclgbMatrix A, int which,
                                            void *d_dst);
 
+/* ---- HYB SpMV without allocation (no counterpart in the reference) --------
+ * For callers that may not allocate device memory at call time: plug-ins
+ * whose host application owns every device allocation through its own
+ * allocator, services that reserve their whole memory budget at start-up,
+ * and latency-bound loops that cannot take the synchronisation an
+ * allocation may cause.  The regular HYB product (vclgbSpmv) allocates a small
+ * carry buffer per call and the engine's matrix objects allocate when built;
+ * this entry point allocates nothing and needs no backend.
+ *
+ * y = alpha*A*x + beta*y for A given directly as the hyb_matrix arrays of the
+ * reference (hyb_matrix.hpp: handle2/handle = ELL coords/values of
+ * rows*ell_width slots, column-major; handle3/4/5 = tail row_ptr[rows+1],
+ * cols, values).  tail_nnz = tail_row_ptr[rows] (0 for an empty tail, whose
+ * arrays hold one placeholder entry).  x and y are contiguous, x has the
+ * matrix's column count, y has rows entries; the call is asynchronous on
+ * cuda_stream (NULL = legacy default stream).
+ *
+ * The tail's segmented reduction keeps its carries in one fixed device array
+ * inside the library, sized for tail_nnz <= 8,388,608 (768 KiB, held on
+ * every GPU that loads the library until the process exits); a larger tail
+ * returns VCLGB_INVALID_ARGUMENT before anything is launched.  The first call
+ * on a device looks up that array's device address with the device current
+ * (a one-time set-up); make the first call before any stream capture.  All
+ * calls on a device share the array and it keeps the last call's contents:
+ * calls that overlap on the GPU (different streams at the same time) race. */
+VCLGB_API vclgbStatus vclgbHybSpmvNoAlloc(void *cuda_stream, vclgbPrecision prec, uint32_t rows,
+                                          uint32_t ell_width, const uint32_t *d_ell_coords,
+                                          const void *d_ell_elems, const uint32_t *d_tail_row_ptr,
+                                          const uint32_t *d_tail_cols, const void *d_tail_vals,
+                                          uint64_t tail_nnz, double alpha, const void *d_x,
+                                          double beta, void *d_y);
+
 #ifdef __cplusplus
 }
 #endif

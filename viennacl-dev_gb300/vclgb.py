@@ -120,6 +120,8 @@ SIGNATURES = {
     "vclgbSolveAdjoint": (_I32, [_P, _P, _I32, _P, _P, _P, _P, _P, ctypes.POINTER(SolverTag),
                                  _I32]),
     "vclgbTransposeExport": (_I32, [_P, _P, _I32, _P]),
+    "vclgbHybSpmvNoAlloc": (_I32, [_P, _I32, _U32, _U32, _P, _P, _P, _P, _P, _U64, _D, _P, _D,
+                                   _P]),
 }
 
 
