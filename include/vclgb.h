@@ -101,6 +101,27 @@ VCLGB_API vclgbStatus vclgbMatrixToSell(vclgbBackend be, vclgbMatrix csr, uint32
                                         uint32_t sigma, vclgbMatrix *out);
 VCLGB_API vclgbStatus vclgbMatrixToHyb(vclgbBackend be, vclgbMatrix csr, double csr_threshold,
                                        vclgbMatrix *out);
+/* ell_matrix / sliced_ell_matrix / hyb_matrix that already live on the device
+ * in the reference's layout (the CUDA buffers behind their handle() ...
+ * handle5()), wrapped without copying; the arrays stay the caller's.
+ *   ELL : ell_matrix<T, 1> (ell_matrix.hpp:52-120): coords/elems of rows*width
+ *   SELL: sliced_ell_matrix<T, unsigned> (sliced_ell_matrix.hpp:45-133), sigma = 1
+ *   HYB : hyb_matrix<T, 1> (hyb_matrix.hpp:37-132); tail_nnz = tail_row_ptr[rows]
+ *         (the wrap derives the COO rows of the tail on the device). */
+VCLGB_API vclgbStatus vclgbEllWrap(vclgbBackend be, vclgbPrecision prec, uint32_t rows,
+                                   uint32_t cols, uint32_t width, const uint32_t *d_coords,
+                                   const void *d_elems, vclgbMatrix *out);
+VCLGB_API vclgbStatus vclgbSellWrap(vclgbBackend be, vclgbPrecision prec, uint32_t rows,
+                                    uint32_t cols, uint32_t slice_height,
+                                    const uint32_t *d_columns_per_block,
+                                    const uint32_t *d_column_indices,
+                                    const uint32_t *d_block_start, const void *d_elems,
+                                    vclgbMatrix *out);
+VCLGB_API vclgbStatus vclgbHybWrap(vclgbBackend be, vclgbPrecision prec, uint32_t rows,
+                                   uint32_t cols, uint32_t ell_width,
+                                   const uint32_t *d_ell_coords, const void *d_ell_elems,
+                                   const uint32_t *d_tail_row_ptr, const uint32_t *d_tail_cols,
+                                   const void *d_tail_vals, uint64_t tail_nnz, vclgbMatrix *out);
 /* FP32 copy of a matrix (same format and pattern), as mixed_precision_cg.hpp:128-137
  * builds for its inner iterations. */
 VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend be, vclgbMatrix m, vclgbMatrix *out);

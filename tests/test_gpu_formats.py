@@ -124,3 +124,96 @@ def test_full_size_lognormal_formats(V):
     A = V.compressed_matrix(rp, ci, v)
     for M in (A, V.sliced_ell_matrix(A, 32, 256), V.hyb_matrix(A)):
         assert rel_err(V.prod(M, x).cpu().numpy(), ref) < 1e-13
+
+
+def _same_nonfinite(out, ref):
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(out), fin)
+    assert np.array_equal(out[~fin], ref[~fin], equal_nan=True)
+    assert rel_err(out[fin], ref[fin]) < 1e-13
+
+
+def test_padded_formats_skip_stored_zeros(V):
+    # Stored zeros (ELL/SELL padding and explicit zeros) contribute nothing,
+    # as in the reference ELL and SELL kernels, even when x holds inf/NaN there:
+    # x[0] = inf reaches every padding slot (column 0), x[n] = NaN is hit only
+    # through explicit zeros appended to every 7th row.
+    rp, ci, v = gen.laplace2d(30, 23)
+    n = len(rp) - 1
+    lens = np.diff(rp)
+    extra = (np.arange(n) % 7 == 3).astype(np.int64)
+    rp2 = np.concatenate([[0], np.cumsum(lens + extra)]).astype(rp.dtype)
+    ci2 = np.empty(rp2[-1], dtype=ci.dtype)
+    v2 = np.empty(rp2[-1])
+    for r in range(n):
+        ci2[rp2[r]:rp2[r] + lens[r]] = ci[rp[r]:rp[r + 1]]
+        v2[rp2[r]:rp2[r] + lens[r]] = v[rp[r]:rp[r + 1]]
+        if extra[r]:
+            ci2[rp2[r + 1] - 1] = n
+            v2[rp2[r + 1] - 1] = 0.0
+    x = np.random.default_rng(8).uniform(-1, 1, n + 1)
+    x[0] = np.inf
+    x[n] = np.nan
+    ref = oracle.spmv(rp, ci, v, x)  # the same matrix without its explicit zeros
+    assert np.isinf(ref[0]) and np.isfinite(ref[n // 2])
+    A = V.compressed_matrix(rp2, ci2, v2, n, n + 1)
+    for M in (V.ell_matrix(A), V.sliced_ell_matrix(A, 32, 1), V.sliced_ell_matrix(A, 7, 8),
+              V.hyb_matrix(A, 1.0)):
+        _same_nonfinite(V.prod(M, x).cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_wrap_reference_layout(V, dtype):
+    # Buffers in the reference's ell/sliced_ell/hyb layout (exported from our
+    # conversions, which match the reference's copy() bit for bit) wrapped
+    # without copying give the same product as the converted matrices.
+    import torch
+    tdt = getattr(torch, dtype)
+    rp, ci, v = gen.lognormal_random(30000, mu=2.0, sigma=1.0, hi=400, seed=12)
+    n = len(rp) - 1
+    v = v.astype(np.float32) if dtype == "float32" else v
+    A = V.compressed_matrix(rp, ci, v)
+    x = np.random.default_rng(6).uniform(-1, 1, n).astype(v.dtype)
+    tol = 1e-5 if dtype == "float32" else 1e-13
+
+    E = V.ell_matrix(A)
+    w = E.info().ell_width
+    We = V.wrap_ell(n, n, w, E.export(0, n * w, torch.int32), E.export(1, n * w, tdt))
+    assert We.info().ell_width == w and We.info().format == V.ELL
+
+    S = V.sliced_ell_matrix(A, 32, 1)
+    si = S.info()
+    Ws = V.wrap_sliced_ell(n, n, 32, S.export(0, si.num_slices, torch.int32),
+                           S.export(1, si.stored, torch.int32),
+                           S.export(2, si.num_slices, torch.int32), S.export(3, si.stored, tdt))
+    assert Ws.info().stored == si.stored and Ws.info().num_slices == si.num_slices
+
+    H = V.hyb_matrix(A, 0.8)
+    hi = H.info()
+    trp = H.export(2, n + 1, torch.int32)
+    tnnz = int(_u32(trp)[-1])
+    assert tnnz > 0
+    Wh = V.wrap_hyb(n, n, hi.ell_width, H.export(0, n * hi.ell_width, torch.int32),
+                    H.export(1, n * hi.ell_width, tdt), trp, H.export(3, tnnz, torch.int32),
+                    H.export(4, tnnz, tdt))
+    ref = oracle.spmv(rp, ci, v, x)
+    for M, W in ((E, We), (S, Ws), (H, Wh)):
+        y = V.prod(M, x).cpu().numpy()
+        yw = V.prod(W, x).cpu().numpy()
+        assert np.array_equal(y, yw)
+        assert rel_err(yw, ref) < tol
+    # a solver runs on a wrapped matrix as on a converted one
+    if dtype == "float64":
+        rp2, ci2, v2 = gen.laplace2d(64, 64)
+        n2 = len(rp2) - 1
+        A2 = V.compressed_matrix(rp2, ci2, v2)
+        S2 = V.sliced_ell_matrix(A2, 32, 1)
+        s2 = S2.info()
+        W2 = V.wrap_sliced_ell(n2, n2, 32, S2.export(0, s2.num_slices, torch.int32),
+                               S2.export(1, s2.stored, torch.int32),
+                               S2.export(2, s2.num_slices, torch.int32),
+                               S2.export(3, s2.stored, torch.float64))
+        b = np.ones(n2)
+        tag = V.cg_tag(tol=1e-10, max_iterations=1000)
+        x2 = V.solve(W2, b, tag).cpu().numpy()
+        assert rel_err(oracle.spmv(rp2, ci2, v2, x2), b) < 1e-9

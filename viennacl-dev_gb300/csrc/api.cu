@@ -174,6 +174,94 @@ VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend h, vclgbMatrix m, vclgbM
   return convert(h, m, out, [&](Backend &be, Matrix &mm) { return convert_f32(be, mm); });
 }
 
+VCLGB_API vclgbStatus vclgbEllWrap(vclgbBackend h, vclgbPrecision prec, uint32_t rows,
+                                   uint32_t cols, uint32_t width, const uint32_t *coords,
+                                   const void *elems, vclgbMatrix *out) {
+  if (!h || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(prec == VCLGB_FLOAT32 || prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "bad precision");
+    require(!((size_t)rows * width) || (coords && elems), VCLGB_INVALID_ARGUMENT, "NULL arrays");
+    auto m = std::make_unique<Matrix>();
+    m->format = VCLGB_ELL;
+    m->prec = prec;
+    m->rows = rows;
+    m->cols = cols;
+    m->ell_width = width;
+    m->nnz = (uint64_t)rows * width;
+    m->ell_coords.borrow(coords, (size_t)rows * width * 4);
+    m->ell_elems.borrow(elems, (size_t)rows * width * m->vsize());
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbSellWrap(vclgbBackend h, vclgbPrecision prec, uint32_t rows,
+                                    uint32_t cols, uint32_t C, const uint32_t *cpb,
+                                    const uint32_t *colidx, const uint32_t *start,
+                                    const void *elems, vclgbMatrix *out) {
+  if (!h || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(prec == VCLGB_FLOAT32 || prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "bad precision");
+    require(C > 0, VCLGB_INVALID_ARGUMENT, "slice height must be positive");
+    auto m = std::make_unique<Matrix>();
+    m->format = VCLGB_SELL;
+    m->prec = prec;
+    m->rows = rows;
+    m->cols = cols;
+    m->C = C;
+    m->sigma = 1;
+    if (rows) {
+      require(cpb && colidx && start && elems, VCLGB_INVALID_ARGUMENT, "NULL arrays");
+      uint32_t ns = (rows - 1) / C + 1;
+      uint32_t last[2] = {0, 0};
+      VCLGB_CUDA(cudaMemcpyAsync(&last[0], start + ns - 1, 4, cudaMemcpyDeviceToHost, be->stream));
+      VCLGB_CUDA(cudaMemcpyAsync(&last[1], cpb + ns - 1, 4, cudaMemcpyDeviceToHost, be->stream));
+      VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+      m->num_slices = ns;
+      m->sell_stored = (uint64_t)last[0] + (uint64_t)last[1] * C;
+      m->nnz = m->sell_stored;
+      m->sell_cpb.borrow(cpb, (size_t)ns * 4);
+      m->sell_start.borrow(start, (size_t)ns * 4);
+      m->sell_cols.borrow(colidx, m->sell_stored * 4);
+      m->sell_elems.borrow(elems, m->sell_stored * m->vsize());
+    }
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbHybWrap(vclgbBackend h, vclgbPrecision prec, uint32_t rows,
+                                   uint32_t cols, uint32_t width, const uint32_t *ec,
+                                   const void *ee, const uint32_t *trp, const uint32_t *tci,
+                                   const void *tv, uint64_t tnnz, vclgbMatrix *out) {
+  if (!h || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(prec == VCLGB_FLOAT32 || prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "bad precision");
+    require(trp != nullptr, VCLGB_INVALID_ARGUMENT, "tail row_ptr is NULL");
+    require(!tnnz || (tci && tv), VCLGB_INVALID_ARGUMENT, "NULL tail arrays");
+    auto m = std::make_unique<Matrix>();
+    m->format = VCLGB_HYB;
+    m->prec = prec;
+    m->rows = rows;
+    m->cols = cols;
+    m->ell_width = width;
+    m->nnz = (uint64_t)rows * width + tnnz;
+    m->ell_coords.borrow(ec, (size_t)rows * width * 4);
+    m->ell_elems.borrow(ee, (size_t)rows * width * m->vsize());
+    m->tail_nnz = tnnz;
+    m->tail_rp.borrow(trp, ((size_t)rows + 1) * 4);
+    m->tail_ci.borrow(tci, std::max<uint64_t>(tnnz, 1) * 4);
+    m->tail_v.borrow(tv, std::max<uint64_t>(tnnz, 1) * m->vsize());
+    if (tnnz) {
+      m->tail_row.alloc(tnnz * 4, be->stream);
+      tail_rows_from_rp(*be, rows, trp, tnnz, m->tail_row.as<uint32_t>());
+      VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    }
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
 VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m) {
   if (!m || !*m) return VCLGB_INVALID_ARGUMENT;
   Matrix *mm = M(*m);

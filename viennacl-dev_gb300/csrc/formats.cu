@@ -616,6 +616,21 @@ std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double thres
   return out;
 }
 
+__global__ void tail_rows_kernel(uint32_t rows, const uint32_t *__restrict__ trp, uint32_t *trow) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x)
+    for (uint32_t k = trp[r]; k < trp[r + 1]; ++k) trow[k] = (uint32_t)r;
+}
+
+void tail_rows_from_rp(Backend &be, uint32_t rows, const uint32_t *trp, uint64_t tnnz,
+                       uint32_t *trow) {
+  if (!rows || !tnnz) return;
+  int g = waves_grid(be, 256, 8, rows);
+  tail_rows_kernel<<<g, 256, 0, be.stream>>>(rows, trp, trow);
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
 // ---------------------------------------------------------------------------
 // FP32 copy (same format, same index arrays shared by value copy)
 // ---------------------------------------------------------------------------

@@ -9,6 +9,9 @@ std::unique_ptr<Matrix> convert_ell(Backend &be, const Matrix &csr);
 std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C, uint32_t sigma);
 std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold);
 std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m);
+// COO row of every tail entry from the tail row_ptr (HYB wrapped from reference arrays)
+void tail_rows_from_rp(Backend &be, uint32_t rows, const uint32_t *trp, uint64_t tnnz,
+                       uint32_t *trow);
 void csr_row_blocks(Backend &be, Matrix &m);
 // out[0..n) = exclusive scan of in, out[n] = total; returns the total (host-synchronising)
 uint64_t extern_scan_u32(Backend &be, const uint32_t *in, size_t n, uint32_t *out);

@@ -96,16 +96,18 @@ struct CsrView {
   uint32_t rows;
 };
 
-// Rows of one bin, LANES threads per row.  Each lane takes up to kMpl entries
+// Rows of one bin, LANES threads per row.  Each lane takes up to MPL entries
 // of its row per round (lane, lane+LANES, ...) and issues every value, index
 // and x load of the round before the first multiply, so a warp keeps
-// 2*kMpl*32 independent loads in flight.  For rows of at most 8 entries
+// 2*MPL*32 independent loads in flight.  For rows of at most 8 entries
 // (stencils) LANES = 1: one thread per row, no shuffles.  The warp's groups
 // take consecutive rows, so the warp reads one contiguous stretch of the
-// value and index arrays.
+// value and index arrays.  A slot past the row's end is predicated off but
+// its FMA still takes an FP64 issue slot, so a stencil matrix whose longest
+// row has 3..7 entries runs with MPL equal to that length.
 constexpr int kMpl = 8;
 
-template <int LANES, typename T, class E>
+template <int LANES, int MPL, typename T, class E>
 __device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__restrict__ x,
                                                int64_t xs, int64_t xinc, uint32_t count,
                                                const uint32_t *__restrict__ list, const E &epi,
@@ -124,18 +126,18 @@ __device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__r
     typename E::Pre pv{};
     if (ok && lane == 0) pv = epi.pre(row);
     T acc = T(0);
-    for (uint32_t k0 = s + lane; k0 < e; k0 += kMpl * LANES) {
-      uint32_t c[kMpl];
-      T vv[kMpl];
+    for (uint32_t k0 = s + lane; k0 < e; k0 += MPL * LANES) {
+      uint32_t c[MPL];
+      T vv[MPL];
 #pragma unroll
-      for (int j = 0; j < kMpl; ++j) {
+      for (int j = 0; j < MPL; ++j) {
         const uint32_t k = k0 + j * LANES;
         const bool in = k < e;
         c[j] = in ? __ldg(A.ci + k) : 0u;
         vv[j] = in ? __ldg(A.v + k) : T(0);
       }
 #pragma unroll
-      for (int j = 0; j < kMpl; ++j)
+      for (int j = 0; j < MPL; ++j)
         if (k0 + j * LANES < e) acc += vv[j] * __ldg(x + xs + (int64_t)c[j] * xinc);
     }
     if constexpr (LANES > 1) acc = group_sum<LANES>(acc);
@@ -164,8 +166,9 @@ __device__ __forceinline__ void csr_rows_block(const CsrView<T> &A, const T *__r
 }
 
 // FIXED > 0: the matrix is one identity bin of FIXED lanes per row (stencils),
-// compiled without the bin dispatch; FIXED == 0: the general binned kernel.
-template <int FIXED, typename T, class E>
+// compiled without the bin dispatch, MPL entries per lane and round;
+// FIXED == 0: the general binned kernel.
+template <int FIXED, int MPL, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     csr_adaptive_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc,
                         BinTable bins, const uint32_t *__restrict__ bin_rows, E epi,
@@ -176,18 +179,18 @@ __global__ void __launch_bounds__(kSpmvThreads)
 #pragma unroll
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
   if constexpr (FIXED > 0) {
-    csr_rows_group<FIXED>(A, x, xs, xinc, A.rows, nullptr, epi, dots);
+    csr_rows_group<FIXED, MPL>(A, x, xs, xinc, A.rows, nullptr, epi, dots);
   } else
   for (int b = 0; b < bins.n; ++b) {
     const CsrBin bin = bins.b[b];
     const uint32_t *list = bin.identity ? nullptr : bin_rows + bin.offset;
     switch (bin.lanes) {
-      case 1: csr_rows_group<1>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 2: csr_rows_group<2>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 4: csr_rows_group<4>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 8: csr_rows_group<8>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 16: csr_rows_group<16>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 32: csr_rows_group<32>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 1: csr_rows_group<1, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 2: csr_rows_group<2, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 4: csr_rows_group<4, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 8: csr_rows_group<8, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 16: csr_rows_group<16, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
+      case 32: csr_rows_group<32, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
       default: csr_rows_block(A, x, xs, xinc, bin.count, list, epi, dots, smem); break;
     }
   }
@@ -198,33 +201,95 @@ __global__ void __launch_bounds__(kSpmvThreads)
 }
 
 // ---------------------------------------------------------------------------
-// ELL: thread per row, column-major slots (ell_matrix.hpp layout); explicit
-// zeros are skipped like the reference kernels do.
+// Padded formats (ELL, SELL, the ELL part of HYB) store explicit zeros that the
+// reference kernels skip (ELL) or replace by a literal 0 (SELL).  For finite x
+// an unconditional FMA of a stored zero adds +-0 and leaves the sum unchanged,
+// so the fast path multiplies every slot and issues all x loads up front; a
+// value-dependent predicate would make each x load wait for its element load.
+// Only a non-finite sum (inf/NaN reached through x) can differ: that row is
+// recomputed with stored zeros skipped, the reference result.
 // ---------------------------------------------------------------------------
-// W > 0: the width is a compile-time constant (fully unrolled, every load of
-// the row issued up front); W == 0: runtime width in rounds of 8.
+// exponent not all ones (integer test, off the FP64 pipe)
+__device__ __forceinline__ bool finite_bits(double v) {
+  return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000;
+}
+__device__ __forceinline__ bool finite_bits(float v) {
+  return (__float_as_int(v) & 0x7f800000) != 0x7f800000;
+}
+
+template <typename T>
+__device__ __forceinline__ T strided_row_skip(size_t base, uint32_t w, size_t stride,
+                                           const uint32_t *__restrict__ cols,
+                                           const T *__restrict__ elems, const T *__restrict__ x,
+                                           int64_t xs, int64_t xinc) {
+  T acc = 0;
+  for (uint32_t j = 0; j < w; ++j) {
+    const T v = elems[base + (size_t)j * stride];
+    if (nonzero_bits(v)) acc += v * x[xs + (int64_t)cols[base + (size_t)j * stride] * xinc];
+  }
+  return acc;
+}
+
+// slots j0 .. j0+R-1 of a row stored at base + j*stride: all R value and
+// index loads, then all R x loads, then the R FMAs in slot order
+template <int R, typename T>
+__device__ __forceinline__ T strided_round(T acc, size_t base, uint32_t j0, size_t stride,
+                                           const uint32_t *__restrict__ cols,
+                                           const T *__restrict__ elems,
+                                           const T *__restrict__ x, int64_t xs, int64_t xinc) {
+  T val[R];
+  uint32_t col[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const size_t off = base + (size_t)(j0 + q) * stride;
+    val[q] = __ldg(elems + off);
+    col[q] = __ldg(cols + off);
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+  return acc;
+}
+
+// A row of w slots: full rounds of 8, then one round of exactly the
+// remaining count.  No slot is predicated off, so no FMA issue slot is spent
+// on padding beyond the stored width (w is warp-uniform in ELL with a fixed
+// width and in SELL with C a multiple of 32, so the switch does not diverge).
+template <typename T>
+__device__ __forceinline__ T strided_row(size_t base, uint32_t w, size_t stride,
+                                         const uint32_t *__restrict__ cols,
+                                         const T *__restrict__ elems, const T *__restrict__ x,
+                                         int64_t xs, int64_t xinc) {
+  T acc = 0;
+  uint32_t j0 = 0;
+  for (; j0 + 8 <= w; j0 += 8) acc = strided_round<8>(acc, base, j0, stride, cols, elems, x, xs, xinc);
+  switch (w - j0) {
+#define VCLGB_REM(R) \
+  case R: acc = strided_round<R>(acc, base, j0, stride, cols, elems, x, xs, xinc); break;
+    VCLGB_REM(1) VCLGB_REM(2) VCLGB_REM(3) VCLGB_REM(4) VCLGB_REM(5) VCLGB_REM(6) VCLGB_REM(7)
+#undef VCLGB_REM
+    default: break;
+  }
+  if (!finite_bits(acc)) acc = strided_row_skip<T>(base, w, stride, cols, elems, x, xs, xinc);
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// ELL: thread per row, column-major slots (ell_matrix.hpp layout).
+// ---------------------------------------------------------------------------
+// W > 0: the width is a compile-time constant (one round, every load of the
+// row issued up front); W == 0: runtime width.
 template <int W, typename T>
 __device__ __forceinline__ T ell_row(size_t r, uint32_t rows, uint32_t width,
                                      const uint32_t *__restrict__ coords,
                                      const T *__restrict__ elems, const T *__restrict__ x,
                                      int64_t xs, int64_t xinc) {
-  constexpr int R = W > 0 ? W : 8;
-  T acc = 0;
-  for (uint32_t j0 = 0; j0 < (W > 0 ? (uint32_t)W : width); j0 += R) {
-    T val[R];
-    uint32_t col[R];
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const bool in = W > 0 || j0 + q < width;
-      const size_t off = (size_t)(j0 + q) * rows + r;
-      val[q] = in ? __ldg(elems + off) : T(0);
-      col[q] = in ? __ldg(coords + off) : 0u;
-    }
-#pragma unroll
-    for (int q = 0; q < R; ++q)
-      if (nonzero_bits(val[q])) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
+  if constexpr (W > 0) {
+    T acc = strided_round<W>(T(0), r, 0, rows, coords, elems, x, xs, xinc);
+    if (!finite_bits(acc)) acc = strided_row_skip<T>(r, W, rows, coords, elems, x, xs, xinc);
+    return acc;
+  } else {
+    return strided_row<T>(r, width, rows, coords, elems, x, xs, xinc);
   }
-  return acc;
 }
 
 template <int W, typename T, class E>
@@ -253,28 +318,12 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // SELL-C-sigma: thread per stored row position; slice s, lane l; element j of
 // the position at block_start[s] + j*C + l (sliced_ell_matrix.hpp layout).
 // ---------------------------------------------------------------------------
-// one stored row position: element j at base + j*C, rounds of 8 loads
 template <typename T>
 __device__ __forceinline__ T sell_row(size_t base, uint32_t w, uint32_t C,
                                       const uint32_t *__restrict__ cols,
                                       const T *__restrict__ elems, const T *__restrict__ x,
                                       int64_t xs, int64_t xinc) {
-  T acc = 0;
-  for (uint32_t j0 = 0; j0 < w; j0 += 8) {
-    T val[8];
-    uint32_t col[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const bool in = j0 + q < w;
-      const size_t off = base + (size_t)(j0 + q) * C;
-      val[q] = in ? __ldg(elems + off) : T(0);
-      col[q] = in ? __ldg(cols + off) : 0u;
-    }
-#pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (nonzero_bits(val[q])) acc += val[q] * __ldg(x + xs + (int64_t)col[q] * xinc);
-  }
-  return acc;
+  return strided_row<T>(base, w, C, cols, elems, x, xs, xinc);
 }
 
 // WARP: C is a multiple of 32 and each warp takes 32 consecutive positions of
@@ -488,18 +537,28 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
       bt.n = m.num_bins;
       for (int i = 0; i < m.num_bins; ++i) bt.b[i] = m.bins[i];
       const bool single = m.num_bins == 1 && m.bins[0].identity;
-      if (single && m.bins[0].lanes == 1)
-        csr_adaptive_kernel<1, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-            A, x, xs, xinc, bt, nullptr, epi, partials, red.counter);
-      else if (single && m.bins[0].lanes == 2)
-        csr_adaptive_kernel<2, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-            A, x, xs, xinc, bt, nullptr, epi, partials, red.counter);
-      else if (single && m.bins[0].lanes == 4)
-        csr_adaptive_kernel<4, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-            A, x, xs, xinc, bt, nullptr, epi, partials, red.counter);
-      else
-        csr_adaptive_kernel<0, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+#define VCLGB_CSR_FIXED(L, R)                                                \
+  csr_adaptive_kernel<L, R, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(     \
+      A, x, xs, xinc, bt, nullptr, epi, partials, red.counter)
+      const uint32_t lanes = single ? m.bins[0].lanes : 0u;
+      if (lanes == 1) {
+        switch (m.max_row_len) {
+          case 3: VCLGB_CSR_FIXED(1, 3); break;
+          case 4: VCLGB_CSR_FIXED(1, 4); break;
+          case 5: VCLGB_CSR_FIXED(1, 5); break;
+          case 6: VCLGB_CSR_FIXED(1, 6); break;
+          case 7: VCLGB_CSR_FIXED(1, 7); break;
+          default: VCLGB_CSR_FIXED(1, kMpl); break;
+        }
+      } else if (lanes == 2) {
+        VCLGB_CSR_FIXED(2, kMpl);
+      } else if (lanes == 4) {
+        VCLGB_CSR_FIXED(4, kMpl);
+      } else {
+        csr_adaptive_kernel<0, kMpl, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
             A, x, xs, xinc, bt, m.bin_rows.as<uint32_t>(), epi, partials, red.counter);
+      }
+#undef VCLGB_CSR_FIXED
       break;
     }
     case VCLGB_ELL:

@@ -48,6 +48,7 @@ struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
+  bool owned = true;  // false: the caller's array, never freed here
   DevBuf() = default;
   DevBuf(size_t b, cudaStream_t s) { alloc(b, s); }
   DevBuf(const DevBuf &) = delete;
@@ -56,7 +57,7 @@ struct DevBuf {
   DevBuf &operator=(DevBuf &&o) noexcept {
     if (this != &o) {
       release();
-      ptr = o.ptr; bytes = o.bytes; stream = o.stream;
+      ptr = o.ptr; bytes = o.bytes; stream = o.stream; owned = o.owned;
       o.ptr = nullptr; o.bytes = 0;
     }
     return *this;
@@ -66,12 +67,21 @@ struct DevBuf {
     release();
     stream = s;
     bytes = b;
+    owned = true;
     if (b) VCLGB_CUDA(cudaMallocAsync(&ptr, b, s));
   }
+  // wrap an existing device array (the reference's own buffers)
+  void borrow(const void *p, size_t b) {
+    release();
+    ptr = const_cast<void *>(p);
+    bytes = b;
+    owned = false;
+  }
   void release() noexcept {
-    if (ptr) cudaFreeAsync(ptr, stream);
+    if (ptr && owned) cudaFreeAsync(ptr, stream);
     ptr = nullptr;
     bytes = 0;
+    owned = true;
   }
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
@@ -207,25 +217,54 @@ __device__ __forceinline__ T group_sum(T v) {
   return v;
 }
 
+// NV rounded up to a power of two (at most 8)
+template <int NV>
+struct Pow2 { static constexpr int v = NV <= 1 ? 1 : NV <= 2 ? 2 : NV <= 4 ? 4 : 8; };
+
+// Warp sums of NV values per lane with a halving butterfly: at each of the
+// first log2(P) exchange steps a lane keeps half of its values and trades the
+// other half with its partner, so the warp spends 5 + log2(P) - 1 additions
+// per lane instead of 5 * NV.  On GB300 every FP64 add takes an issue slot of
+// the narrow FP64 pipe, which the SpMV itself keeps busy.  The sum of value i
+// ends in lane i * (32 / P); the order of additions is fixed (deterministic).
+template <int NV, typename T>
+__device__ __forceinline__ T warp_sum_multi(const T (&v)[NV], int lane) {
+  constexpr int P = Pow2<NV>::v;
+  T a[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) a[i] = i < NV ? v[i] : T(0);
+#pragma unroll
+  for (int h = P / 2, bit = 16; h >= 1; h >>= 1, bit >>= 1) {
+    const bool upper = (lane & bit) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const T keep = upper ? a[j + h] : a[j];
+      const T send = upper ? a[j] : a[j + h];
+      a[j] = keep + __shfl_xor_sync(0xffffffffu, send, bit);
+    }
+  }
+#pragma unroll
+  for (int bit = 16 / P; bit > 0; bit >>= 1) a[0] += __shfl_xor_sync(0xffffffffu, a[0], bit);
+  return a[0];
+}
+
 // Deterministic block reduction of NV values per thread.  Result valid in
 // thread 0.  smem must hold NV * (blockDim.x/32) values.
 template <int NV, typename T>
 __device__ __forceinline__ void block_sum(T (&v)[NV], T *smem) {
+  constexpr int P = Pow2<NV>::v, SPAN = 32 / P;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+  const T w = warp_sum_multi<NV>(v, lane);
   __syncthreads();
-  if (lane == 0) {
-#pragma unroll
-    for (int i = 0; i < NV; ++i) smem[i * nw + warp] = v[i];
-  }
+  if ((lane & (SPAN - 1)) == 0 && lane / SPAN < NV) smem[(lane / SPAN) * nw + warp] = w;
   __syncthreads();
   if (warp == 0) {
+    T t[NV];
 #pragma unroll
-    for (int i = 0; i < NV; ++i) {
-      T t = lane < nw ? smem[i * nw + lane] : T(0);
-      v[i] = warp_sum(t);
-    }
+    for (int i = 0; i < NV; ++i) t[i] = lane < nw ? smem[i * nw + lane] : T(0);
+    const T s = warp_sum_multi<NV>(t, lane);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = __shfl_sync(0xffffffffu, s, i * SPAN);
   }
 }
 

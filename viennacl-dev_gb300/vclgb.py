@@ -92,6 +92,10 @@ SIGNATURES = {
     "vclgbMatrixToSell": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
     "vclgbMatrixToHyb": (_I32, [_P, _P, _D, ctypes.POINTER(_P)]),
     "vclgbMatrixToFloat32": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "vclgbEllWrap": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, ctypes.POINTER(_P)]),
+    "vclgbSellWrap": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, _P, _P, ctypes.POINTER(_P)]),
+    "vclgbHybWrap": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, _P, _P, _P, _U64,
+                            ctypes.POINTER(_P)]),
     "vclgbMatrixDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbMatrixGetInfo": (_I32, [_P, ctypes.POINTER(MatrixInfo)]),
     "vclgbMatrixExport": (_I32, [_P, _P, _I32, _P]),
@@ -329,6 +333,56 @@ class hyb_matrix(_Converted):
 
     def __init__(self, csr, csr_threshold=0.8):
         super().__init__(csr, load_library().vclgbMatrixToHyb, float(csr_threshold))
+
+
+class _Wrapped(_Matrix):
+    """A format already on the device in the reference layout, wrapped without
+    copying; the tensors are kept alive with the handle."""
+
+    def __init__(self, fmt, fn, arrays, *args, be=None):
+        super().__init__()
+        self.fmt = fmt
+        self.be = be or backend()
+        self._keep = list(arrays)
+        h = _P()
+        self.be.check(fn(self.be.h, *args, ctypes.byref(h)))
+        self.h = h
+
+
+def _u32_dev(a):
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda", dtype=torch.int32).contiguous()
+    return _dev(np.asarray(a, dtype=np.uint32).view(np.int32), torch.int32)
+
+
+def wrap_ell(rows, cols, width, coords, elems, be=None):
+    """ell_matrix<T, 1> from its coords/elems buffers (rows*width each,
+    column-major slots as ell_matrix.hpp lays them out)."""
+    co, el = _u32_dev(coords), elems
+    prec = _dtype_prec(el.dtype)
+    return _Wrapped(ELL, load_library().vclgbEllWrap, (co, el), prec, int(rows), int(cols),
+                    int(width), _ptr(co), _ptr(el), be=be)
+
+
+def wrap_sliced_ell(rows, cols, slice_height, columns_per_block, column_indices, block_start,
+                    elems, be=None):
+    """sliced_ell_matrix<T, unsigned> (sigma 1) from its four buffers."""
+    cpb, ci, bs, el = (_u32_dev(columns_per_block), _u32_dev(column_indices),
+                       _u32_dev(block_start), elems)
+    return _Wrapped(SELL, load_library().vclgbSellWrap, (cpb, ci, bs, el), _dtype_prec(el.dtype),
+                    int(rows), int(cols), int(slice_height), _ptr(cpb), _ptr(ci), _ptr(bs),
+                    _ptr(el), be=be)
+
+
+def wrap_hyb(rows, cols, ell_width, ell_coords, ell_elems, tail_row_ptr, tail_cols, tail_vals,
+             be=None):
+    """hyb_matrix<T, 1> from its ELL part and CSR tail buffers."""
+    co, trp, tci = _u32_dev(ell_coords), _u32_dev(tail_row_ptr), _u32_dev(tail_cols)
+    el, tv = ell_elems, tail_vals
+    return _Wrapped(HYB, load_library().vclgbHybWrap, (co, el, trp, tci, tv), _dtype_prec(el.dtype),
+                    int(rows), int(cols), int(ell_width), _ptr(co), _ptr(el), _ptr(trp), _ptr(tci),
+                    _ptr(tv), int(tv.numel()), be=be)
 
 
 def prod(A, x, alpha=1.0, y=None, beta=0.0, x_start=0, x_stride=1, y_start=0, y_stride=1,
