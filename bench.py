@@ -516,10 +516,24 @@ def run_reference(args):
 
 
 def profile_kernels(args):
-    """Small fixed workload for ncu captures: a few SpMVs per format on the
-    128^3 Laplacian (about 300 MB on the device) and one short CG solve."""
+    """Small fixed workloads for ncu captures.  laplace: a few SpMVs per format
+    on the 128^3 Laplacian (about 300 MB on the device) and one short CG
+    solve; lognormal: a few SpMVs per format on a 1M-row lognormal random
+    matrix (about 21M nnz, 250 MB of CSR arrays)."""
     import torch
     import vclgb as V
+    if args.profile_case == "lognormal":
+        rp, ci, v = gen.lognormal_random(1 << 20, mu=2.5, sigma=1.0, hi=2000, seed=1)
+        n = len(rp) - 1
+        A = V.compressed_matrix(rp, ci, v)
+        x = torch.tensor(gen.rhs_uniform(n, 1), device="cuda")
+        y = torch.empty(n, dtype=torch.float64, device="cuda")
+        for M in (A, V.sliced_ell_matrix(A, 32, 256), V.hyb_matrix(A)):
+            for _ in range(3):
+                V.prod(M, x, y=y)
+        torch.cuda.synchronize()
+        print("profile workload done")
+        return
     rp, ci, v = gen.laplace3d(128)
     n = len(rp) - 1
     A = V.compressed_matrix(rp, ci, v)
@@ -537,6 +551,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-kernels", action="store_true",
                     help="run the small fixed workload used for ncu captures")
+    ap.add_argument("--profile-case", default="laplace", choices=["laplace", "lognormal"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

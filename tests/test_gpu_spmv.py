@@ -91,6 +91,27 @@ def test_edge_rows(V):
     assert err < TOL64
 
 
+def test_window_length_classes(V):
+    # every row-length class of the row-window kernel, both sides of each
+    # class limit, rows longer than 4096 (block per row), a partial last window
+    rng = np.random.default_rng(11)
+    n, m = 3001, 12000
+    limits = [0, 1, 4, 5, 8, 9, 16, 17, 32, 33, 64, 65, 128, 129, 4096, 4097, 9000]
+    lens = rng.integers(0, 40, n)
+    lens[rng.choice(n, len(limits) * 3, replace=False)] = np.repeat(limits, 3)
+    lens[-1] = 4097
+    cols = [np.sort(rng.choice(m, size=L, replace=False)) for L in lens]
+    rp = np.zeros(n + 1, np.uint32)
+    rp[1:] = np.cumsum(lens)
+    ci = np.concatenate(cols).astype(np.uint32)
+    v = rng.standard_normal(ci.size)
+    x = rng.uniform(-1, 1, m)
+    err, A = _check(V, rp, ci, v, x, ncols=m)
+    assert err < TOL64 and A.info().num_bins > 1
+    err, _ = _check(V, rp, ci, v, x, -1.5, 0.25, rng.uniform(-1, 1, n), ncols=m)
+    assert err < TOL64
+
+
 def test_rectangular_and_tiny(V):
     rp = np.array([0, 2, 2, 3], np.uint32)
     ci = np.array([0, 6, 3], np.uint32)

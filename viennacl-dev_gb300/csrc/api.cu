@@ -225,6 +225,7 @@ VCLGB_API vclgbStatus vclgbSellWrap(vclgbBackend h, vclgbPrecision prec, uint32_
       m->sell_start.borrow(start, (size_t)ns * 4);
       m->sell_cols.borrow(colidx, m->sell_stored * 4);
       m->sell_elems.borrow(elems, m->sell_stored * m->vsize());
+      sell_wide_chunks(*be, *m);
     }
     *out = reinterpret_cast<vclgbMatrix>(m.release());
   });

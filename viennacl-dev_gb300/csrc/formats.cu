@@ -149,7 +149,7 @@ void csr_validate(Backend &be, const Matrix &m) {
 }
 
 // ---------------------------------------------------------------------------
-// row-length analysis for the adaptive CSR kernel
+// row-length analysis of a CSR matrix (stencil test, length histogram)
 // ---------------------------------------------------------------------------
 // bin of a row: 0..5 = 1,2,4,8,16,32 lanes per row (each lane issues up to 8
 // loads per round, so bin q covers rows of up to 8 << q entries in one round),
@@ -165,9 +165,6 @@ __device__ __host__ inline int lane_bin(uint32_t len) {
 }
 constexpr int kLaneBins = 7;
 constexpr uint32_t kBinLanes[kLaneBins] = {1, 2, 4, 8, 16, 32, 0};
-
-constexpr int kPartThreads = 256;
-constexpr int kPartRows = 2048;  // rows per partition tile
 
 __global__ void row_stats_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
                                  unsigned long long *stats /* [kLaneBins] counts, max, min */) {
@@ -191,55 +188,6 @@ __global__ void row_stats_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
   if (threadIdx.x == 0) {
     atomicMax(&stats[kLaneBins], (unsigned long long)mx);
     atomicMin(&stats[kLaneBins + 1], (unsigned long long)mn);
-  }
-}
-
-// stable partition of the rows by bin: per-tile counts, scan, scatter
-__global__ void part_count_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
-                                  uint32_t *tile_counts /* [kLaneBins][ntiles] */, size_t ntiles) {
-  __shared__ unsigned cnt[kLaneBins];
-  if (threadIdx.x < kLaneBins) cnt[threadIdx.x] = 0;
-  __syncthreads();
-  size_t r0 = (size_t)blockIdx.x * kPartRows;
-  for (size_t r = r0 + threadIdx.x; r < r0 + kPartRows && r < rows; r += blockDim.x)
-    atomicAdd(&cnt[lane_bin(rp[r + 1] - rp[r])], 1u);
-  __syncthreads();
-  if (threadIdx.x < kLaneBins) tile_counts[threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
-}
-
-__global__ void part_scatter_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
-                                    const uint64_t *__restrict__ tile_offsets /* scanned */,
-                                    size_t ntiles, uint32_t *out) {
-  // one warp-synchronous pass per 256 rows keeps the order stable
-  __shared__ unsigned base[kLaneBins];
-  __shared__ unsigned wcnt[kLaneBins][kPartThreads / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x < kLaneBins) base[threadIdx.x] = (unsigned)tile_offsets[threadIdx.x * ntiles + blockIdx.x];
-  __syncthreads();
-  size_t r0 = (size_t)blockIdx.x * kPartRows;
-  for (size_t c = r0; c < r0 + kPartRows && c < rows; c += blockDim.x) {
-    size_t r = c + threadIdx.x;
-    bool ok = r < rows && r < r0 + kPartRows;
-    int b = ok ? lane_bin(rp[r + 1] - rp[r]) : -1;
-    unsigned my_rank = 0;
-    for (int q = 0; q < kLaneBins; ++q) {
-      unsigned m = __ballot_sync(0xffffffffu, b == q);
-      if (b == q) my_rank = __popc(m & ((1u << lane) - 1u));
-      if (lane == 0) wcnt[q][warp] = __popc(m);
-    }
-    __syncthreads();
-    if (ok) {
-      unsigned off = base[b];
-      for (int w = 0; w < warp; ++w) off += wcnt[b][w];
-      out[off + my_rank] = (uint32_t)r;
-    }
-    __syncthreads();
-    if (threadIdx.x < kLaneBins) {
-      unsigned t = 0;
-      for (int w = 0; w < kPartThreads / 32; ++w) t += wcnt[threadIdx.x][w];
-      base[threadIdx.x] += t;
-    }
-    __syncthreads();
   }
 }
 
@@ -271,33 +219,17 @@ void csr_analyse(Backend &be, Matrix &m) {
     m.num_bins = 1;
     return;
   }
-  size_t ntiles = (m.rows + kPartRows - 1) / kPartRows;
-  DevBuf counts(kLaneBins * ntiles * sizeof(uint32_t), be.stream);
-  DevBuf offs((kLaneBins * ntiles + 1) * sizeof(uint64_t), be.stream);
-  part_count_kernel<<<(unsigned)ntiles, kPartThreads, 0, be.stream>>>(m.rows, m.row_ptr,
-                                                                     counts.as<uint32_t>(), ntiles);
-  be.launches++;
-  VCLGB_CHECK_LAUNCH();
-  exclusive_scan<uint32_t, uint64_t>(be, counts.as<uint32_t>(), kLaneBins * ntiles,
-                                     offs.as<uint64_t>());
-  m.bin_rows.alloc((size_t)m.rows * sizeof(uint32_t), be.stream);
-  part_scatter_kernel<<<(unsigned)ntiles, kPartThreads, 0, be.stream>>>(
-      m.rows, m.row_ptr, offs.as<uint64_t>(), ntiles, m.bin_rows.as<uint32_t>());
-  be.launches++;
-  VCLGB_CHECK_LAUNCH();
-  uint64_t off = 0;
+  // irregular rows: the row-window kernel classifies rows per window on the
+  // fly; the bins only record the length histogram
   for (int q = 0; q < kLaneBins; ++q) {
     if (h[q] == 0) continue;
     CsrBin b;
     b.lanes = kBinLanes[q];
     b.count = (uint32_t)h[q];
-    b.offset = (uint32_t)off;
+    b.offset = 0;
     b.identity = 0;
     m.bins[m.num_bins++] = b;
-    off += h[q];
   }
-  // the longest rows first: their blocks start while the short-row bins stream
-  std::reverse(m.bins, m.bins + m.num_bins);
 }
 
 // ---------------------------------------------------------------------------
@@ -506,7 +438,32 @@ std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C,
         out->sell_elems.as<uint32_t>());
   be.launches++;
   VCLGB_CHECK_LAUNCH();
+  sell_wide_chunks(be, *out);
   return out;
+}
+
+// List of the 32-position chunks wider than kSellWide slots (C a multiple of
+// 32), which the SELL kernel hands to whole blocks.
+void sell_wide_chunks(Backend &be, Matrix &m) {
+  m.sell_wide.release();
+  m.sell_nwide = 0;
+  if (m.rows == 0 || m.C % 32 != 0) return;
+  std::vector<uint32_t> cpb(m.num_slices);
+  VCLGB_CUDA(cudaMemcpyAsync(cpb.data(), m.sell_cpb.ptr, (size_t)m.num_slices * 4,
+                             cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  const uint32_t per = m.C / 32, nsub = (m.rows + 31) / 32;
+  std::vector<uint32_t> wide;
+  for (uint32_t s = 0; s < m.num_slices; ++s) {
+    if (cpb[s] <= kSellWide) continue;
+    for (uint32_t k = 0; k < per && s * per + k < nsub; ++k) wide.push_back(s * per + k);
+  }
+  if (wide.empty()) return;
+  m.sell_wide.alloc(wide.size() * 4, be.stream);
+  VCLGB_CUDA(cudaMemcpyAsync(m.sell_wide.ptr, wide.data(), wide.size() * 4,
+                             cudaMemcpyHostToDevice, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  m.sell_nwide = (uint32_t)wide.size();
 }
 
 // ---------------------------------------------------------------------------
@@ -663,11 +620,6 @@ std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m) {
       out->num_bins = m.num_bins;
       for (int i = 0; i < m.num_bins; ++i) out->bins[i] = m.bins[i];
       out->max_row_len = m.max_row_len;
-      if (m.bin_rows.ptr) {
-        out->bin_rows.alloc(m.bin_rows.bytes, be.stream);
-        VCLGB_CUDA(cudaMemcpyAsync(out->bin_rows.ptr, m.bin_rows.ptr, m.bin_rows.bytes,
-                                   cudaMemcpyDeviceToDevice, be.stream));
-      }
       break;
     default:
       throw Error(VCLGB_UNSUPPORTED, "FP32 copies are built from CSR matrices");

@@ -7,6 +7,7 @@ namespace vclgb {
 
 std::unique_ptr<Matrix> convert_ell(Backend &be, const Matrix &csr);
 std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C, uint32_t sigma);
+void sell_wide_chunks(Backend &be, Matrix &m);
 std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold);
 std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m);
 // COO row of every tail entry from the tail row_ptr (HYB wrapped from reference arrays)

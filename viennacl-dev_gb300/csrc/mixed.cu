@@ -268,11 +268,6 @@ static Matrix &f32_scaled(Backend &be, Matrix &A) {
   m->num_bins = A.num_bins;
   for (int i = 0; i < A.num_bins; ++i) m->bins[i] = A.bins[i];
   m->max_row_len = A.max_row_len;
-  if (A.bin_rows.ptr) {
-    m->bin_rows.alloc(A.bin_rows.bytes, be.stream);
-    VCLGB_CUDA(cudaMemcpyAsync(m->bin_rows.ptr, A.bin_rows.ptr, A.bin_rows.bytes,
-                               cudaMemcpyDeviceToDevice, be.stream));
-  }
   A.f32_scaled = std::move(m);
   return *A.f32_scaled;
 }

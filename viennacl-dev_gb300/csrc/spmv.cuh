@@ -1,4 +1,5 @@
-// spmv.cuh -- SpMV kernels for CSR (adaptive, row-length bins), ELL, SELL-C-sigma
+// spmv.cuh -- SpMV kernels for CSR (single-bin stencil kernel, row-window kernel
+// with per-window length classes), ELL, SELL-C-sigma
 // and HYB (ELL + COO tail with a warp-segmented reduction).
 //
 // Every kernel hands each finished row to an epilogue object E:
@@ -81,13 +82,8 @@ template <int N>
 struct DotArr { static constexpr int n = N > 0 ? N : 1; };
 
 // ---------------------------------------------------------------------------
-// adaptive CSR
+// CSR
 // ---------------------------------------------------------------------------
-struct BinTable {
-  int n;
-  CsrBin b[kMaxBins];
-};
-
 template <typename T>
 struct CsrView {
   const uint32_t *rp;
@@ -107,20 +103,21 @@ struct CsrView {
 // row has 3..7 entries runs with MPL equal to that length.
 constexpr int kMpl = 8;
 
+// The warps numbered warp, warp + nwarps, ... share the rows (grid-wide or
+// within one block); list may live in global or shared memory.
 template <int LANES, int MPL, typename T, class E>
 __device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__restrict__ x,
                                                int64_t xs, int64_t xinc, uint32_t count,
-                                               const uint32_t *__restrict__ list, const E &epi,
-                                               T (&dots)[DotArr<E::NDOT>::n]) {
+                                               const uint32_t *list, const E &epi,
+                                               T (&dots)[DotArr<E::NDOT>::n], size_t warp,
+                                               size_t nwarps) {
   constexpr int GPW = 32 / LANES;  // groups per warp
   const uint32_t lane = threadIdx.x & (LANES - 1);
   const uint32_t gw = (threadIdx.x & 31) / LANES;
-  const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
   for (size_t wb = warp * GPW; wb < count; wb += nwarps * GPW) {
     const size_t idx = wb + gw;
     const bool ok = idx < count;
-    const uint32_t row = ok ? (list ? __ldg(list + idx) : (uint32_t)idx) : 0xffffffffu;
+    const uint32_t row = ok ? (list ? list[idx] : (uint32_t)idx) : 0xffffffffu;
     const uint32_t s = ok ? __ldg(A.rp + row) : 0u;
     const uint32_t e = ok ? __ldg(A.rp + row + 1) : 0u;
     typename E::Pre pv{};
@@ -145,14 +142,16 @@ __device__ __forceinline__ void csr_rows_group(const CsrView<T> &A, const T *__r
   }
 }
 
-// one block per row (rows longer than a warp can stream efficiently)
+// one block per row (rows longer than a warp can stream efficiently); the
+// block takes rows first, first + step, ... of the list
 template <typename T, class E>
 __device__ __forceinline__ void csr_rows_block(const CsrView<T> &A, const T *__restrict__ x,
                                                int64_t xs, int64_t xinc, uint32_t count,
-                                               const uint32_t *__restrict__ list, const E &epi,
-                                               T (&dots)[DotArr<E::NDOT>::n], T *smem) {
-  for (size_t i = blockIdx.x; i < count; i += gridDim.x) {
-    uint32_t row = list ? __ldg(list + i) : (uint32_t)i;
+                                               const uint32_t *list, const E &epi,
+                                               T (&dots)[DotArr<E::NDOT>::n], T *smem,
+                                               size_t first, size_t step) {
+  for (size_t i = first; i < count; i += step) {
+    uint32_t row = list ? list[i] : (uint32_t)i;
     uint32_t s = __ldg(A.rp + row), e = __ldg(A.rp + row + 1);
     typename E::Pre pv{};
     if (threadIdx.x == 0) pv = epi.pre(row);
@@ -165,34 +164,139 @@ __device__ __forceinline__ void csr_rows_block(const CsrView<T> &A, const T *__r
   }
 }
 
-// FIXED > 0: the matrix is one identity bin of FIXED lanes per row (stencils),
-// compiled without the bin dispatch, MPL entries per lane and round;
-// FIXED == 0: the general binned kernel.
-template <int FIXED, int MPL, typename T, class E>
+// Matrices whose rows all fall in one length bin (stencils: longest row at
+// most about twice the mean) run without any row classification: LANES
+// threads per row, MPL entries per lane and round, rows in order.
+template <int LANES, int MPL, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
-    csr_adaptive_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc,
-                        BinTable bins, const uint32_t *__restrict__ bin_rows, E epi,
-                        T *partials, unsigned *counter) {
+    csr_fixed_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc, E epi,
+                     T *partials, unsigned *counter) {
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   T dots[DotArr<E::NDOT>::n];
 #pragma unroll
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
-  if constexpr (FIXED > 0) {
-    csr_rows_group<FIXED, MPL>(A, x, xs, xinc, A.rows, nullptr, epi, dots);
-  } else
-  for (int b = 0; b < bins.n; ++b) {
-    const CsrBin bin = bins.b[b];
-    const uint32_t *list = bin.identity ? nullptr : bin_rows + bin.offset;
-    switch (bin.lanes) {
-      case 1: csr_rows_group<1, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 2: csr_rows_group<2, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 4: csr_rows_group<4, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 8: csr_rows_group<8, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 16: csr_rows_group<16, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      case 32: csr_rows_group<32, kMpl>(A, x, xs, xinc, bin.count, list, epi, dots); break;
-      default: csr_rows_block(A, x, xs, xinc, bin.count, list, epi, dots, smem); break;
+  const size_t gwarp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t gnwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  csr_rows_group<LANES, MPL>(A, x, xs, xinc, A.rows, nullptr, epi, dots, gwarp, gnwarps);
+  if constexpr (E::NDOT > 0) {
+    T sums[E::NDOT];
+    if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Row-window CSR for irregular row lengths.  A block takes windows of
+// kWinRows consecutive rows, sorts the window's rows into length classes in
+// shared memory (stable, so the rows a thread handles and the order of its
+// dot partials are fixed for a matrix) and runs each class with its own lane
+// count.  The values and indices of a window are one contiguous stretch that
+// the block reads within a short time, so each sector comes from DRAM once;
+// global length bins sweep the whole matrix once per bin and re-read the
+// sectors that rows of different bins share.
+// ---------------------------------------------------------------------------
+constexpr int kWinRounds = 2;                        // rows per thread and window
+constexpr int kWinRows = kWinRounds * kSpmvThreads;  // 512
+constexpr int kWinClasses = 8;
+constexpr int kWinWarps = kSpmvThreads / 32;
+
+// length classes: <=4, <=8 (one lane), <=16 (2), <=32 (4), <=64 (8), <=128 (16),
+// <=4096 (32 lanes, rounds of 256 entries), longer (the whole block)
+__device__ __forceinline__ uint32_t win_class(uint32_t len) {
+  return len <= 4 ? 0u : len <= 8 ? 1u : len <= 16 ? 2u : len <= 32 ? 3u
+       : len <= 64 ? 4u : len <= 128 ? 5u : len <= 4096 ? 6u : 7u;
+}
+
+template <int LANES, int MPL, typename T, class E>
+__device__ __forceinline__ void win_class_rows(const CsrView<T> &A, const T *__restrict__ x,
+                                               int64_t xs, int64_t xinc, const uint32_t *lists,
+                                               const uint32_t *cstart, int c, uint32_t &slot,
+                                               const E &epi, T (&dots)[DotArr<E::NDOT>::n]) {
+  constexpr uint32_t GPW = 32 / LANES;
+  const uint32_t n = cstart[c + 1] - cstart[c];
+  // the class's first rows go to the warp after the last one the previous
+  // class used, so small classes do not all land on warp 0
+  const uint32_t warp = threadIdx.x >> 5;
+  const uint32_t vw = (warp + kWinWarps - slot % kWinWarps) % kWinWarps;
+  csr_rows_group<LANES, MPL>(A, x, xs, xinc, n, lists + cstart[c], epi, dots, vw, kWinWarps);
+  slot += (n + GPW - 1) / GPW;
+}
+
+template <typename T, class E>
+__global__ void __launch_bounds__(kSpmvThreads)
+    csr_window_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc, E epi,
+                      T *partials, unsigned *counter) {
+  if (epi.skip()) return;
+  __shared__ T smem[3 * kWinWarps + 8];
+  __shared__ uint32_t lists[kWinRows];
+  // rows per (class, round, warp), then their exclusive offsets in lists
+  __shared__ uint32_t woff[kWinClasses * kWinRounds * kWinWarps];
+  __shared__ uint32_t cstart[kWinClasses + 1];
+  T dots[DotArr<E::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nwin = (A.rows + kWinRows - 1) / kWinRows;
+  for (uint32_t w = blockIdx.x; w < nwin; w += gridDim.x) {
+    const uint32_t r0 = w * kWinRows;
+    uint32_t cls[kWinRounds];
+#pragma unroll
+    for (int i = 0; i < kWinRounds; ++i) {
+      const uint32_t r = r0 + i * kSpmvThreads + threadIdx.x;
+      cls[i] = r < A.rows ? win_class(__ldg(A.rp + r + 1) - __ldg(A.rp + r)) : kWinClasses;
+#pragma unroll
+      for (int c = 0; c < kWinClasses; ++c) {
+        const unsigned m = __ballot_sync(0xffffffffu, cls[i] == (uint32_t)c);
+        if (lane == 0) woff[(c * kWinRounds + i) * kWinWarps + warp] = __popc(m);
+      }
     }
+    __syncthreads();
+    if (warp == 0) {
+      constexpr int N = kWinClasses * kWinRounds * kWinWarps;
+      constexpr int PER = N / 32;
+      static_assert(N % 32 == 0 && (kWinRounds * kWinWarps) % PER == 0, "window scan layout");
+      uint32_t v[PER], t = 0;
+#pragma unroll
+      for (int j = 0; j < PER; ++j) {
+        v[j] = woff[lane * PER + j];
+        t += v[j];
+      }
+      uint32_t incl = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += q;
+      }
+      uint32_t run = incl - t;
+      if ((lane * PER) % (kWinRounds * kWinWarps) == 0)
+        cstart[lane * PER / (kWinRounds * kWinWarps)] = run;
+#pragma unroll
+      for (int j = 0; j < PER; ++j) {
+        woff[lane * PER + j] = run;
+        run += v[j];
+      }
+      if (lane == 31) cstart[kWinClasses] = run;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kWinRounds; ++i) {
+      const uint32_t c = cls[i];
+      const unsigned m = __match_any_sync(0xffffffffu, c);
+      if (c < kWinClasses)
+        lists[woff[(c * kWinRounds + i) * kWinWarps + warp] + __popc(m & ((1u << lane) - 1u))] =
+            r0 + i * kSpmvThreads + threadIdx.x;
+    }
+    __syncthreads();
+    uint32_t slot = 0;
+    win_class_rows<1, 4>(A, x, xs, xinc, lists, cstart, 0, slot, epi, dots);
+    win_class_rows<1, 8>(A, x, xs, xinc, lists, cstart, 1, slot, epi, dots);
+    win_class_rows<2, 8>(A, x, xs, xinc, lists, cstart, 2, slot, epi, dots);
+    win_class_rows<4, 8>(A, x, xs, xinc, lists, cstart, 3, slot, epi, dots);
+    win_class_rows<8, 8>(A, x, xs, xinc, lists, cstart, 4, slot, epi, dots);
+    win_class_rows<16, 8>(A, x, xs, xinc, lists, cstart, 5, slot, epi, dots);
+    win_class_rows<32, 8>(A, x, xs, xinc, lists, cstart, 6, slot, epi, dots);
+    csr_rows_block(A, x, xs, xinc, cstart[8] - cstart[7], lists + cstart[7], epi, dots, smem, 0, 1);
+    __syncthreads();  // lists and cstart are rewritten for the next window
   }
   if constexpr (E::NDOT > 0) {
     T sums[E::NDOT];
@@ -250,25 +354,34 @@ __device__ __forceinline__ T strided_round(T acc, size_t base, uint32_t j0, size
   return acc;
 }
 
-// A row of w slots: full rounds of 8, then one round of exactly the
+// Slots [j0, j1) of a row: full rounds of 8, then one round of exactly the
 // remaining count.  No slot is predicated off, so no FMA issue slot is spent
-// on padding beyond the stored width (w is warp-uniform in ELL with a fixed
-// width and in SELL with C a multiple of 32, so the switch does not diverge).
+// on padding beyond the stored width (j0 and j1 are warp-uniform in ELL with a
+// fixed width and in SELL with C a multiple of 32, so the switch does not
+// diverge).
 template <typename T>
-__device__ __forceinline__ T strided_row(size_t base, uint32_t w, size_t stride,
-                                         const uint32_t *__restrict__ cols,
-                                         const T *__restrict__ elems, const T *__restrict__ x,
-                                         int64_t xs, int64_t xinc) {
-  T acc = 0;
-  uint32_t j0 = 0;
-  for (; j0 + 8 <= w; j0 += 8) acc = strided_round<8>(acc, base, j0, stride, cols, elems, x, xs, xinc);
-  switch (w - j0) {
+__device__ __forceinline__ T strided_range(T acc, size_t base, uint32_t j0, uint32_t j1,
+                                           size_t stride, const uint32_t *__restrict__ cols,
+                                           const T *__restrict__ elems, const T *__restrict__ x,
+                                           int64_t xs, int64_t xinc) {
+  for (; j0 + 8 <= j1; j0 += 8) acc = strided_round<8>(acc, base, j0, stride, cols, elems, x, xs, xinc);
+  switch (j1 - j0) {
 #define VCLGB_REM(R) \
   case R: acc = strided_round<R>(acc, base, j0, stride, cols, elems, x, xs, xinc); break;
     VCLGB_REM(1) VCLGB_REM(2) VCLGB_REM(3) VCLGB_REM(4) VCLGB_REM(5) VCLGB_REM(6) VCLGB_REM(7)
 #undef VCLGB_REM
     default: break;
   }
+  return acc;
+}
+
+// a whole row of w slots, with the non-finite fallback
+template <typename T>
+__device__ __forceinline__ T strided_row(size_t base, uint32_t w, size_t stride,
+                                         const uint32_t *__restrict__ cols,
+                                         const T *__restrict__ elems, const T *__restrict__ x,
+                                         int64_t xs, int64_t xinc) {
+  T acc = strided_range<T>(T(0), base, 0, w, stride, cols, elems, x, xs, xinc);
   if (!finite_bits(acc)) acc = strided_row_skip<T>(base, w, stride, cols, elems, x, xs, xinc);
   return acc;
 }
@@ -327,32 +440,58 @@ __device__ __forceinline__ T sell_row(size_t base, uint32_t w, uint32_t C,
 }
 
 // WARP: C is a multiple of 32 and each warp takes 32 consecutive positions of
-// one slice (no division per thread); otherwise thread per position.
+// one slice (no division per thread); the chunks listed in wide (all chunks of
+// more than kSellWide slots, nwide of them) are taken by whole blocks instead.
+// Otherwise thread per position.
 template <bool WARP, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     sell_kernel(uint32_t rows, uint32_t C, const uint32_t *__restrict__ cpb,
                 const uint32_t *__restrict__ start, const uint32_t *__restrict__ cols,
                 const T *__restrict__ elems, const uint32_t *__restrict__ perm,
-                const T *__restrict__ x, int64_t xs, int64_t xinc, E epi, T *partials,
-                unsigned *counter) {
+                const uint32_t *__restrict__ wide, uint32_t nwide, const T *__restrict__ x,
+                int64_t xs, int64_t xinc, E epi, T *partials, unsigned *counter) {
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   T dots[DotArr<E::NDOT>::n];
 #pragma unroll
   for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
   if constexpr (WARP) {
-    const uint32_t lane = threadIdx.x & 31, per = C >> 5;
+    constexpr uint32_t NW = kSpmvThreads / 32;
+    __shared__ T part[NW][32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, per = C >> 5;
     const uint32_t nsub = (rows + 31) >> 5;  // 32-position chunks
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nsub;
          q += (gridDim.x * blockDim.x) >> 5) {
       const uint32_t s = q / per, l = (q - s * per) * 32 + lane;
+      const uint32_t w = __ldg(cpb + s);
+      if (nwide && w > kSellWide) continue;  // a block takes it below
       const uint32_t pos = q * 32 + lane;
       const uint32_t row = pos < rows ? (perm ? __ldg(perm + pos) : pos) : 0u;
       typename E::Pre pv{};
       if (pos < rows) pv = epi.pre(row);
-      const T acc = sell_row(__ldg(start + s) + (size_t)l, __ldg(cpb + s), C, cols, elems, x,
-                             xs, xinc);
+      const T acc = sell_row(__ldg(start + s) + (size_t)l, w, C, cols, elems, x, xs, xinc);
       if (pos < rows) epi.row(row, acc, pv, dots);
+    }
+    for (uint32_t i = blockIdx.x; i < nwide; i += gridDim.x) {
+      const uint32_t q = __ldg(wide + i), s = q / per, l = (q - s * per) * 32 + lane;
+      const uint32_t w = __ldg(cpb + s);
+      const size_t base = __ldg(start + s) + (size_t)l;
+      const uint32_t j0 = (uint32_t)((uint64_t)w * warp / NW);
+      const uint32_t j1 = (uint32_t)((uint64_t)w * (warp + 1) / NW);
+      part[warp][lane] = strided_range<T>(T(0), base, j0, j1, C, cols, elems, x, xs, xinc);
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t pos = q * 32 + lane;
+        T acc = part[0][lane];
+#pragma unroll
+        for (uint32_t k = 1; k < NW; ++k) acc += part[k][lane];
+        if (!finite_bits(acc)) acc = strided_row_skip<T>(base, w, C, cols, elems, x, xs, xinc);
+        if (pos < rows) {
+          const uint32_t row = perm ? __ldg(perm + pos) : pos;
+          epi.row(row, acc, epi.pre(row), dots);
+        }
+      }
+      __syncthreads();
     }
   } else {
     for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < rows;
@@ -533,13 +672,10 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
   switch (m.format) {
     case VCLGB_CSR: {
       CsrView<T> A{m.row_ptr, m.col_idx, static_cast<const T *>(m.values), m.rows};
-      BinTable bt;
-      bt.n = m.num_bins;
-      for (int i = 0; i < m.num_bins; ++i) bt.b[i] = m.bins[i];
       const bool single = m.num_bins == 1 && m.bins[0].identity;
 #define VCLGB_CSR_FIXED(L, R)                                                \
-  csr_adaptive_kernel<L, R, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(     \
-      A, x, xs, xinc, bt, nullptr, epi, partials, red.counter)
+  csr_fixed_kernel<L, R, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(        \
+      A, x, xs, xinc, epi, partials, red.counter)
       const uint32_t lanes = single ? m.bins[0].lanes : 0u;
       if (lanes == 1) {
         switch (m.max_row_len) {
@@ -555,8 +691,10 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
       } else if (lanes == 4) {
         VCLGB_CSR_FIXED(4, kMpl);
       } else {
-        csr_adaptive_kernel<0, kMpl, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
-            A, x, xs, xinc, bt, m.bin_rows.as<uint32_t>(), epi, partials, red.counter);
+        const size_t nwin = (m.rows + kWinRows - 1) / kWinRows;
+        const int wgrid = (int)(nwin < (size_t)grid ? (nwin ? nwin : 1) : grid);
+        csr_window_kernel<T, E><<<wgrid, kSpmvThreads, 0, be.stream>>>(A, x, xs, xinc, epi,
+                                                                       partials, red.counter);
       }
 #undef VCLGB_CSR_FIXED
       break;
@@ -569,14 +707,14 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
         sell_kernel<true, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
             m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
             m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
-            m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, x, xs, xinc, epi, partials,
-            red.counter);
+            m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, m.sell_wide.as<uint32_t>(),
+            m.sell_nwide, x, xs, xinc, epi, partials, red.counter);
       else
         sell_kernel<false, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
             m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
             m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
-            m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, x, xs, xinc, epi, partials,
-            red.counter);
+            m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, nullptr, 0u, x, xs, xinc, epi,
+            partials, red.counter);
       break;
     case VCLGB_HYB: {
       // y = alpha*ELL*x + beta*y, then y += alpha*tail*x, then the epilogue pass

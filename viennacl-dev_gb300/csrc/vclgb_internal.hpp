@@ -121,16 +121,23 @@ inline int waves_grid(const Backend &be, int threads, int blocks_per_sm_cap, siz
 // ---------------------------------------------------------------------------
 // matrices
 // ---------------------------------------------------------------------------
-// Row-length bins of the adaptive CSR kernel: rows of one bin are handled by
-// groups of `lanes` threads (1..32) or, for lanes == 0, one block per row.
+// Row-length histogram of a CSR matrix: rows of a bin need `lanes` threads
+// (1..32) or, for lanes == 0, a block per row.  A matrix whose rows all fit
+// one bin (identity: rows [0, count) in order) runs the single-bin kernel.
 struct CsrBin {
   uint32_t lanes;      // 1,2,4,8,16,32 or 0 (= block per row)
   uint32_t count;      // rows in the bin
-  uint32_t offset;     // offset into the bin row list (unused when identity)
-  uint32_t identity;   // 1: the bin is rows [0, count) in order (no row list)
+  uint32_t offset;     // unused (0)
+  uint32_t identity;   // 1: the one bin covering all rows in order
 };
 
 constexpr int kMaxBins = 8;
+
+// SELL chunks (32 positions of a slice) wider than this many slots are split
+// over the warps of a block; a sort window sigma > 1 gathers the longest rows
+// into a few slices, and one warp running such a slice alone would set the
+// kernel's time.
+constexpr uint32_t kSellWide = 128;
 
 struct Transposed;  // adjoint.cu: A^T and its entry map
 
@@ -146,10 +153,9 @@ struct Matrix {
   const uint32_t *col_idx = nullptr;
   const void *values = nullptr;
   DevBuf own_row_ptr, own_col_idx, own_values;
-  // adaptive-CSR analysis
+  // row-length analysis
   int num_bins = 0;
   CsrBin bins[kMaxBins];
-  DevBuf bin_rows;          // concatenated row lists of non-identity bins
   uint32_t max_row_len = 0;
   // reference row blocks (generate_row_block_information), built on demand
   DevBuf row_blocks;
@@ -164,6 +170,8 @@ struct Matrix {
   uint32_t C = 32, sigma = 1, num_slices = 0;
   uint64_t sell_stored = 0;
   DevBuf sell_cpb, sell_start, sell_cols, sell_elems, sell_perm;
+  DevBuf sell_wide;          // 32-position chunks wider than the warp limit
+  uint32_t sell_nwide = 0;
 
   // HYB tail: reference CSR arrays + COO rows for the segmented kernel
   uint64_t tail_nnz = 0;     // real tail entries (0 if empty)
