@@ -752,7 +752,7 @@ __global__ void __launch_bounds__(256)
                       unsigned *counter) {
   if (g->done != kRunning) return;
   __shared__ T hs[KB];
-  __shared__ T smem[16];
+  __shared__ T smem[256];  // block_sum_wide over 256 threads
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = g->h[j];
   __syncthreads();
   T *vk = V + (size_t)k * ld;
@@ -767,7 +767,7 @@ __global__ void __launch_bounds__(256)
     vk[i] = v;
   }
   T s[1];
-  if (grid_reduce<1>(d, partials, counter, smem, s)) g->vnorm2 = s[0];
+  if (grid_reduce<1, true>(d, partials, counter, smem, s)) g->vnorm2 = s[0];
 }
 
 template <typename T>

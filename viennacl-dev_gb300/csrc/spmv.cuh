@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
     csr_window_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc, E epi,
                       T *partials, unsigned *counter) {
   if (epi.skip()) return;
-  __shared__ T smem[3 * kWinWarps + 8];
+  __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   __shared__ uint32_t lists[kWinRows];
   // rows per (class, round, warp), then their exclusive offsets in lists
   __shared__ uint32_t woff[kWinClasses * kWinRounds * kWinWarps];

@@ -256,8 +256,13 @@ __device__ __forceinline__ T warp_sum_multi(const T (&v)[NV], int lane) {
   return a[0];
 }
 
-// Deterministic block reduction of NV values per thread.  Result valid in
-// thread 0.  smem must hold NV * (blockDim.x/32) values.
+// Deterministic block reductions of NV values per thread; the result is
+// valid in thread 0.  The FP64 adds are the cost that matters: the fused SpMV
+// and vector kernels saturate the FP64 pipe.
+//
+// block_sum: warp butterflies, then warp 0 over the warp sums.  smem holds
+// NV * (blockDim.x / 32) values, so the kernel keeps its L1 capacity (the
+// SpMV kernels' x gathers hit in L1).
 template <int NV, typename T>
 __device__ __forceinline__ void block_sum(T (&v)[NV], T *smem) {
   constexpr int P = Pow2<NV>::v, SPAN = 32 / P;
@@ -276,13 +281,42 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], T *smem) {
   }
 }
 
+// block_sum_wide: every thread parks its values in shared memory (no
+// arithmetic), then warp 0 adds them: blockDim.x/32 adds per value plus one
+// butterfly for the block, instead of a butterfly in every warp.  smem holds
+// NV * blockDim.x values; used by the streaming vector passes, which gain
+// nothing from L1.
+template <int NV, typename T>
+__device__ __forceinline__ void block_sum_wide(T (&v)[NV], T *smem) {
+  constexpr int P = Pow2<NV>::v, SPAN = 32 / P;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = blockDim.x;
+  __syncthreads();  // a previous reduction may still be reading smem
+#pragma unroll
+  for (int i = 0; i < NV; ++i) smem[i * nt + threadIdx.x] = v[i];
+  __syncthreads();
+  if (warp == 0) {
+    T t[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      T a = T(0);
+      for (int k = lane; k < nt; k += 32) a += smem[i * nt + k];
+      t[i] = a;
+    }
+    const T s = warp_sum_multi<NV>(t, lane);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = __shfl_sync(0xffffffffu, s, i * SPAN);
+  }
+}
+
 // Grid-level two-stage reduction: every block writes NV partials, the last
 // block to arrive sums all partials in a fixed order (deterministic) and
 // returns true in thread 0 with the sums in out[].  counter is reset.
-template <int NV, typename T>
+// WIDE selects block_sum_wide (smem of NV * blockDim.x values) over block_sum.
+template <int NV, bool WIDE = false, typename T>
 __device__ __forceinline__ bool grid_reduce(T (&v)[NV], T *partials, unsigned *counter, T *smem,
                                             T (&out)[NV]) {
-  block_sum<NV>(v, smem);
+  if constexpr (WIDE) block_sum_wide<NV>(v, smem);
+  else block_sum<NV>(v, smem);
   __shared__ bool am_last;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -302,7 +336,8 @@ __device__ __forceinline__ bool grid_reduce(T (&v)[NV], T *partials, unsigned *c
       s += ((volatile T *)partials)[(size_t)i * gridDim.x + b];
     acc[i] = s;
   }
-  block_sum<NV>(acc, smem);
+  if constexpr (WIDE) block_sum_wide<NV>(acc, smem);
+  else block_sum<NV>(acc, smem);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) out[i] = acc[i];

@@ -13,7 +13,7 @@ template <typename T, class F>
 __global__ void __launch_bounds__(kVecThreads)
     vec_pass_kernel(size_t n, F f, T *partials, unsigned *counter) {
   if (f.skip()) return;
-  __shared__ T smem[4 * (kVecThreads / 32) + 8];
+  __shared__ T smem[DotArr<F::NDOT>::n * kVecThreads];
   T dots[DotArr<F::NDOT>::n];
 #pragma unroll
   for (int i = 0; i < DotArr<F::NDOT>::n; ++i) dots[i] = T(0);
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(kVecThreads)
   if (i < n) f.apply(i, sc, dots);
   if constexpr (F::NDOT > 0) {
     T sums[F::NDOT];
-    if (grid_reduce<F::NDOT>(dots, partials, counter, smem, sums)) f.finalize(sums);
+    if (grid_reduce<F::NDOT, true>(dots, partials, counter, smem, sums)) f.finalize(sums);
   }
 }
 
