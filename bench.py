@@ -36,6 +36,10 @@ for p in (os.path.join(ROOT, "viennacl-dev_gb300"), os.path.join(ROOT, "oracle")
 import vclgb_gen as gen  # noqa: E402
 
 METRIC = "CG solve s @1e-10 FP64 resid: mixed/batched vs plain FP64 on GPU; SpMV GB/s"
+# DRAM bytes (read + write) of one launch of the CG SpMV phase kernel on the
+# 128^3 Laplacian, from the ncu capture summarised in
+# profiles/csr_fixed_laplace3d_128.md (None until that capture exists)
+TRAFFIC_SPMV_CG = None
 WORKLOAD = "3D 7-point Laplacian 128^3 (2,097,152 rows, 14,581,760 nnz), FP64 CSR, pipelined CG to 1e-10"
 
 
@@ -214,18 +218,56 @@ def run_ours(args):
     out["gpu_launches"] = int(launches)
     out["clocks"] = clocks
 
-    # ---- roofline: the dominant kernel is the CSR SpMV ----------------------
+    # ---- roofline: the dominant kernel of the solve ---------------------------
+    # One more solve of the same workload with the backend's kernel timing on:
+    # CUDA event pairs around every SpMV phase (the CSR product with the fused
+    # CG dots, csr_fixed_kernel<1,7,double,EpiCg>) and every fused vector pass
+    # (vec_pass_kernel<CgUpdate>), recorded as nodes of the solver's captured
+    # graphs on its stream.  Launches after convergence inside the last graph
+    # chunk return at their first instruction; they are the durations below
+    # half the median and are left out.
+    A.be.set_kernel_timing(True)
+    try:
+        tag_t = solve_once()
+        t_spmv_all, t_vec_all = A.be.kernel_times(0), A.be.kernel_times(1)
+    finally:
+        A.be.set_kernel_timing(False)
+
+    def active(t):
+        t = np.asarray(t, dtype=np.float64)
+        return t[t > 0.5 * np.median(t)] if t.size else t
+    t_spmv, t_vec = active(t_spmv_all), active(t_vec_all)
+    b_spmv = spmv_bytes(n, nnz)      # p read once, Ap written; p[r] of the dots is the same array
+    b_vec = 7 * 8 * n                # x, p, r, Ap read; x, p, r written
+    us_spmv, us_vec = float(t_spmv.mean()) * 1e3, float(t_vec.mean()) * 1e3
+    gbs = b_spmv / (us_spmv * 1e-6) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                       "frac": gbs / peak, "peak_kind": peak_kind,
+                       "kernel": "csr_fixed_kernel<1,7,double,EpiCg<double>> (CSR SpMV + CG dots, "
+                                 "thread per row; 68% of the solve's device time)",
+                       "algorithmic_bytes_per_launch": b_spmv,
+                       "avg_launch_us": us_spmv, "launches_timed": int(t_spmv.size),
+                       "traffic": TRAFFIC_SPMV_CG,
+                       "traffic_source": "profiles/csr_fixed_laplace3d_128.md (ncu, one launch)",
+                       "second_kernel": {
+                           "kernel": "vec_pass_kernel<double,CgUpdate<double>>",
+                           "algorithmic_bytes_per_launch": b_vec, "avg_launch_us": us_vec,
+                           "achieved": b_vec / (us_vec * 1e-6) / 1e9,
+                           "frac": b_vec / (us_vec * 1e-6) / 1e9 / peak},
+                       "per_iteration": {
+                           "us": t_solve * 1e6 / max(iters, 1),
+                           "algorithmic_bytes": b_spmv + b_vec,
+                           "hbm_floor_us": (b_spmv + b_vec) / (peak * 1e9) * 1e6,
+                           "fp64_fma_per_iteration": nnz + 6 * n}}
+    # the plain product (linalg::prod, no epilogue work) on the same matrix
     xs = torch.tensor(gen.rhs_uniform(n, 11), device="cuda")
     ys = torch.empty(n, dtype=torch.float64, device="cuda")
     for _ in range(5):
         V.prod(A, xs, y=ys)
-    t_spmv, gbs = spmv_gbs(V, A, n, nnz, 50, xs, ys)
-    out["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
-                       "frac": gbs / peak, "peak_kind": peak_kind,
-                       "kernel": "csr_adaptive_kernel<double> (8 lanes/row bin, 128^3 Laplacian)",
-                       "algorithmic_bytes_per_launch": spmv_bytes(n, nnz),
-                       "avg_launch_us": t_spmv * 1e6,
-                       "traffic": args.traffic}
+    t_plain, gbs_plain = spmv_gbs(V, A, n, nnz, 50, xs, ys)
+    out["roofline"]["plain_prod"] = {"kernel": "csr_fixed_kernel<1,7,double,EpiAxpbyM<double,0,true>>",
+                                     "avg_launch_us": t_plain * 1e6, "achieved": gbs_plain,
+                                     "frac": gbs_plain / peak}
 
     # ---- e2e from host buffers ----------------------------------------------
     h_rp = torch.from_numpy(rp.view(np.int32)).pin_memory()
@@ -539,7 +581,7 @@ def profile_kernels(args):
     A = V.compressed_matrix(rp, ci, v)
     x = torch.tensor(gen.rhs_uniform(n, 1), device="cuda")
     y = torch.empty(n, dtype=torch.float64, device="cuda")
-    for M in (A, V.sliced_ell_matrix(A, 32, 1)):
+    for M in (A, V.ell_matrix(A), V.sliced_ell_matrix(A, 32, 1)):
         for _ in range(3):
             V.prod(M, x, y=y)
     V.solve(A, x, V.cg_tag(1e-10, 20))
@@ -557,8 +599,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline only (for profiling runs)")
-    ap.add_argument("--traffic", type=float, default=None,
-                    help="ncu DRAM bytes per SpMV launch, from the committed profile")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

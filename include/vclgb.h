@@ -65,6 +65,19 @@ VCLGB_API uint64_t vclgbBackendLaunchCount(vclgbBackend backend);
 /* Library version string. */
 VCLGB_API const char *vclgbVersion(void);
 
+/* Kernel timing (a measurement hook with no reference counterpart; off by
+ * default).  While enabled, every SpMV phase (kind 0: the product with its
+ * fused epilogue, all formats) and every fused vector pass (kind 1) the
+ * backend launches is bracketed by two CUDA events on its stream -- inside
+ * the solvers' captured CUDA graphs as event nodes -- so that kernel
+ * durations can be read from a real solve.  vclgbBackendKernelTimes copies up
+ * to `capacity` durations in milliseconds (host array; may be NULL) of the
+ * given kind recorded since the last call, sets *count to how many there
+ * were, and clears them.  Enabling or disabling clears both lists. */
+VCLGB_API vclgbStatus vclgbBackendSetKernelTiming(vclgbBackend be, int enable);
+VCLGB_API vclgbStatus vclgbBackendKernelTimes(vclgbBackend be, int kind, float *h_ms,
+                                              uint64_t capacity, uint64_t *count);
+
 /* ---- sparse matrices ----------------------------------------------------- */
 typedef struct vclgbMatrix_st *vclgbMatrix;
 
@@ -72,7 +85,8 @@ typedef enum {
   VCLGB_CSR = 0,   /* viennacl::compressed_matrix   (compressed_matrix.hpp:629-1198) */
   VCLGB_ELL = 1,   /* viennacl::ell_matrix          (ell_matrix.hpp:52-120) */
   VCLGB_SELL = 2,  /* viennacl::sliced_ell_matrix   (sliced_ell_matrix.hpp:45-133) */
-  VCLGB_HYB = 3    /* viennacl::hyb_matrix          (hyb_matrix.hpp:37-132) */
+  VCLGB_HYB = 3,   /* viennacl::hyb_matrix          (hyb_matrix.hpp:37-132) */
+  VCLGB_COO = 4    /* viennacl::coordinate_matrix   (coordinate_matrix.hpp:186-397) */
 } vclgbFormat;
 
 /* compressed_matrix(row_ptr, cols, vals, CUDA_MEMORY, rows, cols, nnz): wraps
@@ -101,6 +115,14 @@ VCLGB_API vclgbStatus vclgbMatrixToSell(vclgbBackend be, vclgbMatrix csr, uint32
                                         uint32_t sigma, vclgbMatrix *out);
 VCLGB_API vclgbStatus vclgbMatrixToHyb(vclgbBackend be, vclgbMatrix csr, double csr_threshold,
                                        vclgbMatrix *out);
+/* COO: viennacl::copy(host_matrix, coordinate_matrix<T, 128>)
+ * (coordinate_matrix.hpp:46-101): (row, col) pairs interleaved in one u32
+ * array and the values, both padded with zeros to a multiple of 128 entries,
+ * plus the 65 group boundaries the reference computes (bit-identical,
+ * including its rule that puts the first non-empty row alone in group 0 and
+ * every later entry in group 63).  The product runs the warp-segmented
+ * reduction over all entries and does not use the groups. */
+VCLGB_API vclgbStatus vclgbMatrixToCoo(vclgbBackend be, vclgbMatrix csr, vclgbMatrix *out);
 /* ell_matrix / sliced_ell_matrix / hyb_matrix that already live on the device
  * in the reference's layout (the CUDA buffers behind their handle() ...
  * handle5()), wrapped without copying; the arrays stay the caller's.
@@ -122,6 +144,35 @@ VCLGB_API vclgbStatus vclgbHybWrap(vclgbBackend be, vclgbPrecision prec, uint32_
                                    const uint32_t *d_ell_coords, const void *d_ell_elems,
                                    const uint32_t *d_tail_row_ptr, const uint32_t *d_tail_cols,
                                    const void *d_tail_vals, uint64_t tail_nnz, vclgbMatrix *out);
+/* coordinate_matrix<T, A> already on the device (handle12() = interleaved
+ * (row, col) pairs, handle() = values), entries sorted by row as the
+ * reference's copy() leaves them; wrapped without copying.  d_coords must be
+ * 8-byte aligned (the reference's CUDA kernel reads the pairs as uint2). */
+VCLGB_API vclgbStatus vclgbCooWrap(vclgbBackend be, vclgbPrecision prec, uint32_t rows,
+                                   uint32_t cols, uint64_t nnz, const uint32_t *d_coords,
+                                   const void *d_elems, vclgbMatrix *out);
+/* viennacl::io::read_matrix_market_file(matrix, path, index_base)
+ * (io/matrix_market.hpp:101-369) straight into a device compressed_matrix that
+ * owns its arrays.  Same file rules as the reference: "%%MatrixMarket matrix
+ * coordinate real|complex|pattern general|symmetric" (complex keeps the real
+ * part, pattern entries are 1), comment and blank lines, "rows cols nnz",
+ * then nnz entries whose indices count from index_base (1 in the reference's
+ * default); symmetric files set both A(i,j) and A(j,i); a later entry for the
+ * same position replaces an earlier one.  *lines_read (may be NULL) receives
+ * the reference's return value, the number of lines read.  A file that
+ * cannot be opened, a bad header, index or number, or fewer entries than
+ * announced returns VCLGB_INVALID_ARGUMENT with the cause (file, line) in
+ * vclgbBackendLastError. */
+VCLGB_API vclgbStatus vclgbReadMatrixMarket(vclgbBackend be, const char *path, int64_t index_base,
+                                            vclgbPrecision prec, vclgbMatrix *out,
+                                            uint64_t *lines_read);
+/* viennacl::io::write_matrix_market_file(matrix, path, index_base)
+ * (io/matrix_market.hpp:374-417) for a compressed_matrix: the "coordinate
+ * real general" header, the size line, one entry per line in row order.
+ * Values carry `digits` significant digits; 0 selects 6, the reference's
+ * default stream precision (17 writes values that read back exactly). */
+VCLGB_API vclgbStatus vclgbWriteMatrixMarket(vclgbBackend be, vclgbMatrix A, const char *path,
+                                             int64_t index_base, int digits);
 /* FP32 copy of a matrix (same format and pattern), as mixed_precision_cg.hpp:128-137
  * builds for its inner iterations. */
 VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend be, vclgbMatrix m, vclgbMatrix *out);
@@ -132,7 +183,7 @@ typedef struct {
   int32_t precision;     /* vclgbPrecision */
   uint32_t rows, cols;
   uint64_t nnz;          /* nonzeros of the source pattern */
-  uint64_t stored;       /* stored slots incl. padding (ELL/SELL/HYB-ELL part) */
+  uint64_t stored;       /* stored slots incl. padding (ELL/SELL/HYB-ELL part/COO) */
   uint32_t ell_width;    /* ELL: maxnnz; HYB: ellnnz */
   uint32_t slice_height; /* SELL: C */
   uint32_t sigma;        /* SELL: sort window */
@@ -151,6 +202,8 @@ VCLGB_API vclgbStatus vclgbMatrixGetInfo(vclgbMatrix m, vclgbMatrixInfo *info);
  *         (handle), 4 row permutation u32[rows] (position -> row)
  *   HYB : 0 ell coords, 1 ell elements, 2 tail row_ptr u32[rows+1] (handle3),
  *         3 tail cols u32[tail_nnz] (handle4), 4 tail elements T[tail_nnz] (handle5)
+ *   COO : 0 coords u32[2*stored] (handle12), 1 elements T[stored] (handle),
+ *         2 group boundaries u32[65] (handle3); stored = nnz rounded up to 128
  *   CSR : 0 row_ptr, 1 cols, 2 values, 3 row blocks u32[nblocks+1] of
  *         generate_row_block_information (compressed_matrix.hpp:1152-1188);
  *         use vclgbCsrRowBlockCount for its length. */
@@ -184,6 +237,14 @@ typedef struct vclgbPrecond_st *vclgbPrecond;
  * extracts diag(A) on the device (row_info SPARSE_ROW_DIAGONAL).  A zero
  * diagonal entry returns VCLGB_ZERO_ON_DIAGONAL. */
 VCLGB_API vclgbStatus vclgbJacobiCreate(vclgbBackend be, vclgbMatrix A, vclgbPrecond *out);
+/* row_scaling<compressed_matrix>(A, row_scaling_tag(norm)) (linalg/row_scaling.hpp:150-191):
+ * a diagonal of row norms of A -- norm 0: max |a_ij|, 1: sum |a_ij|, 2: Euclidean
+ * (row_info, linalg/host_based/sparse_matrix_operations.hpp:52-98) -- applied as
+ * element_div like Jacobi.  Any other norm returns VCLGB_INVALID_ARGUMENT (the
+ * reference throws unknown_norm_exception); a zero row is not checked, as in
+ * the reference's compressed_matrix specialisation. */
+VCLGB_API vclgbStatus vclgbRowScalingCreate(vclgbBackend be, vclgbMatrix A, uint32_t norm,
+                                            vclgbPrecond *out);
 /* ilu0_precond<compressed_matrix>(A, ilu0_tag(use_level_scheduling))
  * (linalg/detail/ilu/ilu0.hpp:189-352).  The factorisation runs on the
  * device, level-scheduled row by row; the level sets of L and U are built on

@@ -57,6 +57,7 @@ def lib():
         L.vo_csr_spmv_strided_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _SZ, _SZ, _D, _D,
                                             _f64p, _SZ, _SZ]
         L.vo_csr_diag_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p]
+        L.vo_row_norms_d.argtypes = [_U32, _u32p, _f64p, _U32, _f64p]
         L.vo_csr_row_blocks.argtypes = [_U32, _u32p, _u32p]
         L.vo_csr_row_blocks.restype = _SZ
         L.vo_ell_width.argtypes = [_U32, _u32p]
@@ -75,6 +76,9 @@ def lib():
                                     _f64p]
         L.vo_hyb_spmv_d.argtypes = [_U32, _U32, _u32p, _f64p, _u32p, _u32p, _f64p, _f64p, _D, _D,
                                     _f64p]
+        L.vo_coo_fill_d.argtypes = [_U32, _u32p, _u32p, _f64p, _u32p, _f64p, _u32p]
+        L.vo_coo_fill_d.restype = _SZ
+        L.vo_coo_spmv_d.argtypes = [_U32, _SZ, _u32p, _f64p, _f64p, _D, _D, _f64p]
         for name in ("vo_cg_d", "vo_bicgstab_d"):
             getattr(L, name).argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p,
                                          ctypes.POINTER(Tag), ctypes.POINTER(Precond)]
@@ -147,6 +151,14 @@ def diag(rp, ci, v):
     return d
 
 
+def row_norms(rp, v, norm):
+    """row_scaling's diagonal: row norms (0 max, 1 sum, 2 Euclidean)."""
+    n = len(rp) - 1
+    d = np.zeros(n)
+    lib().vo_row_norms_d(n, _c(rp, np.uint32), _c(v, np.float64), int(norm), d)
+    return d
+
+
 def row_blocks(rp):
     n = len(rp) - 1
     out = np.zeros(n + 1, np.uint32)
@@ -201,12 +213,32 @@ def hyb(rp, ci, v, ncols, threshold=0.8, is_float=False):
                 tail_ci=tci[:max(tn, 1)], tail_v=tv[:max(tn, 1)], tail_nnz=tn)
 
 
+def coo(rp, ci, v):
+    """coordinate_matrix copy: interleaved pairs, values (padded to 128), groups."""
+    n = len(rp) - 1
+    rp, ci, v = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64)
+    nnz = int(rp[-1])
+    stored = (nnz + 127) // 128 * 128
+    co = np.zeros(max(2 * stored, 2), np.uint32)
+    el = np.zeros(max(stored, 1))
+    gr = np.zeros(65, np.uint32)
+    lib().vo_coo_fill_d(n, rp, ci, v, co, el, gr)
+    return dict(coords=co[:2 * stored], elems=el[:stored], groups=gr, nnz=nnz, stored=stored)
+
+
+def coo_spmv(n, C, x, alpha=1.0, beta=0.0, y0=None):
+    y = np.zeros(n) if y0 is None else np.array(y0, dtype=np.float64)
+    lib().vo_coo_spmv_d(n, C["nnz"], _c(C["coords"], np.uint32), _c(C["elems"], np.float64),
+                        _c(x, np.float64), alpha, beta, y)
+    return y
+
+
 def _precond(kind, rp=None, ci=None, v=None):
     P = Precond()
-    P.kind = {"none": 0, "jacobi": 1, "ilu0": 2}[kind]
+    P.kind = {"none": 0, "jacobi": 1, "ilu0": 2, "row0": 1, "row1": 1, "row2": 1}[kind]
     keep = []
-    if kind == "jacobi":
-        d = diag(rp, ci, v)
+    if kind == "jacobi" or kind.startswith("row"):
+        d = diag(rp, ci, v) if kind == "jacobi" else row_norms(rp, v, int(kind[3]))
         keep.append(d)
         P.diag = d.ctypes.data
     elif kind == "ilu0":
@@ -342,3 +374,84 @@ def run_ref(cmd, rp, ci, v, ncols=None, args=(), **vecs):
                 it, err, sec = open(p).read().split()
                 out["iters"], out["error"], out["seconds"] = int(it), float(err), float(sec)
         return out
+
+
+# ---- io/matrix_market.hpp:101-326 (reader), restated in Python -------------
+def read_matrix_market(path, index_base=1):
+    """Follows read_matrix_market_file_impl: returns (lines_read, rows, cols,
+    rp, ci, v) or raises ValueError where the reference returns 0.  Entries
+    assign A(r, c) (and A(c, r) when symmetric); the later one wins."""
+    symmetric = pattern = False
+    header_done = False
+    nnz = rows = cols = 0
+    A = {}
+    valid = 0
+    linenum = 0
+    with open(path, "rb") as f:
+        raw = f.read().decode("latin-1").split("\n")
+    if raw and raw[-1] == "":
+        raw.pop()
+    for text in raw:
+        linenum += 1
+        s = text.strip(" ")
+        if s == "":
+            continue
+        if s[0] == "%":
+            if s[1:2] != "%":
+                continue
+            words, tok = s[2:].split(), ""
+            it = iter(words)
+
+            def nxt():
+                nonlocal tok
+                tok = next(it, tok)  # a missing word keeps the previous one
+                return tok.lower()
+            if nxt() != "matrixmarket" or nxt() != "matrix":
+                raise ValueError("header")
+            kind = nxt()
+            if kind != "coordinate":
+                raise ValueError("array or unknown format")
+            field = nxt()
+            if field == "pattern":
+                pattern = True
+            elif field not in ("complex", "real"):
+                raise ValueError("field")
+            sym = nxt()
+            if sym == "symmetric":
+                symmetric = True
+            elif sym != "general":
+                raise ValueError("symmetry")
+            continue
+        w = s.split()
+        if not header_done:
+            if len(w) < 3:
+                raise ValueError("size line")
+            rows, cols, nnz = int(w[0]), int(w[1]), int(w[2])
+            if rows == 0 or cols == 0:
+                rows = cols = 0
+            header_done = True
+            if nnz == 0:
+                break
+            continue
+        if len(w) < (2 if pattern else 3):
+            raise ValueError("entry")
+        r, c = int(w[0]) - index_base, int(w[1]) - index_base
+        val = 1.0 if pattern else float(w[2])
+        if not (0 <= r < rows) or not (0 <= c < cols):
+            raise ValueError("index out of bounds")
+        A[(r, c)] = val
+        if symmetric:
+            A[(c, r)] = val
+        valid += 1
+        if valid == nnz:
+            break
+    if not header_done or valid < nnz:
+        raise ValueError("file ends early")
+    keys = sorted(A)
+    rp = np.zeros(rows + 1, np.uint32)
+    for r, _ in keys:
+        rp[r + 1] += 1
+    rp = np.cumsum(rp).astype(np.uint32)
+    ci = np.array([c for _, c in keys], np.uint32)
+    v = np.array([A[k] for k in keys], np.float64)
+    return linenum, rows, cols, rp, ci, v

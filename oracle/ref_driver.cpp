@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "viennacl/compressed_matrix.hpp"
+#include "viennacl/coordinate_matrix.hpp"
 #include "viennacl/ell_matrix.hpp"
 #include "viennacl/hyb_matrix.hpp"
 #include "viennacl/linalg/bicgstab.hpp"
@@ -30,6 +31,8 @@
 #include "viennacl/linalg/jacobi_precond.hpp"
 #include "viennacl/linalg/mixed_precision_cg.hpp"
 #include "viennacl/linalg/prod.hpp"
+#include "viennacl/linalg/row_scaling.hpp"
+#include "viennacl/io/matrix_market.hpp"
 #include "viennacl/sliced_ell_matrix.hpp"
 #include "viennacl/tools/adapter.hpp"
 #include "viennacl/vector.hpp"
@@ -155,6 +158,25 @@ int main(int argc, char **argv) {
   }
   std::string cmd = argv[1];
   g_dir = argv[2];
+  if (cmd == "mm_read") {  // args: file index_base -> mm_ret.u32, mm_rp.u32, mm_ci.u32, mm_v.f64
+    std::vector<std::map<unsigned, double> > S;
+    long ret = viennacl::io::read_matrix_market_file(S, argv[3], std::atol(argv[4]));
+    std::vector<unsigned> rp(1, 0), ci;
+    std::vector<double> v;
+    for (size_t r = 0; r < S.size(); ++r) {
+      for (std::map<unsigned, double>::const_iterator it = S[r].begin(); it != S[r].end(); ++it) {
+        ci.push_back(it->first);
+        v.push_back(it->second);
+      }
+      rp.push_back(static_cast<unsigned>(ci.size()));
+    }
+    unsigned meta[2] = {static_cast<unsigned>(ret), static_cast<unsigned>(S.size())};
+    save("mm_ret.u32", meta, 2);
+    save("mm_rp.u32", rp.data(), rp.size());
+    save("mm_ci.u32", ci.data(), ci.size());
+    save("mm_v.f64", v.data(), v.size());
+    return 0;
+  }
   Csr A = load_csr();
   size_t n = A.n;
 
@@ -234,6 +256,26 @@ int main(int argc, char **argv) {
     y = viennacl::linalg::prod(H, x);
     yh = from_vcl(y);
     save("y_hyb.f64", yh.data(), n);
+  } else if (cmd == "coo") {  // args: alpha beta -> coo_coords, coo_elems, coo_groups, y_coo
+    double alpha = std::atof(argv[3]), beta = std::atof(argv[4]);
+    std::vector<std::map<unsigned, double> > S = to_maps<double>(A);
+    viennacl::tools::const_sparse_matrix_adapter<double, unsigned> ad(S, n, A.ncols);
+    viennacl::coordinate_matrix<double> Co;
+    viennacl::copy(ad, Co);
+    size_t inz = Co.internal_nnz();
+    unsigned meta[2] = {static_cast<unsigned>(Co.nnz()), static_cast<unsigned>(inz)};
+    save("coo_nnz.u32", meta, 2);
+    save("coo_coords.u32", raw<unsigned>(Co.handle12()), 2 * inz);
+    save("coo_elems.f64", raw<double>(Co.handle()), inz);
+    save("coo_groups.u32", raw<unsigned>(Co.handle3()), 65);
+    std::vector<double> xh = load<double>("x.f64", A.ncols);
+    viennacl::vector<double> x(A.ncols), y(n);
+    to_vcl(xh, x);
+    std::vector<double> y0 = load<double>("y0.f64", n, true);
+    if (!y0.empty()) to_vcl(y0, y);
+    viennacl::linalg::prod_impl(Co, x, alpha, y, beta);
+    std::vector<double> yh = from_vcl(y);
+    save("y_coo.f64", yh.data(), n);
   } else if (cmd == "hyb_f32_width") {  // args: thr -> hybf_width.u32
     double thr = std::atof(argv[3]);
     std::vector<std::map<unsigned, float> > S = to_maps<float>(A);
@@ -269,6 +311,12 @@ int main(int argc, char **argv) {
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag, P);
         t1 = now();
+      } else if (pc.compare(0, 3, "row") == 0) {  // row0 / row1 / row2
+        viennacl::linalg::row_scaling<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::row_scaling_tag(static_cast<unsigned>(pc[3] - '0')));
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
       } else {
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag);
@@ -281,6 +329,12 @@ int main(int argc, char **argv) {
       if (pc == "jacobi") {
         viennacl::linalg::jacobi_precond<viennacl::compressed_matrix<double> > P(
             M, viennacl::linalg::jacobi_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc.compare(0, 3, "row") == 0) {
+        viennacl::linalg::row_scaling<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::row_scaling_tag(static_cast<unsigned>(pc[3] - '0')));
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag, P);
         t1 = now();
@@ -338,6 +392,18 @@ int main(int argc, char **argv) {
     P.apply(z);
     std::vector<double> zh = from_vcl(z);
     save("z.f64", zh.data(), n);
+  } else if (cmd == "row_norms") {  // -> norm0.f64, norm1.f64, norm2.f64 (row_info)
+    viennacl::compressed_matrix<double> M;
+    fill_matrix(A, M);
+    viennacl::linalg::detail::row_info_types sel[3] = {
+        viennacl::linalg::detail::SPARSE_ROW_NORM_INF, viennacl::linalg::detail::SPARSE_ROW_NORM_1,
+        viennacl::linalg::detail::SPARSE_ROW_NORM_2};
+    for (int p = 0; p < 3; ++p) {
+      viennacl::vector<double> d(n);
+      viennacl::linalg::detail::row_info(M, d, sel[p]);
+      std::vector<double> dh = from_vcl(d);
+      save("norm" + std::to_string(p) + ".f64", dh.data(), n);
+    }
   } else if (cmd == "jacobi_diag") {  // -> diag.f64
     viennacl::compressed_matrix<double> M;
     fill_matrix(A, M);

@@ -87,6 +87,20 @@ void vo_csr_spmv_strided_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const d
 VO_DEF_DIAG(double, d)
 VO_DEF_DIAG(float, s)
 
+/* row_info(SPARSE_ROW_NORM_INF / _1 / _2) -- host_based/sparse_matrix_operations.hpp:52-98,
+ * the diagonal of row_scaling (linalg/row_scaling.hpp:166-182) */
+void vo_row_norms_d(vo_u32 n, const vo_u32 *rp, const double *v, vo_u32 norm, double *d) {
+  for (vo_u32 r = 0; r < n; ++r) {
+    double value = 0;
+    for (vo_u32 k = rp[r]; k < rp[r + 1]; ++k) {
+      if (norm == 0) value = value < fabs(v[k]) ? fabs(v[k]) : value;
+      else if (norm == 1) value += fabs(v[k]);
+      else value += v[k] * v[k];
+    }
+    d[r] = norm == 2 ? sqrt(value) : value;
+  }
+}
+
 /* compressed_matrix::generate_row_block_information -- compressed_matrix.hpp:1152-1188.
  * Greedy blocks of at most 1024 entries; a row longer than that forms its own
  * block; a trailing run of empty rows after a boundary gets no block. */
@@ -331,6 +345,43 @@ void vo_hyb_spmv_d(vo_u32 n, vo_u32 width, const vo_u32 *ell_coords, const doubl
     else
       y[r] = alpha * acc;
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* COO -- coordinate_matrix.hpp:46-101 (copy), host SpMV                     */
+/* host_based/sparse_matrix_operations.hpp:1222-1245                         */
+/* ------------------------------------------------------------------------ */
+/* coords u32[2*stored], elems[stored], groups u32[65]; stored = nnz rounded up
+ * to AlignmentV = 128 (coordinate_matrix.hpp:363), padding zero.  The group
+ * loop follows coordinate_matrix.hpp:74-91 literally, including its cast of
+ * (f+1)/64.0 to an integer before the multiplication by nnz. */
+size_t vo_coo_fill_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                     vo_u32 *coords, double *elems, vo_u32 *groups) {
+  size_t nnz = rp[n], stored = (nnz + 127) / 128 * 128;
+  size_t data_index = 0, f = 0;
+  if (stored) {
+    memset(coords, 0, 2 * stored * sizeof(vo_u32));
+    memset(elems, 0, stored * sizeof(double));
+  }
+  memset(groups, 0, 65 * sizeof(vo_u32));
+  for (vo_u32 r = 0; r < n; ++r) {
+    for (vo_u32 k = rp[r]; k < rp[r + 1]; ++k) {
+      coords[2 * data_index] = r;
+      coords[2 * data_index + 1] = ci[k];
+      elems[data_index] = v[k];
+      ++data_index;
+    }
+    while (data_index > (size_t)((double)(f + 1) / 64.0) * nnz) groups[++f] = (vo_u32)data_index;
+  }
+  groups[64] = (vo_u32)data_index;
+  return stored;
+}
+
+/* y = beta*y (or 0), then y[row] += alpha*e*x[col] entry by entry (sequential) */
+void vo_coo_spmv_d(vo_u32 n, size_t nnz, const vo_u32 *coords, const double *elems,
+                   const double *x, double alpha, double beta, double *y) {
+  for (vo_u32 i = 0; i < n; ++i) y[i] = (beta < 0 || beta > 0) ? y[i] * beta : 0.0;
+  for (size_t k = 0; k < nnz; ++k) y[coords[2 * k]] += alpha * elems[k] * x[coords[2 * k + 1]];
 }
 
 /* ------------------------------------------------------------------------ */

@@ -36,6 +36,7 @@ void vo_csr_spmv_strided_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const d
 /* diagonal extraction (row_info SPARSE_ROW_DIAGONAL) */
 void vo_csr_diag_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, double *d);
 void vo_csr_diag_s(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const float *v, float *d);
+void vo_row_norms_d(vo_u32 n, const vo_u32 *rp, const double *v, vo_u32 norm, double *d);
 
 /* CSR-adaptive row blocks (compressed_matrix::generate_row_block_information).
  * blocks must hold n+1 entries; returns the number of blocks. */
@@ -73,6 +74,10 @@ void vo_hyb_fill_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v
                    double *tail_v);
 void vo_hyb_spmv_d(vo_u32 n, vo_u32 width, const vo_u32 *ell_coords, const double *ell_elems,
                    const vo_u32 *tail_rp, const vo_u32 *tail_ci, const double *tail_v,
+                   const double *x, double alpha, double beta, double *y);
+size_t vo_coo_fill_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                     vo_u32 *coords, double *elems, vo_u32 *groups);
+void vo_coo_spmv_d(vo_u32 n, size_t nnz, const vo_u32 *coords, const double *elems,
                    const double *x, double alpha, double beta, double *y);
 
 /* ---- solvers ---------------------------------------------------------- */

@@ -5,12 +5,15 @@ inputs next to the reference outputs, so the tests need neither the reference
 tree nor a particular numpy random stream.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(python tests/golden/make_golden.py coo | row_scaling | matrix_market  writes only
+that fixture; matrix_market also writes the input files under tests/golden/mm/)
 GMRES fixtures are produced with OMP_NUM_THREADS=1 (the host stage-1 kernel's
 result depends on the thread count).
 """
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -135,6 +138,145 @@ def main():
     save("ilu0_convdiff.npz", rp=rp, ci=ci, v=v, b=b,
          **{k: r[k] for k in r if k.startswith(("L_", "U_")) or k in ("lu", "udiag", "z")})
 
+    coo_fixture()
+    row_scaling_fixture()
+    mm_fixture()
+
+
+def coo_fixture():
+    """coordinate_matrix: the reference's arrays, its 65 group boundaries and
+    its host product; two leading empty rows exercise the group rule."""
+    rp, ci, v = gen.lognormal_random(1500, mu=2.0, sigma=0.9, hi=200, seed=21)
+    ncols = len(rp) - 1
+    rp = np.concatenate([[0, 0], rp]).astype(np.uint32)
+    n = len(rp) - 1
+    rng = np.random.default_rng(25)
+    x = rng.uniform(-1, 1, ncols)
+    y0 = rng.uniform(-1, 1, n)
+    r = oracle.run_ref("coo", rp, ci, v, ncols=ncols, args=(1.5, -0.5), x=x, y0=y0)
+    save("coo_lognormal.npz", rp=rp, ci=ci, v=v, ncols=ncols, x=x, y0=y0, alpha=1.5, beta=-0.5,
+         nnz=r["coo_nnz"], coords=r["coo_coords"], elems=r["coo_elems"],
+         groups=r["coo_groups"], y=r["y_coo"])
+
+
+
+def row_scaling_fixture():
+    """row_scaling: the three row-norm diagonals (row_info) and BiCGStab / CG
+    solves preconditioned by them."""
+    rp, ci, v = gen.convdiff2d(30, 28, peclet=20.0, shift=0.05)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 3)
+    r = oracle.run_ref("row_norms", rp, ci, v)
+    res = {"norm%d" % p: r["norm%d" % p] for p in range(3)}
+    for p in range(3):
+        s = oracle.run_ref("bicgstab", rp, ci, v, args=(1e-10, 2000, "row%d" % p), b=b)
+        res["x_bicgstab_row%d" % p] = s["x"]
+        res["iters_bicgstab_row%d" % p] = s["iters"]
+        res["error_bicgstab_row%d" % p] = s["error"]
+    lp, lc, lv = gen.laplace2d(40, 40)
+    lb = gen.rhs_uniform(len(lp) - 1, 0)
+    s = oracle.run_ref("cg", lp, lc, lv, args=(1e-8, 2000, "row2"), b=lb)
+    save("row_scaling_convdiff.npz", rp=rp, ci=ci, v=v, b=b, lp=lp, lc=lc, lv=lv, lb=lb,
+         x_cg_row2=s["x"], iters_cg_row2=s["iters"], error_cg_row2=s["error"], **res)
+
+
+
+MM_DIR = os.path.join(OUT, "mm")
+
+
+def _mm_write(name, header, size, entries, comments=(), blank=False, fmt="%d %d %s"):
+    lines = [header] + list(comments) + [size]
+    for i, e in enumerate(entries):
+        lines.append(fmt % e if isinstance(e, tuple) else e)
+        if blank and i % 7 == 3:
+            lines.append("")
+    with open(os.path.join(MM_DIR, name), "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def mm_inputs():
+    """Small synthetic MatrixMarket files (seeded) covering the reader's rules:
+    general / symmetric / pattern / complex, comments, blank lines, mixed-case
+    header words, leading and trailing spaces, duplicate positions (the later
+    one wins), 0-based indices, lines after the announced entries, and the
+    error cases (bad header words, array format, index out of range, too few
+    entries, a missing value)."""
+    os.makedirs(MM_DIR, exist_ok=True)
+    rng = np.random.default_rng(31)
+
+    def rand_entries(n, m, k, sym=False):
+        out = []
+        for _ in range(k):
+            i, j = int(rng.integers(1, n + 1)), int(rng.integers(1, m + 1))
+            if sym and j > i:
+                i, j = j, i
+            out.append((i, j, repr(float(rng.normal()))))
+        return out
+
+    g = rand_entries(40, 30, 150)
+    g += [(g[5][0], g[5][1], "7.25"), (g[9][0], g[9][1], "-0.5")]  # duplicates: later wins
+    _mm_write("general.mtx", "%%MatrixMarket matrix coordinate real general", "40 30 %d" % len(g),
+              g, comments=("% a comment", "%another one"), blank=True)
+    _mm_write("general_case.mtx", "%%MATRIXMARKET Matrix Coordinate REAL General",
+              "   12 12 20  ", ["  %d %d %s  " % e for e in rand_entries(12, 12, 20)])
+    s = rand_entries(50, 50, 120, sym=True) + [(3, 3, "4.0"), (7, 2, "1.5"), (2, 7, "2.5")]
+    _mm_write("symmetric.mtx", "%%MatrixMarket matrix coordinate real symmetric",
+              "50 50 %d" % len(s), s)
+    p = [(i, j) for i, j, _ in rand_entries(25, 35, 60)]
+    _mm_write("pattern.mtx", "%%MatrixMarket matrix coordinate pattern general", "25 35 60", p,
+              fmt="%d %d")
+    c = [(i, j, "%s %s" % (v, repr(float(rng.normal())))) for i, j, v in rand_entries(20, 20, 45)]
+    _mm_write("complex.mtx", "%%MatrixMarket matrix coordinate complex general", "20 20 45", c)
+    z = [(i - 1, j - 1, v) for i, j, v in rand_entries(15, 15, 30)]
+    _mm_write("zero_based.mtx", "%%MatrixMarket matrix coordinate real general", "15 15 30", z)
+    e = rand_entries(10, 10, 12)
+    _mm_write("extra_lines.mtx", "%%MatrixMarket matrix coordinate real general", "10 10 8",
+              e, comments=("%",))
+    _mm_write("bad_word.mtx", "%%MatrixMarket tensor coordinate real general", "5 5 2",
+              [(1, 1, "1.0"), (2, 2, "2.0")])
+    _mm_write("bad_field.mtx", "%%MatrixMarket matrix coordinate integer general", "5 5 2",
+              [(1, 1, "1"), (2, 2, "2")])
+    _mm_write("bad_symmetry.mtx", "%%MatrixMarket matrix coordinate real skew-symmetric", "5 5 2",
+              [(2, 1, "1.0"), (3, 2, "2.0")])
+    _mm_write("array.mtx", "%%MatrixMarket matrix array real general", "2 2",
+              ["1.0", "2.0", "3.0", "4.0"])
+    _mm_write("out_of_range.mtx", "%%MatrixMarket matrix coordinate real general", "5 5 3",
+              [(1, 1, "1.0"), (6, 2, "2.0"), (3, 3, "3.0")])
+    _mm_write("too_few.mtx", "%%MatrixMarket matrix coordinate real general", "5 5 4",
+              [(1, 1, "1.0"), (2, 2, "2.0")])
+    _mm_write("missing_value.mtx", "%%MatrixMarket matrix coordinate real general", "5 5 2",
+              [(1, 1, "1.0"), "2 2"])
+
+
+MM_CASES = [("general.mtx", 1), ("general_case.mtx", 1), ("symmetric.mtx", 1),
+            ("pattern.mtx", 1), ("complex.mtx", 1), ("zero_based.mtx", 0), ("extra_lines.mtx", 1),
+            ("bad_word.mtx", 1), ("bad_field.mtx", 1), ("bad_symmetry.mtx", 1), ("array.mtx", 1),
+            ("out_of_range.mtx", 1), ("too_few.mtx", 1), ("missing_value.mtx", 1)]
+
+
+def mm_fixture():
+    """The reference reader's result for each file: its return value (0 =
+    error) and the matrix as CSR (rows sorted by column, as std::map holds them)."""
+    mm_inputs()
+    res = {}
+    for name, base in MM_CASES:
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.run([oracle.REF_DRIVER, "mm_read", d, os.path.join(MM_DIR, name),
+                            str(base)], check=True, stdout=subprocess.DEVNULL,
+                           stderr=subprocess.DEVNULL)
+            key = name[:-4]
+            for f in ("ret", "rp", "ci"):
+                res[key + "__" + f] = np.fromfile(os.path.join(d, "mm_%s.u32" % f), np.uint32)
+            res[key + "__v"] = np.fromfile(os.path.join(d, "mm_v.f64"), np.float64)
+    save("matrix_market.npz", **res)
+
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["coo"]:
+        coo_fixture()
+    elif sys.argv[1:] == ["row_scaling"]:
+        row_scaling_fixture()
+    elif sys.argv[1:] == ["matrix_market"]:
+        mm_fixture()
+    else:
+        main()

@@ -1,4 +1,4 @@
-"""GPU conversions CSR -> ELL / SELL-C-sigma / HYB: bit-exact against the
+"""GPU conversions CSR -> ELL / SELL-C-sigma / HYB / COO: bit-exact against the
 reference's copy() output (golden) and the oracle, plus SpMV per format."""
 import numpy as np
 import pytest
@@ -27,6 +27,66 @@ def _ell_arrays(M, n):
     inf = M.info()
     w = inf.ell_width
     return w, _u32(M.export(0, n * w, torch.int32)), M.export(1, n * w, torch.float64).cpu().numpy()
+
+
+def test_coo_golden(V, golden):
+    # coordinate_matrix arrays and group boundaries bit-exact against the
+    # reference's copy(); the product against the reference's host product
+    import torch
+    d = golden("coo_lognormal.npz")
+    rp, ci, v, ncols = d["rp"], d["ci"], d["v"], int(d["ncols"])
+    n = len(rp) - 1
+    A = V.compressed_matrix(rp, ci, v, n, ncols)
+    Co = V.coordinate_matrix(A)
+    inf = Co.info()
+    assert inf.format == V.COO and inf.nnz == int(d["nnz"][0]) and inf.stored == int(d["nnz"][1])
+    assert np.array_equal(_u32(Co.export(0, 2 * inf.stored, torch.int32)), d["coords"])
+    assert np.array_equal(Co.export(1, inf.stored, torch.float64).cpu().numpy(), d["elems"])
+    assert np.array_equal(_u32(Co.export(2, 65, torch.int32)), d["groups"])
+    y = torch.tensor(d["y0"], device="cuda")
+    V.prod(Co, d["x"], alpha=float(d["alpha"]), y=y, beta=float(d["beta"]))
+    assert rel_err(y.cpu().numpy(), d["y"]) < 1e-13
+    # the same arrays wrapped as the reference's own buffers
+    W = V.wrap_coordinate(n, ncols, inf.nnz, Co.export(0, 2 * inf.nnz, torch.int32),
+                          Co.export(1, inf.nnz, torch.float64))
+    assert np.array_equal(_u32(W.export(2, 65, torch.int32)), d["groups"])
+    y2 = torch.tensor(d["y0"], device="cuda")
+    V.prod(W, d["x"], alpha=float(d["alpha"]), y=y2, beta=float(d["beta"]))
+    assert np.array_equal(y2.cpu().numpy(), y.cpu().numpy())
+
+
+@pytest.mark.parametrize("case", ["lognormal", "laplace3d", "empty_rows"])
+def test_coo_spmv_shapes(V, case):
+    # long rows across many warp chunks, short stencil rows, empty rows
+    if case == "lognormal":
+        rp, ci, v = gen.lognormal_random(30000, mu=2.5, sigma=1.2, hi=2000, seed=9)
+    elif case == "laplace3d":
+        rp, ci, v = gen.laplace3d(30)
+    else:
+        rp0, ci, v = gen.lognormal_random(5000, mu=1.0, sigma=1.0, hi=40, seed=3)
+        keep = np.random.default_rng(3).uniform(size=5000) < 0.5
+        lens = np.diff(rp0.astype(np.int64)) * keep
+        mask = np.repeat(keep, np.diff(rp0.astype(np.int64)))
+        ci, v = ci[mask], v[mask]
+        rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint32)
+    n = len(rp) - 1
+    A = V.compressed_matrix(rp, ci, v)
+    Co = V.coordinate_matrix(A)
+    x = np.random.default_rng(4).uniform(-1, 1, n)
+    y0 = np.random.default_rng(5).uniform(-1, 1, n)
+    import torch
+    for alpha, beta in ((1.0, 0.0), (-0.75, 2.0)):
+        y = torch.tensor(y0, device="cuda")
+        V.prod(Co, x, alpha=alpha, y=y, beta=beta)
+        assert rel_err(y.cpu().numpy(), oracle.spmv(rp, ci, v, x, alpha, beta, y0)) < 1e-13
+
+
+def test_coo_wrap_rejects_unsorted_rows(V):
+    import torch
+    coords = torch.tensor(np.array([1, 0, 0, 1], np.uint32).view(np.int32), device="cuda")
+    with pytest.raises(V.VclgbError) as e:
+        V.wrap_coordinate(2, 2, 2, coords, torch.ones(2, dtype=torch.float64, device="cuda"))
+    assert e.value.status == V.INVALID_MATRIX
 
 
 @pytest.mark.parametrize("name", ["formats_lognormal.npz", "formats_laplace2d.npz"])
@@ -217,3 +277,26 @@ def test_wrap_reference_layout(V, dtype):
         tag = V.cg_tag(tol=1e-10, max_iterations=1000)
         x2 = V.solve(W2, b, tag).cpu().numpy()
         assert rel_err(oracle.spmv(rp2, ci2, v2, x2), b) < 1e-9
+
+
+def test_coo_in_the_solvers(V):
+    # the pipelined CG and BiCGStab run on a coordinate_matrix through the same
+    # fused epilogues as on CSR; iterations and solutions agree
+    rp, ci, v = gen.laplace2d(48, 40)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 6)
+    A = V.compressed_matrix(rp, ci, v)
+    Co = V.coordinate_matrix(A)
+    for name, tagf in (("cg", lambda: V.cg_tag(1e-10, 3000)),
+                       ("bicgstab", lambda: V.bicgstab_tag(1e-10, 3000))):
+        t1, t2 = tagf(), tagf()
+        x1 = V.solve(A, b, t1).cpu().numpy()
+        x2 = V.solve(Co, b, t2).cpu().numpy()
+        assert t2.status() == V.SUCCESS
+        # CG: within 2 %; pipelined BiCGStab's stopping estimate cancels near
+        # convergence, so the COO summation order moves it by a few iterations
+        band = 0.02 if name == "cg" else 0.15
+        assert abs(t1.iters() - t2.iters()) <= max(1, int(band * t1.iters()))
+        assert rel_err(x2, x1) < 1e-7
+        if name == "cg":  # pipelined BiCGStab returns before its last update
+            assert oracle.rel_residual(rp, ci, v, x2, b) < 1e-9

@@ -175,3 +175,58 @@ def test_zero_on_diagonal(V):
     with pytest.raises(V.VclgbError) as e:
         V.jacobi_precond(A)
     assert e.value.status == V.ZERO_ON_DIAGONAL
+
+
+@pytest.mark.parametrize("p", [0, 1, 2])
+def test_row_scaling_golden(V, golden, p):
+    # row_scaling<compressed_matrix>: the row norms bit-exact (applied to a
+    # vector of ones they come back as 1/norm), BiCGStab preconditioned by them
+    # against the reference's run
+    import torch
+    d = golden("row_scaling_convdiff.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    P = V.row_scaling(A, V.row_scaling_tag(p))
+    ones = torch.ones(len(d["rp"]) - 1, dtype=torch.float64, device="cuda")
+    assert np.array_equal(_np(P.apply(ones)), 1.0 / d["norm%d" % p])
+    tag = V.bicgstab_tag(1e-10, 2000)
+    x = _np(V.solve(A, d["b"], tag, P))
+    assert tag.status() == V.SUCCESS
+    assert iters_close(tag.iters(), int(d["iters_bicgstab_row%d" % p]))
+    assert rel_err(x, d["x_bicgstab_row%d" % p]) < 1e-6
+    if p == 2:
+        L = V.compressed_matrix(d["lp"], d["lc"], d["lv"])
+        tag = V.cg_tag(1e-8, 2000)
+        x = _np(V.solve(L, d["lb"], tag, V.row_scaling(L, V.row_scaling_tag(2))))
+        assert iters_close(tag.iters(), int(d["iters_cg_row2"]))
+        assert rel_err(x, d["x_cg_row2"]) < 1e-6
+
+
+def test_row_scaling_rejects_unknown_norm(V):
+    rp, ci, v = gen.laplace2d(8, 8)
+    A = V.compressed_matrix(rp, ci, v)
+    with pytest.raises(V.VclgbError) as e:
+        V.row_scaling(A, V.row_scaling_tag(3))
+    assert e.value.status == V.INVALID_ARGUMENT
+
+
+def test_kernel_timing_inside_captured_solves(V):
+    # event pairs around each SpMV phase and vector pass, also inside the
+    # solver's CUDA graphs; the solve's result does not change
+    rp, ci, v = gen.laplace2d(64, 64)
+    b = gen.rhs_uniform(len(rp) - 1, 2)
+    A = V.compressed_matrix(rp, ci, v)
+    t0 = V.cg_tag(1e-10, 2000)
+    x0 = _np(V.solve(A, b, t0))
+    A.be.set_kernel_timing(True)
+    try:
+        t1 = V.cg_tag(1e-10, 2000)
+        x1 = _np(V.solve(A, b, t1))
+        spmv, vec = A.be.kernel_times(0), A.be.kernel_times(1)
+    finally:
+        A.be.set_kernel_timing(False)
+    assert np.array_equal(x0, x1) and t0.iters() == t1.iters()
+    # one SpMV and one vector pass per iteration (plus the set-up pair and the
+    # launches of the last captured chunk after convergence)
+    assert len(spmv) >= t1.iters() and len(vec) >= t1.iters()
+    assert np.all(spmv > 0) and np.median(spmv) < 1.0
+    assert len(A.be.kernel_times(0)) == 0  # read and cleared

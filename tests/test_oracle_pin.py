@@ -42,6 +42,61 @@ def test_spmv_alpha_beta_golden(golden):
     assert np.array_equal(oracle.row_blocks(d["rp"]), d["row_blocks"])
 
 
+def test_coo_golden(golden):
+    # coordinate_matrix copy (coordinate_matrix.hpp:46-101) incl. its group
+    # boundaries, and the host COO product: both bit-exact
+    d = golden("coo_lognormal.npz")
+    C = oracle.coo(d["rp"], d["ci"], d["v"])
+    assert C["nnz"] == int(d["nnz"][0]) and C["stored"] == int(d["nnz"][1])
+    assert np.array_equal(C["coords"], d["coords"]) and np.array_equal(C["elems"], d["elems"])
+    assert np.array_equal(C["groups"], d["groups"])
+    assert d["groups"][1] == d["rp"][3] and d["groups"][63] == d["groups"][1]  # group rule
+    n = len(d["rp"]) - 1
+    y = oracle.coo_spmv(n, C, d["x"], float(d["alpha"]), float(d["beta"]), d["y0"])
+    assert np.array_equal(y, d["y"])
+
+
+def test_row_scaling_golden(golden):
+    # row_info row norms (bit-exact) and the solves they precondition
+    # (single thread: iteration count, estimate and solution identical)
+    d = golden("row_scaling_convdiff.npz")
+    for p in range(3):
+        assert np.array_equal(oracle.row_norms(d["rp"], d["v"], p), d["norm%d" % p])
+    oracle.set_threads(1)
+    try:
+        for p in range(3):
+            x, it, err = oracle.solve("bicgstab", d["rp"], d["ci"], d["v"], d["b"], 1e-10, 2000,
+                                      "row%d" % p)
+            assert it == int(d["iters_bicgstab_row%d" % p]) and err == float(d["error_bicgstab_row%d" % p])
+            assert rel_err(x, d["x_bicgstab_row%d" % p]) < 1e-12
+        x, it, err = oracle.solve("cg", d["lp"], d["lc"], d["lv"], d["lb"], 1e-8, 2000, "row2")
+        assert it == int(d["iters_cg_row2"]) and rel_err(x, d["x_cg_row2"]) < 1e-12
+    finally:
+        oracle.set_threads(oracle.max_threads())
+
+
+MM_CASES = [("general", 1), ("general_case", 1), ("symmetric", 1), ("pattern", 1), ("complex", 1),
+            ("zero_based", 0), ("extra_lines", 1), ("bad_word", 1), ("bad_field", 1),
+            ("bad_symmetry", 1), ("array", 1), ("out_of_range", 1), ("too_few", 1),
+            ("missing_value", 1)]
+
+
+@pytest.mark.parametrize("name,base", MM_CASES)
+def test_matrix_market_golden(golden, name, base):
+    # io/matrix_market.hpp reader: lines read, the matrix, and which files fail
+    d = golden("matrix_market.npz")
+    path = os.path.join(os.path.dirname(__file__), "golden", "mm", name + ".mtx")
+    ret = int(d[name + "__ret"][0])
+    if ret == 0:
+        with pytest.raises(ValueError):
+            oracle.read_matrix_market(path, base)
+        return
+    lines, rows, cols, rp, ci, v = oracle.read_matrix_market(path, base)
+    assert lines == ret and rows == int(d[name + "__ret"][1])
+    assert np.array_equal(rp, d[name + "__rp"]) and np.array_equal(ci, d[name + "__ci"])
+    assert np.array_equal(v, d[name + "__v"])
+
+
 def test_spmv_f32_golden(golden):
     d = golden("spmv_f32_lognormal.npz")
     y = oracle.spmv_f32(d["rp"], d["ci"], d["v"].astype(np.float32), d["x"].astype(np.float32))

@@ -101,6 +101,7 @@ VCLGB_API vclgbStatus vclgbBackendDestroy(vclgbBackend *h) {
   be->red_counter.release();
   cudaStreamSynchronize(be->stream);
   if (be->host_flags) cudaFreeHost(be->host_flags);
+  for (cudaEvent_t e : be->tev) cudaEventDestroy(e);
   if (be->own_stream) cudaStreamDestroy(be->stream);
   delete be;
   *h = nullptr;
@@ -130,6 +131,37 @@ VCLGB_API const char *vclgbBackendLastError(vclgbBackend h) {
 }
 
 VCLGB_API uint64_t vclgbBackendLaunchCount(vclgbBackend h) { return h ? B(h)->launches : 0; }
+
+VCLGB_API vclgbStatus vclgbBackendSetKernelTiming(vclgbBackend h, int enable) {
+  if (!h) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    timing_collect(*be, false);
+    be->timing = enable != 0;
+    if (be->timing && be->tev.size() < 1024) {
+      while (be->tev.size() < 1024) {
+        cudaEvent_t e;
+        VCLGB_CUDA(cudaEventCreate(&e));
+        be->tev.push_back(e);
+      }
+    }
+    be->times[0].clear();
+    be->times[1].clear();
+  });
+}
+
+VCLGB_API vclgbStatus vclgbBackendKernelTimes(vclgbBackend h, int kind, float *out,
+                                              uint64_t capacity, uint64_t *count) {
+  if (!h || !count || (kind != 0 && kind != 1)) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    timing_collect(*be, false);
+    std::vector<float> &t = be->times[kind];
+    *count = t.size();
+    if (out) std::memcpy(out, t.data(), std::min<uint64_t>(capacity, t.size()) * sizeof(float));
+    t.clear();
+  });
+}
 
 // ---------------------------------------------------------------------------
 VCLGB_API vclgbStatus vclgbCsrCreate(vclgbBackend h, vclgbPrecision prec, uint32_t rows,
@@ -169,6 +201,9 @@ VCLGB_API vclgbStatus vclgbMatrixToSell(vclgbBackend h, vclgbMatrix csr, uint32_
 VCLGB_API vclgbStatus vclgbMatrixToHyb(vclgbBackend h, vclgbMatrix csr, double thr,
                                        vclgbMatrix *out) {
   return convert(h, csr, out, [&](Backend &be, Matrix &m) { return convert_hyb(be, m, thr); });
+}
+VCLGB_API vclgbStatus vclgbMatrixToCoo(vclgbBackend h, vclgbMatrix csr, vclgbMatrix *out) {
+  return convert(h, csr, out, [](Backend &be, Matrix &m) { return convert_coo(be, m); });
 }
 VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend h, vclgbMatrix m, vclgbMatrix *out) {
   return convert(h, m, out, [&](Backend &be, Matrix &mm) { return convert_f32(be, mm); });
@@ -263,6 +298,55 @@ VCLGB_API vclgbStatus vclgbHybWrap(vclgbBackend h, vclgbPrecision prec, uint32_t
   });
 }
 
+VCLGB_API vclgbStatus vclgbCooWrap(vclgbBackend h, vclgbPrecision prec, uint32_t rows,
+                                   uint32_t cols, uint64_t nnz, const uint32_t *coords,
+                                   const void *elems, vclgbMatrix *out) {
+  if (!h || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(prec == VCLGB_FLOAT32 || prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "bad precision");
+    require(!nnz || (coords && elems), VCLGB_INVALID_ARGUMENT, "NULL arrays");
+    require(((uintptr_t)coords & 7) == 0, VCLGB_INVALID_ARGUMENT,
+            "COO coordinate pairs must be 8-byte aligned");
+    require(nnz <= 0xffffffffull, VCLGB_INVALID_ARGUMENT, "nnz exceeds 32-bit indices");
+    auto m = std::make_unique<Matrix>();
+    m->format = VCLGB_COO;
+    m->prec = prec;
+    m->rows = rows;
+    m->cols = cols;
+    m->nnz = nnz;
+    m->tail_nnz = nnz;
+    m->coo_stored = nnz;
+    if (nnz) {
+      m->coo_coords.borrow(coords, nnz * 8);
+      m->coo_elems.borrow(elems, nnz * m->vsize());
+      coo_validate(*be, *m);
+    }
+    coo_groups(*be, *m);
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbReadMatrixMarket(vclgbBackend h, const char *path, int64_t index_base,
+                                            vclgbPrecision prec, vclgbMatrix *out,
+                                            uint64_t *lines_read) {
+  if (!h || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    require(prec == VCLGB_FLOAT32 || prec == VCLGB_FLOAT64, VCLGB_INVALID_ARGUMENT, "bad precision");
+    auto m = read_matrix_market(*be, path, (long)index_base, prec, lines_read);
+    *out = reinterpret_cast<vclgbMatrix>(m.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbWriteMatrixMarket(vclgbBackend h, vclgbMatrix A, const char *path,
+                                             int64_t index_base, int digits) {
+  if (!h || !A) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { write_matrix_market(*be, *M(A), path, (long)index_base, digits); });
+}
+
 VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m) {
   if (!m || !*m) return VCLGB_INVALID_ARGUMENT;
   Matrix *mm = M(*m);
@@ -295,6 +379,7 @@ VCLGB_API vclgbStatus vclgbMatrixGetInfo(vclgbMatrix h, vclgbMatrixInfo *info) {
       info->ell_width = m.ell_width;
       info->tail_nnz = m.tail_nnz ? m.tail_nnz : 1;
       break;
+    case VCLGB_COO: info->stored = m.coo_stored; break;
   }
   return VCLGB_SUCCESS;
 }
@@ -357,6 +442,11 @@ VCLGB_API vclgbStatus vclgbMatrixExport(vclgbBackend h, vclgbMatrix mh, int whic
         else if (which == 4) { src = m.tail_v.ptr; bytes = t * vs; }
         break;
       }
+      case VCLGB_COO:
+        if (which == 0) { src = m.coo_coords.ptr; bytes = m.coo_stored * 8; }
+        else if (which == 1) { src = m.coo_elems.ptr; bytes = m.coo_stored * vs; }
+        else if (which == 2) { src = m.coo_groups.ptr; bytes = 65 * 4; }
+        break;
     }
     require(which >= 0 && (src != nullptr || bytes == 0) && which <= 4, VCLGB_INVALID_ARGUMENT,
             "no such array for this format");
@@ -377,20 +467,28 @@ VCLGB_API vclgbStatus vclgbSpmv(vclgbBackend h, vclgbMatrix A, double alpha, con
     if (m.rows == 0) return;
     Reduction red{be->red_partials.ptr, be->red_counter.as<unsigned>()};
     DevBuf hyb;
-    if (m.format == VCLGB_HYB && m.tail_nnz) hyb.alloc(hyb_scratch_bytes(m), be->stream);
+    if (hyb_scratch_bytes(m)) hyb.alloc(hyb_scratch_bytes(m), be->stream);
+    const bool unit = ys == 0 && yinc == 1;
     if (m.prec == VCLGB_FLOAT64) {
       with_axpby_mode(alpha, beta, [&](auto mode) {
-        EpiAxpbyM<double, decltype(mode)::value> e{alpha, beta, static_cast<double *>(y), ys,
-                                                   yinc};
-        spmv_launch<double>(*be, m, static_cast<const double *>(x), xs, xinc, e, red,
-                            static_cast<double *>(y), ys, yinc, alpha, beta, nullptr, hyb.ptr);
+        auto go = [&](auto e) {
+          e.alpha = alpha; e.beta = beta; e.y = static_cast<double *>(y); e.ys = ys; e.yinc = yinc;
+          spmv_launch<double>(*be, m, static_cast<const double *>(x), xs, xinc, e, red,
+                              static_cast<double *>(y), ys, yinc, alpha, beta, nullptr, hyb.ptr);
+        };
+        if (unit) go(EpiAxpbyM<double, decltype(mode)::value, true>{});
+        else go(EpiAxpbyM<double, decltype(mode)::value, false>{});
       });
     } else {
       const float af = (float)alpha, bf = (float)beta;
       with_axpby_mode(af, bf, [&](auto mode) {
-        EpiAxpbyM<float, decltype(mode)::value> e{af, bf, static_cast<float *>(y), ys, yinc};
-        spmv_launch<float>(*be, m, static_cast<const float *>(x), xs, xinc, e, red,
-                           static_cast<float *>(y), ys, yinc, af, bf, nullptr, hyb.ptr);
+        auto go = [&](auto e) {
+          e.alpha = af; e.beta = bf; e.y = static_cast<float *>(y); e.ys = ys; e.yinc = yinc;
+          spmv_launch<float>(*be, m, static_cast<const float *>(x), xs, xinc, e, red,
+                             static_cast<float *>(y), ys, yinc, af, bf, nullptr, hyb.ptr);
+        };
+        if (unit) go(EpiAxpbyM<float, decltype(mode)::value, true>{});
+        else go(EpiAxpbyM<float, decltype(mode)::value, false>{});
       });
     }
   });
@@ -417,6 +515,17 @@ VCLGB_API vclgbStatus vclgbJacobiCreate(vclgbBackend h, vclgbMatrix A, vclgbPrec
   Backend *be = B(h);
   return guarded(be, [&]() {
     auto P = jacobi_create(*be, *M(A));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbPrecond>(P.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbRowScalingCreate(vclgbBackend h, vclgbMatrix A, uint32_t norm,
+                                            vclgbPrecond *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    auto P = row_scaling_create(*be, *M(A), norm);
     VCLGB_CUDA(cudaStreamSynchronize(be->stream));
     *out = reinterpret_cast<vclgbPrecond>(P.release());
   });

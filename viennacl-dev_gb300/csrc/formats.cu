@@ -573,6 +573,116 @@ std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double thres
   return out;
 }
 
+// ---------------------------------------------------------------------------
+// COO (coordinate_matrix.hpp:46-101): (row, col) pairs interleaved, values,
+// both zero-padded to a multiple of 128 entries (AlignmentV = 128), and the
+// 65 group boundaries of the reference's copy().
+// ---------------------------------------------------------------------------
+constexpr uint64_t kCooAlign = 128;
+
+template <typename V>
+__global__ void coo_fill_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                const uint32_t *__restrict__ ci, const V *__restrict__ vals,
+                                uint2 *coords, V *elems) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x)
+    for (uint32_t k = rp[r]; k < rp[r + 1]; ++k) {
+      coords[k] = make_uint2((uint32_t)r, ci[k]);
+      elems[k] = vals[k];
+    }
+}
+
+// The reference's boundary loop (coordinate_matrix.hpp:74-91) compares the
+// running entry count with vcl_size_t((f+1)/64.0) * nnz: the cast truncates
+// the ratio, so the bound is 0 for every f < 63.  Group 0 therefore ends
+// after the first non-empty row, groups 1..62 are empty and group 63 holds
+// the rest; this kernel writes exactly that (d1 = entries of the first row).
+__global__ void coo_groups_kernel(uint64_t nnz, const uint2 *__restrict__ coords,
+                                  uint32_t *groups) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  uint64_t d1 = 0;
+  if (nnz > 0) {
+    const uint32_t row0 = coords[0].x;
+    uint64_t lo = 1, hi = nnz;  // first k with coords[k].x != row0 (rows sorted)
+    while (lo < hi) {
+      const uint64_t mid = lo + (hi - lo) / 2;
+      if (coords[mid].x == row0) lo = mid + 1;
+      else hi = mid;
+    }
+    d1 = lo;
+  }
+  groups[0] = 0;
+  for (int g = 1; g < 64; ++g) groups[g] = (uint32_t)d1;
+  groups[64] = (uint32_t)nnz;
+}
+
+void coo_groups(Backend &be, Matrix &m) {
+  m.coo_groups.alloc(65 * sizeof(uint32_t), be.stream);
+  coo_groups_kernel<<<1, 32, 0, be.stream>>>(m.tail_nnz, m.coo_coords.as<uint2>(),
+                                             m.coo_groups.as<uint32_t>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
+std::unique_ptr<Matrix> convert_coo(Backend &be, const Matrix &csr) {
+  require(csr.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "conversion source must be CSR");
+  auto out = std::make_unique<Matrix>();
+  copy_header(csr, *out, VCLGB_COO);
+  const uint64_t nnz = csr.nnz;
+  const uint64_t stored = (nnz + kCooAlign - 1) / kCooAlign * kCooAlign;
+  const size_t vs = csr.vsize();
+  out->coo_stored = stored;
+  out->tail_nnz = nnz;
+  out->coo_coords.alloc(std::max<uint64_t>(stored, 1) * 2 * sizeof(uint32_t), be.stream);
+  out->coo_elems.alloc(std::max<uint64_t>(stored, 1) * vs, be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(out->coo_coords.ptr, 0, out->coo_coords.bytes, be.stream));
+  VCLGB_CUDA(cudaMemsetAsync(out->coo_elems.ptr, 0, out->coo_elems.bytes, be.stream));
+  if (nnz > 0) {
+    int g = waves_grid(be, 256, 8, csr.rows);
+    if (vs == 8)
+      coo_fill_kernel<uint64_t><<<g, 256, 0, be.stream>>>(
+          csr.rows, csr.row_ptr, csr.col_idx, static_cast<const uint64_t *>(csr.values),
+          out->coo_coords.as<uint2>(), out->coo_elems.as<uint64_t>());
+    else
+      coo_fill_kernel<uint32_t><<<g, 256, 0, be.stream>>>(
+          csr.rows, csr.row_ptr, csr.col_idx, static_cast<const uint32_t *>(csr.values),
+          out->coo_coords.as<uint2>(), out->coo_elems.as<uint32_t>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+  }
+  coo_groups(be, *out);
+  return out;
+}
+
+// wrapped COO arrays: rows sorted and in range, columns in range
+__global__ void coo_validate_kernel(uint64_t nnz, uint32_t rows, uint32_t cols,
+                                    const uint2 *__restrict__ coords, unsigned *bad) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const uint2 rc = coords[k];
+    if (rc.x >= rows) atomicOr(bad, 1u);
+    if (rc.y >= cols) atomicOr(bad, 2u);
+    if (k > 0 && coords[k - 1].x > rc.x) atomicOr(bad, 4u);
+  }
+}
+
+void coo_validate(Backend &be, const Matrix &m) {
+  if (m.tail_nnz == 0) return;
+  DevBuf flag(sizeof(unsigned), be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), be.stream));
+  int g = waves_grid(be, 256, 8, m.tail_nnz);
+  coo_validate_kernel<<<g, 256, 0, be.stream>>>(m.tail_nnz, m.rows, m.cols,
+                                                m.coo_coords.as<uint2>(), flag.as<unsigned>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  unsigned h = 0;
+  VCLGB_CUDA(cudaMemcpyAsync(&h, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  if (h & 1) throw Error(VCLGB_INVALID_MATRIX, "COO row index out of range");
+  if (h & 2) throw Error(VCLGB_INVALID_MATRIX, "COO column index out of range");
+  if (h & 4) throw Error(VCLGB_INVALID_MATRIX, "COO entries are not sorted by row");
+}
+
 __global__ void tail_rows_kernel(uint32_t rows, const uint32_t *__restrict__ trp, uint32_t *trow) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
        r += (size_t)gridDim.x * blockDim.x)

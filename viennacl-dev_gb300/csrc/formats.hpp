@@ -10,6 +10,10 @@ std::unique_ptr<Matrix> convert_sell(Backend &be, const Matrix &csr, uint32_t C,
 void sell_wide_chunks(Backend &be, Matrix &m);
 std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold);
 std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m);
+std::unique_ptr<Matrix> convert_coo(Backend &be, const Matrix &csr);
+// COO wrapped from reference arrays: checks the pairs, then derives the groups
+void coo_validate(Backend &be, const Matrix &m);
+void coo_groups(Backend &be, Matrix &m);
 // COO row of every tail entry from the tail row_ptr (HYB wrapped from reference arrays)
 void tail_rows_from_rp(Backend &be, uint32_t rows, const uint32_t *trp, uint64_t tnnz,
                        uint32_t *trow);
@@ -17,8 +21,15 @@ void csr_row_blocks(Backend &be, Matrix &m);
 // out[0..n) = exclusive scan of in, out[n] = total; returns the total (host-synchronising)
 uint64_t extern_scan_u32(Backend &be, const uint32_t *in, size_t n, uint32_t *out);
 
+// MatrixMarket files (mmio.cu)
+std::unique_ptr<Matrix> read_matrix_market(Backend &be, const char *path, long index_base,
+                                           vclgbPrecision prec, uint64_t *lines_read);
+void write_matrix_market(Backend &be, const Matrix &m, const char *path, long index_base,
+                         int digits);
+
 // preconditioners (precond.cu)
 std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A);
+std::unique_ptr<Precond> row_scaling_create(Backend &be, const Matrix &A, uint32_t norm);
 std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_scheduling);
 // z = M^-1 z in place; skipped on the device when *skip_flag != 0
 void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);

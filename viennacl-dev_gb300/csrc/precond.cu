@@ -70,6 +70,72 @@ std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A) {
 }
 
 // ---------------------------------------------------------------------------
+// row_scaling (linalg/row_scaling.hpp:150-191): a diagonal preconditioner
+// whose entries are row norms of A, from row_info SPARSE_ROW_NORM_INF / _1 / _2
+// (linalg/host_based/sparse_matrix_operations.hpp:52-98): rows summed in
+// storage order with separate multiply and add (no fused multiply-add), so
+// the norms equal the reference's bit for bit.  The apply is Jacobi's
+// element_div, fused into the solvers in the same way.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b);
+template <>
+__device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
+template <>
+__device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T sqr_rn(T a);
+template <>
+__device__ __forceinline__ double sqr_rn<double>(double a) { return __dmul_rn(a, a); }
+template <>
+__device__ __forceinline__ float sqr_rn<float>(float a) { return __fmul_rn(a, a); }
+
+template <typename T>
+__global__ void row_norm_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                const T *__restrict__ v, uint32_t norm, T *d) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    T value = 0;
+    const uint32_t e = rp[r + 1];
+    if (norm == 0) {
+      for (uint32_t k = rp[r]; k < e; ++k) {
+        const T a = fabs(v[k]);
+        value = value < a ? a : value;  // std::max(value, |a|)
+      }
+    } else if (norm == 1) {
+      for (uint32_t k = rp[r]; k < e; ++k) value = add_rn(value, T(fabs(v[k])));
+    } else {
+      for (uint32_t k = rp[r]; k < e; ++k) value = add_rn(value, sqr_rn(v[k]));
+      value = sqrt(value);
+    }
+    d[r] = value;
+  }
+}
+
+std::unique_ptr<Precond> row_scaling_create(Backend &be, const Matrix &A, uint32_t norm) {
+  require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "row_scaling is built from CSR");
+  require(norm <= 2, VCLGB_INVALID_ARGUMENT,
+          "unknown norm for row_scaling (0 = max, 1 = sum, 2 = Euclidean)");
+  auto P = std::make_unique<Precond>();
+  P->kind = 1;  // a diagonal, applied like Jacobi's
+  P->prec = A.prec;
+  P->rows = A.rows;
+  P->diag.alloc(std::max<size_t>(A.rows, 1) * A.vsize(), be.stream);
+  if (A.rows) {
+    int g = waves_grid(be, 256, 8, A.rows);
+    if (A.prec == VCLGB_FLOAT64)
+      row_norm_kernel<double><<<g, 256, 0, be.stream>>>(
+          A.rows, A.row_ptr, static_cast<const double *>(A.values), norm, P->diag.as<double>());
+    else
+      row_norm_kernel<float><<<g, 256, 0, be.stream>>>(
+          A.rows, A.row_ptr, static_cast<const float *>(A.values), norm, P->diag.as<float>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+  }
+  return P;
+}
+
+// ---------------------------------------------------------------------------
 // ILU0
 // ---------------------------------------------------------------------------
 // numeric factorisation of the rows of one level (thread per row)

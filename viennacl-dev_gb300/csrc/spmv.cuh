@@ -39,16 +39,22 @@ __device__ __forceinline__ bool nonzero_bits(float v) { return (__float_as_int(v
 
 // epilogue: y = alpha*acc + beta*y (linalg/cuda/sparse_matrix_operations.hpp prod_impl).
 // MODE 0: alpha == 1, beta == 0; MODE 1: beta == 0; MODE 2: general (y read).
-template <typename T, int MODE>
+// UNIT: y is contiguous (start 0, stride 1), so a row's slot needs no 64-bit
+// index arithmetic -- measurable in the padded formats' short per-row paths.
+template <typename T, int MODE, bool UNIT = false>
 struct EpiAxpbyM {
   static constexpr int NDOT = 0;
   T alpha, beta;
   T *y;
   int64_t ys, yinc;
   struct Pre { T yold; };
+  __device__ __forceinline__ T *slot(uint32_t r) const {
+    if constexpr (UNIT) return y + r;
+    else return y + ys + (int64_t)r * yinc;
+  }
   __device__ __forceinline__ bool skip() const { return false; }
   __device__ __forceinline__ Pre pre(uint32_t r) const {
-    if constexpr (MODE == 2) return {y[ys + (int64_t)r * yinc]};
+    if constexpr (MODE == 2) return {*slot(r)};
     else return {T(0)};
   }
   __device__ __forceinline__ void row(uint32_t r, T acc, const Pre &pv, T (&)[1]) const {
@@ -56,7 +62,7 @@ struct EpiAxpbyM {
     if constexpr (MODE == 0) out = acc;
     else if constexpr (MODE == 1) out = alpha * acc;
     else out = alpha * acc + beta * pv.yold;
-    y[ys + (int64_t)r * yinc] = out;
+    *slot(r) = out;
   }
   __device__ __forceinline__ void finalize(const T (&)[1]) const {}
 };
@@ -72,8 +78,8 @@ void with_axpby_mode(T alpha, T beta, F &&f) {
 }
 
 // same, with an early-exit flag (solver converged)
-template <typename T, int MODE>
-struct EpiAxpbySkip : EpiAxpbyM<T, MODE> {
+template <typename T, int MODE, bool UNIT = false>
+struct EpiAxpbySkip : EpiAxpbyM<T, MODE, UNIT> {
   const int *flag;
   __device__ __forceinline__ bool skip() const { return flag && *flag; }
 };
@@ -321,12 +327,15 @@ __device__ __forceinline__ bool finite_bits(float v) {
   return (__float_as_int(v) & 0x7f800000) != 0x7f800000;
 }
 
+// The rare non-finite path: a plain loop (not unrolled), so that it takes no
+// registers from the fast path of every row.
 template <typename T>
 __device__ __forceinline__ T strided_row_skip(size_t base, uint32_t w, size_t stride,
                                            const uint32_t *__restrict__ cols,
                                            const T *__restrict__ elems, const T *__restrict__ x,
                                            int64_t xs, int64_t xinc) {
   T acc = 0;
+#pragma unroll 1
   for (uint32_t j = 0; j < w; ++j) {
     const T v = elems[base + (size_t)j * stride];
     if (nonzero_bits(v)) acc += v * x[xs + (int64_t)cols[base + (size_t)j * stride] * xinc];
@@ -511,15 +520,23 @@ __global__ void __launch_bounds__(kSpmvThreads)
 }
 
 // ---------------------------------------------------------------------------
-// HYB tail: COO entries (row-sorted) in chunks of 32*K per warp.  Products are
-// combined with a warp-segmented scan; segments that lie wholly inside a chunk
-// are added to y directly, the first and last segment of every chunk go to a
-// carry array that hyb_tail_fixup adds in chunk order (deterministic).
+// HYB tail: COO entries (row-sorted) in chunks of 32*K per warp; lane l of the
+// warp owns the K consecutive entries c0 + K*l ... of its chunk.  A lane sums
+// its entries in order, row by row (one multiply and one add per entry); the
+// rows that start and end inside a lane are complete and go to y at once.
+// Only the lane's first and last row can continue into a neighbouring lane:
+// one warp-segmented scan over the 32 lane partials (keyed by row) joins
+// them.  The first and last row of every chunk can continue into the
+// neighbouring chunk: they go to a carry array that hyb_tail_fixup adds in
+// chunk order (deterministic, no atomics).  Per entry this costs about three
+// FP64 instructions, against six for a scan over every entry.
 // ---------------------------------------------------------------------------
-constexpr int kTailK = 8;                       // steps of 32 entries per warp chunk
+constexpr int kTailK = 8;                       // consecutive entries per lane
 constexpr int kTailChunk = 32 * kTailK;
 
-template <typename T>
+// PAIRS: trow holds interleaved (row, col) pairs (coordinate_matrix's
+// handle12 layout) and tcol is unused.
+template <typename T, bool PAIRS = false>
 __global__ void __launch_bounds__(kSpmvThreads)
     hyb_tail_kernel(uint64_t tnnz, const uint32_t *__restrict__ trow,
                     const uint32_t *__restrict__ tcol, const T *__restrict__ tval,
@@ -534,42 +551,86 @@ __global__ void __launch_bounds__(kSpmvThreads)
   for (size_t ch = warp; ch < nchunks; ch += nwarps) {
     const size_t c0 = ch * kTailChunk;
     const size_t c1 = c0 + kTailChunk < tnnz ? c0 + kTailChunk : tnnz;
-    const uint32_t first_row = __ldg(trow + c0);
-    const uint32_t last_row = __ldg(trow + c1 - 1);
-    T run = 0;             // inclusive sum at the last entry of the previous step
-    uint32_t run_row = INV;
-    for (size_t k0 = c0; k0 < c1; k0 += 32) {
-      const size_t k = k0 + lane;
-      const bool ok = k < c1;
-      const uint32_t r = ok ? __ldg(trow + k) : INV;
-      T p = ok ? __ldg(tval + k) * __ldg(x + xs + (int64_t)__ldg(tcol + k) * xinc) : T(0);
-      if (lane == 0 && r == run_row) p += run;
-      // segmented inclusive scan (rows are sorted, so equal row <=> same segment)
+    const uint32_t chunk_first = __ldg(trow + (PAIRS ? 2 * c0 : c0));
+    const uint32_t chunk_last = __ldg(trow + (PAIRS ? 2 * (c1 - 1) : c1 - 1));
+    const size_t e0 = c0 + (size_t)lane * kTailK;
+    const uint32_t cnt = e0 < c1 ? (uint32_t)(c1 - e0 < (size_t)kTailK ? c1 - e0 : kTailK) : 0u;
+    // every load of the lane's entries first, then its x gathers
+    uint32_t r[kTailK], c[kTailK];
+    T v[kTailK];
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        T q = __shfl_up_sync(0xffffffffu, p, o);
-        uint32_t qr = __shfl_up_sync(0xffffffffu, r, o);
-        if ((int)lane >= o && qr == r) p += q;
+    for (int k = 0; k < kTailK; ++k) {
+      const bool in = (uint32_t)k < cnt;
+      if constexpr (PAIRS) {
+        const uint2 rc = in ? __ldg(reinterpret_cast<const uint2 *>(trow) + e0 + k)
+                            : make_uint2(INV, 0u);
+        r[k] = rc.x;
+        c[k] = rc.y;
+      } else {
+        r[k] = in ? __ldg(trow + e0 + k) : INV;
+        c[k] = in ? __ldg(tcol + e0 + k) : 0u;
       }
-      uint32_t nr = __shfl_down_sync(0xffffffffu, r, 1);
-      if (lane == 31) nr = (k + 1 < c1) ? __ldg(trow + k + 1) : INV;
-      if (ok && nr != r) {  // last entry of row r inside this chunk
-        if (r == first_row) {
-          carry_row[2 * ch] = r;
-          carry_val[2 * ch] = p;
-        } else if (r == last_row) {
-          carry_row[2 * ch + 1] = r;
-          carry_val[2 * ch + 1] = p;
+      v[k] = in ? __ldg(tval + e0 + k) : T(0);
+    }
+    T p[kTailK];
+#pragma unroll
+    for (int k = 0; k < kTailK; ++k)
+      p[k] = (uint32_t)k < cnt ? v[k] * __ldg(x + xs + (int64_t)c[k] * xinc) : T(0);
+    // in-lane pass: first row's sum, complete interior rows, running last row
+    const uint32_t first_row = r[0];
+    uint32_t cur_row = r[0];
+    T cur = p[0], first_sum = T(0);
+    bool multi = false;
+#pragma unroll
+    for (int k = 1; k < kTailK; ++k) {
+      if ((uint32_t)k < cnt) {
+        if (r[k] == cur_row) {
+          cur += p[k];
         } else {
-          T *py = y + ys + (int64_t)r * yinc;
-          *py += alpha * p;
+          if (!multi) {
+            first_sum = cur;
+            multi = true;
+          } else {  // starts and ends inside this lane: neither chunk end
+            T *py = y + ys + (int64_t)cur_row * yinc;
+            *py += alpha * cur;
+          }
+          cur_row = r[k];
+          cur = p[k];
         }
       }
-      const int lastlane = (int)((c1 - k0 < 32 ? c1 - k0 : 32) - 1);
-      run = __shfl_sync(0xffffffffu, p, lastlane);
-      run_row = __shfl_sync(0xffffffffu, r, lastlane);
     }
-    if (lane == 0 && first_row == last_row) carry_row[2 * ch + 1] = INV;
+    // segmented inclusive scan of the lanes' last-row partials; equal keys
+    // are contiguous because the rows are sorted
+    const uint32_t key = cur_row;
+    T run = cur;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T q = __shfl_up_sync(0xffffffffu, run, o);
+      const uint32_t qk = __shfl_up_sync(0xffffffffu, key, o);
+      if ((int)lane >= o && qk == key) run += q;
+    }
+    const T prev_run = __shfl_up_sync(0xffffffffu, run, 1);
+    const uint32_t prev_key = __shfl_up_sync(0xffffffffu, key, 1);
+    const uint32_t next_first = __shfl_down_sync(0xffffffffu, first_row, 1);
+    if (cnt > 0) {
+      // a row that ends here: goes to the chunk's carry slots if it is the
+      // chunk's first or last row, else straight to y
+      auto emit = [&](uint32_t row, T total) {
+        if (row == chunk_first) {
+          carry_row[2 * ch] = row;
+          carry_val[2 * ch] = total;
+        } else if (row == chunk_last) {
+          carry_row[2 * ch + 1] = row;
+          carry_val[2 * ch + 1] = total;
+        } else {
+          T *py = y + ys + (int64_t)row * yinc;
+          *py += alpha * total;
+        }
+      };
+      if (multi) emit(first_row, (lane > 0 && prev_key == first_row) ? first_sum + prev_run : first_sum);
+      if (lane == 31 || next_first != key) emit(key, run);
+    }
+    if (lane == 0 && chunk_first == chunk_last) carry_row[2 * ch + 1] = INV;
   }
 }
 
@@ -645,9 +706,9 @@ template <typename T, class E>
 void ell_launch(Backend &be, int grid, const Matrix &m, const T *x, int64_t xs, int64_t xinc,
                 const E &epi, T *partials, unsigned *counter) {
 #define VCLGB_ELL(W)                                                                          \
-  ell_kernel<W, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(                                  \
-      m.rows, m.ell_width, m.ell_coords.as<uint32_t>(), m.ell_elems.as<T>(), x, xs, xinc, epi, \
-      partials, counter)
+  ell_kernel<W, T, E><<<one_wave<ell_kernel<W, T, E>>(be, grid, kSpmvThreads), kSpmvThreads, 0, \
+                        be.stream>>>(m.rows, m.ell_width, m.ell_coords.as<uint32_t>(),          \
+                                     m.ell_elems.as<T>(), x, xs, xinc, epi, partials, counter)
   switch (m.ell_width) {
     case 1: VCLGB_ELL(1); break;
     case 2: VCLGB_ELL(2); break;
@@ -669,12 +730,15 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
                  void *hyb_scratch = nullptr) {
   int grid = spmv_grid(be, m);
   T *partials = static_cast<T *>(red.partials);
+  const int tp = timing_begin(be, 0);
   switch (m.format) {
     case VCLGB_CSR: {
       CsrView<T> A{m.row_ptr, m.col_idx, static_cast<const T *>(m.values), m.rows};
       const bool single = m.num_bins == 1 && m.bins[0].identity;
 #define VCLGB_CSR_FIXED(L, R)                                                \
-  csr_fixed_kernel<L, R, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(        \
+  csr_fixed_kernel<L, R, T, E><<<one_wave<csr_fixed_kernel<L, R, T, E>>(    \
+                                     be, grid, kSpmvThreads),               \
+                                 kSpmvThreads, 0, be.stream>>>(             \
       A, x, xs, xinc, epi, partials, red.counter)
       const uint32_t lanes = single ? m.bins[0].lanes : 0u;
       if (lanes == 1) {
@@ -692,7 +756,8 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
         VCLGB_CSR_FIXED(4, kMpl);
       } else {
         const size_t nwin = (m.rows + kWinRows - 1) / kWinRows;
-        const int wgrid = (int)(nwin < (size_t)grid ? (nwin ? nwin : 1) : grid);
+        const int wgrid = one_wave<csr_window_kernel<T, E>>(
+            be, (int)(nwin < (size_t)grid ? (nwin ? nwin : 1) : grid), kSpmvThreads);
         csr_window_kernel<T, E><<<wgrid, kSpmvThreads, 0, be.stream>>>(A, x, xs, xinc, epi,
                                                                        partials, red.counter);
       }
@@ -704,43 +769,61 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
       break;
     case VCLGB_SELL:
       if (m.C % 32 == 0)
-        sell_kernel<true, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+        sell_kernel<true, T, E><<<one_wave<sell_kernel<true, T, E>>(be, grid, kSpmvThreads),
+                                  kSpmvThreads, 0, be.stream>>>(
             m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
             m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
             m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, m.sell_wide.as<uint32_t>(),
             m.sell_nwide, x, xs, xinc, epi, partials, red.counter);
       else
-        sell_kernel<false, T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+        sell_kernel<false, T, E><<<one_wave<sell_kernel<false, T, E>>(be, grid, kSpmvThreads),
+                                   kSpmvThreads, 0, be.stream>>>(
             m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
             m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
             m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, nullptr, 0u, x, xs, xinc, epi,
             partials, red.counter);
       break;
-    case VCLGB_HYB: {
-      // y = alpha*ELL*x + beta*y, then y += alpha*tail*x, then the epilogue pass
+    case VCLGB_HYB:
+    case VCLGB_COO: {
+      // y = alpha*ELL*x + beta*y, then y += alpha*tail*x, then the epilogue
+      // pass; COO is the case of an empty ELL part (width 0: the first pass
+      // only scales y) and a tail of all entries
       with_axpby_mode(alpha, beta, [&](auto mode) {
-        EpiAxpbySkip<T, decltype(mode)::value> sp;
-        sp.alpha = alpha; sp.beta = beta; sp.y = y_for_hyb; sp.ys = ys; sp.yinc = yinc;
-        sp.flag = skip_flag;
-        ell_launch<T, EpiAxpbySkip<T, decltype(mode)::value>>(be, grid, m, x, xs, xinc, sp,
-                                                              partials, red.counter);
+        constexpr int MODE = decltype(mode)::value;
+        auto part = [&](auto sp) {
+          sp.alpha = alpha; sp.beta = beta; sp.y = y_for_hyb; sp.ys = ys; sp.yinc = yinc;
+          sp.flag = skip_flag;
+          ell_launch<T, decltype(sp)>(be, grid, m, x, xs, xinc, sp, partials, red.counter);
+        };
+        if (ys == 0 && yinc == 1) part(EpiAxpbySkip<T, MODE, true>{});
+        else part(EpiAxpbySkip<T, MODE, false>{});
       });
       if (m.tail_nnz > 0) {
         size_t nchunks = (m.tail_nnz + kTailChunk - 1) / kTailChunk;
         uint32_t *carry_row = static_cast<uint32_t *>(hyb_scratch);
         T *carry_val = reinterpret_cast<T *>(static_cast<char *>(hyb_scratch) +
                                              ((2 * nchunks * sizeof(uint32_t) + 15) / 16) * 16);
-        int g = waves_grid(be, kSpmvThreads, 8, nchunks * 32);
-        hyb_tail_kernel<T><<<g, kSpmvThreads, 0, be.stream>>>(
-            m.tail_nnz, m.tail_row.as<uint32_t>(), m.tail_ci.as<uint32_t>(), m.tail_v.as<T>(),
-            x, xs, xinc, alpha, y_for_hyb, ys, yinc, carry_row, carry_val, skip_flag);
+        const int g0 = waves_grid(be, kSpmvThreads, 8, nchunks * 32);
+        if (m.format == VCLGB_COO)
+          hyb_tail_kernel<T, true>
+              <<<one_wave<hyb_tail_kernel<T, true>>(be, g0, kSpmvThreads), kSpmvThreads, 0,
+                 be.stream>>>(m.tail_nnz, m.coo_coords.as<uint32_t>(), nullptr,
+                              m.coo_elems.as<T>(), x, xs, xinc, alpha, y_for_hyb, ys, yinc,
+                              carry_row, carry_val, skip_flag);
+        else
+          hyb_tail_kernel<T, false>
+              <<<one_wave<hyb_tail_kernel<T, false>>(be, g0, kSpmvThreads), kSpmvThreads, 0,
+                 be.stream>>>(m.tail_nnz, m.tail_row.as<uint32_t>(), m.tail_ci.as<uint32_t>(),
+                              m.tail_v.as<T>(), x, xs, xinc, alpha, y_for_hyb, ys, yinc,
+                              carry_row, carry_val, skip_flag);
         int g2 = (int)((nchunks + 255) / 256);
         hyb_tail_fixup<T><<<g2, 256, 0, be.stream>>>(nchunks, carry_row, carry_val, alpha,
                                                       y_for_hyb, ys, yinc, skip_flag);
         be.launches += 2;
       }
       if constexpr (E::NDOT > 0) {
-        epilogue_pass_kernel<T, E><<<grid, kSpmvThreads, 0, be.stream>>>(
+        epilogue_pass_kernel<T, E><<<one_wave<epilogue_pass_kernel<T, E>>(be, grid, kSpmvThreads),
+                                     kSpmvThreads, 0, be.stream>>>(
             m.rows, y_for_hyb, epi, partials, red.counter);
         be.launches++;
       }
@@ -749,11 +832,12 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
   }
   be.launches++;
   VCLGB_CHECK_LAUNCH();
+  timing_end(be, tp);
 }
 
 // scratch bytes the HYB tail needs (carry arrays)
 inline size_t hyb_scratch_bytes(const Matrix &m) {
-  if (m.format != VCLGB_HYB || m.tail_nnz == 0) return 0;
+  if ((m.format != VCLGB_HYB && m.format != VCLGB_COO) || m.tail_nnz == 0) return 0;
   size_t nchunks = (m.tail_nnz + kTailChunk - 1) / kTailChunk;
   return ((2 * nchunks * sizeof(uint32_t) + 15) / 16) * 16 + 2 * nchunks * 8 + 16;
 }

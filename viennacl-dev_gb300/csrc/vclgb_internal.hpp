@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <stdint.h>
 
 #include <cstdio>
@@ -103,7 +104,63 @@ struct Backend {
   // persistent reduction scratch for the vector reductions
   DevBuf red_partials;
   DevBuf red_counter;
+  // kernel timing (off by default): every SpMV phase and fused vector pass is
+  // bracketed by a pair of CUDA events, recorded as event nodes when the
+  // launches are captured into a graph; durations (ms) by kind
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;   // event pool, pairs (2k, 2k+1)
+  std::vector<int> tev_kind;      // kind of pair k: 0 SpMV, 1 vector pass
+  size_t tev_used = 0;            // events recorded since the last collection
+  std::vector<float> times[2];
 };
+
+// Starts a timed region of `kind` on the backend's stream; returns the pair
+// index, or -1 when timing is off.
+inline int timing_begin(Backend &be, int kind) {
+  if (!be.timing) return -1;
+  if (be.tev_used + 2 > be.tev.size()) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t e;
+      VCLGB_CUDA(cudaEventCreate(&e));
+      be.tev.push_back(e);
+    }
+  }
+  const int pair = (int)(be.tev_used / 2);
+  if ((size_t)pair >= be.tev_kind.size()) be.tev_kind.resize(pair + 1);
+  be.tev_kind[pair] = kind;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  VCLGB_CUDA(cudaStreamIsCapturing(be.stream, &cs));
+  if (cs == cudaStreamCaptureStatusActive)
+    VCLGB_CUDA(cudaEventRecordWithFlags(be.tev[be.tev_used], be.stream, cudaEventRecordExternal));
+  else
+    VCLGB_CUDA(cudaEventRecord(be.tev[be.tev_used], be.stream));
+  be.tev_used += 2;
+  return pair;
+}
+inline void timing_end(Backend &be, int pair) {
+  if (pair < 0) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  VCLGB_CUDA(cudaStreamIsCapturing(be.stream, &cs));
+  if (cs == cudaStreamCaptureStatusActive)
+    VCLGB_CUDA(cudaEventRecordWithFlags(be.tev[2 * pair + 1], be.stream, cudaEventRecordExternal));
+  else
+    VCLGB_CUDA(cudaEventRecord(be.tev[2 * pair + 1], be.stream));
+}
+// Reads the durations of the recorded pairs (after the stream has finished
+// them).  keep: the events stay in use (they are nodes of a graph that is
+// replayed again).
+inline void timing_collect(Backend &be, bool keep) {
+  if (!be.timing || be.tev_used == 0) return;
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  for (size_t k = 0; k < be.tev_used / 2; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, be.tev[2 * k], be.tev[2 * k + 1]) == cudaSuccess)
+      be.times[be.tev_kind[k] != 0].push_back(ms);
+    else
+      (void)cudaGetLastError();
+  }
+  if (!keep) be.tev_used = 0;
+}
 
 // grid size for grid-stride kernels: a whole number of waves on the 152 SMs
 inline int waves_grid(const Backend &be, int threads, int blocks_per_sm_cap, size_t work_items,
@@ -116,6 +173,32 @@ inline int waves_grid(const Backend &be, int threads, int blocks_per_sm_cap, siz
                 ((size_t)threads * items_per_thread);
   if (need < 1) need = 1;
   return (int)(need < full ? need : full);
+}
+
+// Blocks of kernel K (launched with `threads` threads) that one SM holds at a
+// time, from the occupancy calculator (registers, shared memory).  A kernel
+// needing more than 32 registers a thread fits fewer than 8 blocks of 256
+// threads, and a grid of 8 per SM would then run in two uneven waves.  The
+// value is cached per kernel once known; a failed query is not cached.
+template <auto K>
+inline int resident_blocks(int threads) {
+  static std::atomic<int> cached{0};
+  int v = cached.load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, K, threads, 0) != cudaSuccess || b < 1) {
+    (void)cudaGetLastError();
+    return 8;
+  }
+  cached.store(b, std::memory_order_relaxed);
+  return b;
+}
+
+// caps the grid of a grid-stride kernel at one full wave of K
+template <auto K>
+inline int one_wave(const Backend &be, int grid, int threads) {
+  const long full = (long)be.num_sms * resident_blocks<K>(threads);
+  return grid < full ? grid : (int)full;
 }
 
 // ---------------------------------------------------------------------------
@@ -176,6 +259,11 @@ struct Matrix {
   // HYB tail: reference CSR arrays + COO rows for the segmented kernel
   uint64_t tail_nnz = 0;     // real tail entries (0 if empty)
   DevBuf tail_rp, tail_ci, tail_v, tail_row;
+
+  // COO (coordinate_matrix): interleaved (row, col) pairs, values, groups;
+  // tail_nnz holds the entry count the segmented kernel runs over
+  uint64_t coo_stored = 0;   // nnz rounded up to the reference's 128
+  DevBuf coo_coords, coo_elems, coo_groups;
 
   // cached FP32 copy used by the mixed-precision solvers
   std::unique_ptr<Matrix> f32_copy;

@@ -36,10 +36,13 @@ inline int vec_grid(const Backend &be, size_t n) { return waves_grid(be, kVecThr
 
 template <typename T, class F>
 void vec_pass(Backend &be, size_t n, const F &f, const Reduction &red) {
-  vec_pass_kernel<T, F><<<vec_grid(be, n), kVecThreads, 0, be.stream>>>(
+  const int tp = timing_begin(be, 1);
+  vec_pass_kernel<T, F><<<one_wave<vec_pass_kernel<T, F>>(be, vec_grid(be, n), kVecThreads),
+                          kVecThreads, 0, be.stream>>>(
       n, f, static_cast<T *>(red.partials), red.counter);
   be.launches++;
   VCLGB_CHECK_LAUNCH();
+  timing_end(be, tp);
 }
 
 // a single-thread device step (scalar bookkeeping between passes)
@@ -68,6 +71,7 @@ void run_iterations(Backend &be, const int *d_done, uint32_t max_chunks_hint, ui
   if (check_every == 0) check_every = 16;
   cudaGraphExec_t exec = nullptr;
   uint64_t per_chunk = 0;
+  timing_collect(be, false);  // launches before the loop (timing on only)
   if (use_graph) {
     cudaGraph_t graph = nullptr;
     VCLGB_CUDA(cudaStreamBeginCapture(be.stream, cudaStreamCaptureModeThreadLocal));
@@ -98,6 +102,7 @@ void run_iterations(Backend &be, const int *d_done, uint32_t max_chunks_hint, ui
     VCLGB_CUDA(cudaMemcpyAsync(be.host_flags, d_done, sizeof(int), cudaMemcpyDeviceToHost,
                                be.stream));
     VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    timing_collect(be, exec != nullptr);  // graph events are replayed again
     ++chunks;
     if (*be.host_flags != kRunning) break;
     if (chunks > limit) {
@@ -106,6 +111,7 @@ void run_iterations(Backend &be, const int *d_done, uint32_t max_chunks_hint, ui
     }
   }
   if (exec) VCLGB_CUDA(cudaGraphExecDestroy(exec));
+  be.tev_used = 0;
 }
 
 }  // namespace vclgb

@@ -28,7 +28,7 @@ STATUS_NAMES = ["SUCCESS", "GENERIC_FAILURE", "INVALID_ARGUMENT", "INVALID_MATRI
                 "OUT_OF_MEMORY", "CUDA_ERROR", "NOT_CONVERGED", "BREAKDOWN",
                 "ZERO_ON_DIAGONAL", "TIMEOUT", "UNSUPPORTED"]
 FLOAT32, FLOAT64 = 0, 1
-CSR, ELL, SELL, HYB = 0, 1, 2, 3
+CSR, ELL, SELL, HYB, COO = 0, 1, 2, 3, 4
 
 
 class VclgbError(RuntimeError):
@@ -87,15 +87,23 @@ SIGNATURES = {
     "vclgbBackendSynchronize": (_I32, [_P]),
     "vclgbBackendLastError": (ctypes.c_char_p, [_P]),
     "vclgbBackendLaunchCount": (_U64, [_P]),
+    "vclgbBackendSetKernelTiming": (_I32, [_P, _I32]),
+    "vclgbBackendKernelTimes": (_I32, [_P, _I32, ctypes.POINTER(ctypes.c_float), _U64,
+                                       ctypes.POINTER(_U64)]),
     "vclgbCsrCreate": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, _P, ctypes.POINTER(_P)]),
     "vclgbMatrixToEll": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "vclgbMatrixToSell": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
     "vclgbMatrixToHyb": (_I32, [_P, _P, _D, ctypes.POINTER(_P)]),
+    "vclgbMatrixToCoo": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "vclgbMatrixToFloat32": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "vclgbEllWrap": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, ctypes.POINTER(_P)]),
     "vclgbSellWrap": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, _P, _P, ctypes.POINTER(_P)]),
     "vclgbHybWrap": (_I32, [_P, _I32, _U32, _U32, _U32, _P, _P, _P, _P, _P, _U64,
                             ctypes.POINTER(_P)]),
+    "vclgbCooWrap": (_I32, [_P, _I32, _U32, _U32, _U64, _P, _P, ctypes.POINTER(_P)]),
+    "vclgbReadMatrixMarket": (_I32, [_P, ctypes.c_char_p, _I64, _I32, ctypes.POINTER(_P),
+                                     ctypes.POINTER(_U64)]),
+    "vclgbWriteMatrixMarket": (_I32, [_P, _P, ctypes.c_char_p, _I64, _I32]),
     "vclgbMatrixDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbMatrixGetInfo": (_I32, [_P, ctypes.POINTER(MatrixInfo)]),
     "vclgbMatrixExport": (_I32, [_P, _P, _I32, _P]),
@@ -104,6 +112,7 @@ SIGNATURES = {
     "vclgbDot": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, _P]),
     "vclgbNorm2": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P]),
     "vclgbJacobiCreate": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "vclgbRowScalingCreate": (_I32, [_P, _P, _U32, ctypes.POINTER(_P)]),
     "vclgbIlu0Create": (_I32, [_P, _P, _I32, ctypes.POINTER(_P)]),
     "vclgbPrecondApply": (_I32, [_P, _P, _P]),
     "vclgbPrecondDestroy": (_I32, [ctypes.POINTER(_P)]),
@@ -183,6 +192,17 @@ class Backend:
 
     def launches(self):
         return int(self.lib.vclgbBackendLaunchCount(self.h))
+
+    def set_kernel_timing(self, enable):
+        """Brackets every SpMV phase and fused vector pass with CUDA events."""
+        self.check(self.lib.vclgbBackendSetKernelTiming(self.h, 1 if enable else 0))
+
+    def kernel_times(self, kind, capacity=1 << 20):
+        """Durations (ms) recorded since the last call: kind 0 SpMV, 1 vector pass."""
+        buf = (ctypes.c_float * capacity)()
+        cnt = _U64()
+        self.check(self.lib.vclgbBackendKernelTimes(self.h, kind, buf, capacity, ctypes.byref(cnt)))
+        return np.frombuffer(buf, dtype=np.float32, count=min(cnt.value, capacity)).copy()
 
     def __del__(self):
         if _exiting:
@@ -335,6 +355,15 @@ class hyb_matrix(_Converted):
         super().__init__(csr, load_library().vclgbMatrixToHyb, float(csr_threshold))
 
 
+class coordinate_matrix(_Converted):
+    """viennacl::coordinate_matrix<T, 128> built on the GPU from a
+    compressed_matrix: interleaved (row, col) pairs, values, group boundaries."""
+    fmt = COO
+
+    def __init__(self, csr):
+        super().__init__(csr, load_library().vclgbMatrixToCoo)
+
+
 class _Wrapped(_Matrix):
     """A format already on the device in the reference layout, wrapped without
     copying; the tensors are kept alive with the handle."""
@@ -383,6 +412,43 @@ def wrap_hyb(rows, cols, ell_width, ell_coords, ell_elems, tail_row_ptr, tail_co
     return _Wrapped(HYB, load_library().vclgbHybWrap, (co, el, trp, tci, tv), _dtype_prec(el.dtype),
                     int(rows), int(cols), int(ell_width), _ptr(co), _ptr(el), _ptr(trp), _ptr(tci),
                     _ptr(tv), int(tv.numel()), be=be)
+
+
+def wrap_coordinate(rows, cols, nnz, coords, elems, be=None):
+    """coordinate_matrix<T, A> from its handle12 (interleaved (row, col)
+    pairs, row-sorted) and handle buffers."""
+    co, el = _u32_dev(coords), elems
+    return _Wrapped(COO, load_library().vclgbCooWrap, (co, el), _dtype_prec(el.dtype), int(rows),
+                    int(cols), int(nnz), _ptr(co), _ptr(el), be=be)
+
+
+class _Loaded(compressed_matrix):
+    """A compressed_matrix whose device arrays the library owns (file reader)."""
+
+    def __init__(self, h, be):
+        _Matrix.__init__(self)
+        self.be, self.h = be, h
+
+
+def read_matrix_market_file(path, index_base=1, dtype=None, be=None):
+    """io::read_matrix_market_file: returns (compressed_matrix, lines read).
+    Raises VclgbError (INVALID_ARGUMENT, the cause in the message) where the
+    reference prints an error and returns 0."""
+    torch = _torch()
+    be = be or backend()
+    h = _P()
+    lines = _U64()
+    prec = _dtype_prec(dtype or torch.float64)
+    be.check(be.lib.vclgbReadMatrixMarket(be.h, os.fsencode(path), int(index_base), prec,
+                                          ctypes.byref(h), ctypes.byref(lines)))
+    return _Loaded(h, be), int(lines.value)
+
+
+def write_matrix_market_file(A, path, index_base=1, digits=0):
+    """io::write_matrix_market_file for a compressed_matrix (digits 0 = the
+    reference's 6 significant digits)."""
+    A.be.check(A.be.lib.vclgbWriteMatrixMarket(A.be.h, A.h, os.fsencode(path), int(index_base),
+                                               int(digits)))
 
 
 def prod(A, x, alpha=1.0, y=None, beta=0.0, x_start=0, x_stride=1, y_start=0, y_stride=1,
@@ -522,6 +588,24 @@ class jacobi_precond(_Precond):
 
     def __init__(self, A, tag=None):
         super().__init__(A, load_library().vclgbJacobiCreate)
+
+
+class row_scaling_tag:
+    """row_scaling_tag(p): 0 = max norm, 1 = sum norm, 2 = Euclidean norm of each row."""
+
+    def __init__(self, p=2):
+        self.p = int(p)
+
+    def norm(self):
+        return self.p
+
+
+class row_scaling(_Precond):
+    """row_scaling<compressed_matrix>(A, row_scaling_tag(p)): divides by row norms."""
+
+    def __init__(self, A, tag=None):
+        super().__init__(A, load_library().vclgbRowScalingCreate,
+                         (tag or row_scaling_tag()).norm())
 
 
 class ilu0_precond(_Precond):
