@@ -173,6 +173,25 @@ VCLGB_API vclgbStatus vclgbReadMatrixMarket(vclgbBackend be, const char *path, i
  * default stream precision (17 writes values that read back exactly). */
 VCLGB_API vclgbStatus vclgbWriteMatrixMarket(vclgbBackend be, vclgbMatrix A, const char *path,
                                              int64_t index_base, int digits);
+/* viennacl::reorder(matrix, cuthill_mckee_tag()) (misc/cuthill_mckee.hpp:366-421)
+ * or, advanced != 0, reorder(matrix, advanced_cuthill_mckee_tag(a, gmax))
+ * (misc/cuthill_mckee.hpp:429-605) on the pattern of a square CSR matrix, its
+ * rows read in ascending column order as the reference's host maps hold them.
+ * Writes d_perm[i] = new label of node i (rows device array), identical to
+ * the reference's result.  The ordering itself is a sequential search and
+ * runs on the host. */
+VCLGB_API vclgbStatus vclgbCuthillMcKee(vclgbBackend be, vclgbMatrix A, int advanced,
+                                        double starting_node_param, uint64_t max_root_nodes,
+                                        uint32_t *d_perm);
+/* B = P A P^T on the device: B(perm[i], perm[j]) = A(i, j), columns ascending
+ * in every row of B; the result owns its arrays.  A perm that is not a
+ * permutation of 0..rows-1 returns VCLGB_INVALID_ARGUMENT.  (The reference
+ * leaves applying its permutation to the caller.) */
+VCLGB_API vclgbStatus vclgbCsrPermute(vclgbBackend be, vclgbMatrix A, const uint32_t *d_perm,
+                                      vclgbMatrix *out);
+/* max over rows of (largest - smallest column index) -- the bandwidth measure
+ * of misc/cuthill_mckee.hpp:46-76 for a fully numbered matrix. */
+VCLGB_API vclgbStatus vclgbCsrBandwidth(vclgbBackend be, vclgbMatrix A, uint32_t *bandwidth);
 /* FP32 copy of a matrix (same format and pattern), as mixed_precision_cg.hpp:128-137
  * builds for its inner iterations. */
 VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend be, vclgbMatrix m, vclgbMatrix *out);

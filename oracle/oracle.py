@@ -455,3 +455,100 @@ def read_matrix_market(path, index_base=1):
     ci = np.array([c for _, c in keys], np.uint32)
     v = np.array([A[k] for k in keys], np.float64)
     return linenum, rows, cols, rp, ci, v
+
+
+# ---- misc/cuthill_mckee.hpp, restated in Python (small matrices) ------------
+# Each node's unnumbered neighbours are ordered by degree with a stable sort;
+# the reference's std::sort agrees with that whenever a node has at most 16
+# such neighbours (its insertion-sort range), which holds for the stencil and
+# banded test matrices used here.
+def _cm_component(rp, ci, queue, done, perm, nxt):
+    from collections import deque
+    q = deque(queue)
+    while q:
+        node = q.popleft()
+        if done[node]:
+            continue
+        perm[node] = nxt
+        nxt += 1
+        done[node] = True
+        nb = [int(c) for c in ci[rp[node]:rp[node + 1]] if not done[c]]
+        nb.sort(key=lambda c: rp[c + 1] - rp[c])
+        q.extend(nb)
+    return nxt
+
+
+def cuthill_mckee(rp, ci, advanced=False, a=0.0, gmax=1):
+    """reorder(matrix, cuthill_mckee_tag / advanced_cuthill_mckee_tag(a, gmax)):
+    perm[i] = new label of node i (cuthill_mckee.hpp:366-421, 472-605)."""
+    from collections import deque
+    from itertools import combinations
+    rp = np.asarray(rp, np.int64)
+    ci = np.asarray(ci, np.int64)
+    n = len(rp) - 1
+    deg = np.diff(rp)
+    perm = [0] * n
+    done = [False] * n
+    nxt = 0
+    if not advanced:
+        while nxt < n:
+            root, found = 0, False
+            for i in range(n):
+                if done[i]:
+                    continue
+                if deg[i] == 1:
+                    perm[i] = nxt
+                    done[i] = True
+                    nxt += 1
+                    continue
+                if not found or deg[i] < deg[root]:
+                    root, found = i, True
+            if not found:
+                break
+            nxt = _cm_component(rp, ci, [root], done, perm, nxt)
+        return np.array(perm, np.uint32)
+
+    def bw_of(done, perm):
+        bw = 0
+        for i in range(n):
+            if not done[i]:
+                continue
+            cols = [perm[c] for c in ci[rp[i]:rp[i + 1]] if done[c]]
+            if cols and max(cols) > min(cols):
+                bw = max(bw, max(cols) - min(cols))
+        return bw
+    while nxt < n:
+        start = next(i for i in range(n) if not done[i])
+        comp, seen, q = [], [False] * n, deque([start])
+        while q:
+            v = q.popleft()
+            if seen[v]:
+                continue
+            comp.append(v)
+            seen[v] = True
+            q.extend(int(c) for c in ci[rp[v]:rp[v + 1]] if c != v and not seen[c])
+        dmin, dmax = min(deg[comp]), max(deg[comp])
+        da = dmin + int(a * float(dmax - dmin))
+        roots = [v for v in comp if deg[v] <= da]
+        done0, perm0, nxt0 = list(done), list(perm), nxt
+        best = None
+        bw_best = 0
+        for g in range(1, (len(roots) if gmax == 0 else min(gmax, len(roots))) + 1):
+            for comb in combinations(range(len(roots)), g):
+                d, p = list(done0), list(perm0)
+                nxt = _cm_component(rp, ci, [roots[c] for c in comb], d, p, nxt0)
+                bw = bw_of(d, p)
+                if bw_best == 0 or bw < bw_best:
+                    best, bw_best = (p, d), bw
+        perm, done = list(best[0]), list(best[1])
+    return np.array(perm, np.uint32)
+
+
+def bandwidth(rp, ci):
+    """max over rows of (largest - smallest column)."""
+    bw = 0
+    for i in range(len(rp) - 1):
+        c = ci[rp[i]:rp[i + 1]]
+        if len(c):
+            bw = max(bw, int(c.max()) - int(c.min()))
+    return bw

@@ -33,6 +33,7 @@
 #include "viennacl/linalg/prod.hpp"
 #include "viennacl/linalg/row_scaling.hpp"
 #include "viennacl/io/matrix_market.hpp"
+#include "viennacl/misc/cuthill_mckee.hpp"
 #include "viennacl/sliced_ell_matrix.hpp"
 #include "viennacl/tools/adapter.hpp"
 #include "viennacl/vector.hpp"
@@ -404,6 +405,22 @@ int main(int argc, char **argv) {
       std::vector<double> dh = from_vcl(d);
       save("norm" + std::to_string(p) + ".f64", dh.data(), n);
     }
+  } else if (cmd == "cm") {  // args: advanced a gmax -> perm.u32, bw.u32 (before, after)
+    std::vector<std::map<unsigned, double> > S = to_maps<double>(A);
+    int advanced = std::atoi(argv[3]);
+    std::vector<unsigned> perm;
+    if (advanced)
+      perm = viennacl::reorder(S, viennacl::advanced_cuthill_mckee_tag(
+                                      std::atof(argv[4]), static_cast<std::size_t>(std::atol(argv[5]))));
+    else
+      perm = viennacl::reorder(S, viennacl::cuthill_mckee_tag());
+    std::vector<bool> all(n, true);
+    std::vector<unsigned> ident(n);
+    for (size_t i = 0; i < n; ++i) ident[i] = static_cast<unsigned>(i);
+    unsigned bw[2] = {viennacl::detail::calc_reordered_bw(S, all, ident),
+                      viennacl::detail::calc_reordered_bw(S, all, perm)};
+    save("perm.u32", perm.data(), n);
+    save("bw.u32", bw, 2);
   } else if (cmd == "jacobi_diag") {  // -> diag.f64
     viennacl::compressed_matrix<double> M;
     fill_matrix(A, M);

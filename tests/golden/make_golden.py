@@ -5,7 +5,8 @@ inputs next to the reference outputs, so the tests need neither the reference
 tree nor a particular numpy random stream.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(python tests/golden/make_golden.py coo | row_scaling | matrix_market  writes only
+(python tests/golden/make_golden.py coo | row_scaling | matrix_market | cuthill_mckee
+ writes only
 that fixture; matrix_market also writes the input files under tests/golden/mm/)
 GMRES fixtures are produced with OMP_NUM_THREADS=1 (the host stage-1 kernel's
 result depends on the thread count).
@@ -141,6 +142,7 @@ def main():
     coo_fixture()
     row_scaling_fixture()
     mm_fixture()
+    cm_fixture()
 
 
 def coo_fixture():
@@ -271,6 +273,56 @@ def mm_fixture():
     save("matrix_market.npz", **res)
 
 
+
+def _sym_permute(rp, ci, v, p):
+    """B(p[i], p[j]) = A(i, j) as CSR with ascending columns (numpy)."""
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    r2, c2 = p[rows], p[ci.astype(np.int64)]
+    order = np.lexsort((c2, r2))
+    rp2 = np.zeros(n + 1, np.int64)
+    np.add.at(rp2, r2 + 1, 1)
+    return np.cumsum(rp2).astype(np.uint32), c2[order].astype(np.uint32), v[order]
+
+
+def cm_fixture():
+    """Cuthill-McKee: a 2D Laplacian with scrambled numbering (two copies, so
+    there are two components) plus isolated nodes, and a convection-diffusion
+    matrix; permutations from both tags and the bandwidths before and after."""
+    rng = np.random.default_rng(41)
+    rp, ci, v = gen.laplace2d(24, 18)
+    n1 = len(rp) - 1
+    # block diagonal: Laplacian, Laplacian, 5 diagonal-only rows
+    blocks = [(rp, ci, v, 0), (rp, ci, v, n1)]
+    rows_r, rows_c, rows_v = [], [], []
+    for brp, bci, bv, off in blocks:
+        r = np.repeat(np.arange(n1), np.diff(brp.astype(np.int64))) + off
+        rows_r.append(r)
+        rows_c.append(bci.astype(np.int64) + off)
+        rows_v.append(bv)
+    iso = np.arange(2 * n1, 2 * n1 + 5)
+    rows_r.append(iso)
+    rows_c.append(iso)
+    rows_v.append(np.full(5, 2.0))
+    r, c, vv = np.concatenate(rows_r), np.concatenate(rows_c), np.concatenate(rows_v)
+    n = 2 * n1 + 5
+    order = np.lexsort((c, r))
+    brp = np.zeros(n + 1, np.int64)
+    np.add.at(brp, r + 1, 1)
+    brp = np.cumsum(brp).astype(np.uint32)
+    bci, bv = c[order].astype(np.uint32), vv[order]
+    rp, ci, v = _sym_permute(brp, bci, bv, rng.permutation(n))
+    res = {}
+    for key, args in (("cm", (0, 0, 0)), ("acm_a0_g1", (1, 0.0, 1)), ("acm_a05_g2", (1, 0.5, 2))):
+        out = oracle.run_ref("cm", rp, ci, v, args=args)
+        res["perm_" + key], res["bw_" + key] = out["perm"], out["bw"]
+    cp, cc, cv = gen.convdiff2d(17, 23, peclet=5.0, shift=0.2)
+    cp, cc, cv = _sym_permute(cp, cc, cv, np.random.default_rng(42).permutation(len(cp) - 1))
+    out = oracle.run_ref("cm", cp, cc, cv, args=(0, 0, 0))
+    save("cuthill_mckee.npz", rp=rp, ci=ci, v=v, cp=cp, cc=cc, cv=cv, perm_cd=out["perm"],
+         bw_cd=out["bw"], **res)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["coo"]:
         coo_fixture()
@@ -278,5 +330,7 @@ if __name__ == "__main__":
         row_scaling_fixture()
     elif sys.argv[1:] == ["matrix_market"]:
         mm_fixture()
+    elif sys.argv[1:] == ["cuthill_mckee"]:
+        cm_fixture()
     else:
         main()

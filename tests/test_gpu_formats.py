@@ -300,3 +300,73 @@ def test_coo_in_the_solvers(V):
         assert rel_err(x2, x1) < 1e-7
         if name == "cg":  # pipelined BiCGStab returns before its last update
             assert oracle.rel_residual(rp, ci, v, x2, b) < 1e-9
+
+
+def _sym_permute_np(rp, ci, v, p):
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    r2, c2 = p[rows], p[ci.astype(np.int64)]
+    order = np.lexsort((c2, r2))
+    rp2 = np.zeros(n + 1, np.int64)
+    np.add.at(rp2, r2 + 1, 1)
+    return np.cumsum(rp2).astype(np.uint32), c2[order].astype(np.uint32), v[order]
+
+
+@pytest.mark.parametrize("key,tag", [("cm", None), ("acm_a0_g1", (0.0, 1)), ("acm_a05_g2", (0.5, 2))])
+def test_cuthill_mckee_golden(V, golden, key, tag):
+    # the reference's permutation exactly; P A P^T on the device equals the
+    # host-built one; its bandwidth is the reference's
+    import torch
+    d = golden("cuthill_mckee.npz")
+    rp, ci, v = d["rp"], d["ci"], d["v"]
+    A = V.compressed_matrix(rp, ci, v)
+    t = V.cuthill_mckee_tag() if tag is None else V.advanced_cuthill_mckee_tag(*tag)
+    perm = V.reorder(A, t).cpu().numpy().view(np.uint32)
+    assert np.array_equal(perm, d["perm_" + key])
+    B = V.permute(A, perm)
+    n = len(rp) - 1
+    inf = B.info()
+    brp = B.export(0, n + 1, torch.int32).cpu().numpy().view(np.uint32)
+    bci = B.export(1, inf.nnz, torch.int32).cpu().numpy().view(np.uint32)
+    bv = B.export(2, inf.nnz, torch.float64).cpu().numpy()
+    erp, eci, ev = _sym_permute_np(rp, ci, v, perm.astype(np.int64))
+    assert np.array_equal(brp, erp) and np.array_equal(bci, eci) and np.array_equal(bv, ev)
+    assert V.bandwidth(A) == int(d["bw_" + key][0]) and V.bandwidth(B) == int(d["bw_" + key][1])
+    # B (P x) = P (A x)
+    x = np.random.default_rng(3).uniform(-1, 1, n)
+    px = np.empty(n)
+    px[perm] = x
+    y = V.prod(A, x).cpu().numpy()
+    py = np.empty(n)
+    py[perm] = y
+    assert rel_err(V.prod(B, px).cpu().numpy(), py) < 1e-14
+
+
+def test_cuthill_mckee_ordering_in_an_ilu0_solve(V, golden):
+    # the reordered system is the same system: ILU0-BiCGStab on P A P^T solves
+    # A x = b (banded order: ILU0 on it drops less fill than on a scrambled one)
+    d = golden("cuthill_mckee.npz")
+    cp, cc, cv = d["cp"], d["cc"], d["cv"]
+    A = V.compressed_matrix(cp, cc, cv)
+    perm = V.reorder(A, V.cuthill_mckee_tag()).cpu().numpy().view(np.uint32)
+    assert np.array_equal(perm, d["perm_cd"])
+    B = V.permute(A, perm)
+    assert V.bandwidth(B) == int(d["bw_cd"][1]) < V.bandwidth(A)
+    n = len(cp) - 1
+    b = gen.rhs_uniform(n, 9)
+    pb = np.empty(n)
+    pb[perm] = b
+    tA, tB = V.bicgstab_tag(1e-10, 2000), V.bicgstab_tag(1e-10, 2000)
+    xa = V.solve(A, b, tA, V.ilu0_precond(A)).cpu().numpy()
+    xb = V.solve(B, pb, tB, V.ilu0_precond(B)).cpu().numpy()
+    assert tA.status() == V.SUCCESS and tB.status() == V.SUCCESS
+    assert rel_err(xb[perm], xa) < 1e-7
+    assert tB.iters() <= tA.iters()
+
+
+def test_permute_rejects_a_non_permutation(V):
+    rp, ci, v = gen.laplace2d(5, 5)
+    A = V.compressed_matrix(rp, ci, v)
+    with pytest.raises(V.VclgbError) as e:
+        V.permute(A, np.zeros(25, np.uint32))
+    assert e.value.status == V.INVALID_ARGUMENT

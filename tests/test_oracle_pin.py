@@ -97,6 +97,16 @@ def test_matrix_market_golden(golden, name, base):
     assert np.array_equal(v, d[name + "__v"])
 
 
+def test_cuthill_mckee_golden(golden):
+    # misc/cuthill_mckee.hpp: both tags, two components and isolated nodes
+    d = golden("cuthill_mckee.npz")
+    for key, args in (("cm", (False, 0.0, 0)), ("acm_a0_g1", (True, 0.0, 1)),
+                      ("acm_a05_g2", (True, 0.5, 2))):
+        assert np.array_equal(oracle.cuthill_mckee(d["rp"], d["ci"], *args), d["perm_" + key]), key
+    assert np.array_equal(oracle.cuthill_mckee(d["cp"], d["cc"]), d["perm_cd"])
+    assert oracle.bandwidth(d["rp"], d["ci"]) == int(d["bw_cm"][0])
+
+
 def test_spmv_f32_golden(golden):
     d = golden("spmv_f32_lognormal.npz")
     y = oracle.spmv_f32(d["rp"], d["ci"], d["v"].astype(np.float32), d["x"].astype(np.float32))

@@ -347,6 +347,31 @@ VCLGB_API vclgbStatus vclgbWriteMatrixMarket(vclgbBackend h, vclgbMatrix A, cons
   return guarded(be, [&]() { write_matrix_market(*be, *M(A), path, (long)index_base, digits); });
 }
 
+VCLGB_API vclgbStatus vclgbCuthillMcKee(vclgbBackend h, vclgbMatrix A, int advanced,
+                                        double starting_node_param, uint64_t max_root_nodes,
+                                        uint32_t *d_perm) {
+  if (!h || !A) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    cuthill_mckee_perm(*be, *M(A), advanced != 0, starting_node_param, max_root_nodes, d_perm);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbCsrPermute(vclgbBackend h, vclgbMatrix A, const uint32_t *d_perm,
+                                      vclgbMatrix *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    *out = reinterpret_cast<vclgbMatrix>(csr_permute(*be, *M(A), d_perm).release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbCsrBandwidth(vclgbBackend h, vclgbMatrix A, uint32_t *bandwidth) {
+  if (!h || !A || !bandwidth) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { *bandwidth = csr_bandwidth(*be, *M(A)); });
+}
+
 VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m) {
   if (!m || !*m) return VCLGB_INVALID_ARGUMENT;
   Matrix *mm = M(*m);

@@ -27,6 +27,12 @@ std::unique_ptr<Matrix> read_matrix_market(Backend &be, const char *path, long i
 void write_matrix_market(Backend &be, const Matrix &m, const char *path, long index_base,
                          int digits);
 
+// bandwidth reduction (reorder.cu)
+void cuthill_mckee_perm(Backend &be, const Matrix &A, bool advanced, double a, uint64_t gmax,
+                        uint32_t *d_perm);
+std::unique_ptr<Matrix> csr_permute(Backend &be, const Matrix &A, const uint32_t *d_perm);
+uint32_t csr_bandwidth(Backend &be, const Matrix &A);
+
 // preconditioners (precond.cu)
 std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A);
 std::unique_ptr<Precond> row_scaling_create(Backend &be, const Matrix &A, uint32_t norm);

@@ -104,6 +104,9 @@ SIGNATURES = {
     "vclgbReadMatrixMarket": (_I32, [_P, ctypes.c_char_p, _I64, _I32, ctypes.POINTER(_P),
                                      ctypes.POINTER(_U64)]),
     "vclgbWriteMatrixMarket": (_I32, [_P, _P, ctypes.c_char_p, _I64, _I32]),
+    "vclgbCuthillMcKee": (_I32, [_P, _P, _I32, _D, _U64, _P]),
+    "vclgbCsrPermute": (_I32, [_P, _P, _P, ctypes.POINTER(_P)]),
+    "vclgbCsrBandwidth": (_I32, [_P, _P, ctypes.POINTER(_U32)]),
     "vclgbMatrixDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbMatrixGetInfo": (_I32, [_P, ctypes.POINTER(MatrixInfo)]),
     "vclgbMatrixExport": (_I32, [_P, _P, _I32, _P]),
@@ -449,6 +452,44 @@ def write_matrix_market_file(A, path, index_base=1, digits=0):
     reference's 6 significant digits)."""
     A.be.check(A.be.lib.vclgbWriteMatrixMarket(A.be.h, A.h, os.fsencode(path), int(index_base),
                                                int(digits)))
+
+
+class cuthill_mckee_tag:
+    """reorder(matrix, cuthill_mckee_tag())."""
+    advanced, a, gmax = 0, 0.0, 1
+
+
+class advanced_cuthill_mckee_tag:
+    """advanced_cuthill_mckee_tag(a, gmax): root candidates of degree at most
+    deg_min + a (deg_max - deg_min), up to gmax roots at once."""
+    advanced = 1
+
+    def __init__(self, a=0.0, gmax=1):
+        self.a, self.gmax = float(a), int(gmax)
+
+
+def reorder(A, tag):
+    """viennacl::reorder on a compressed_matrix: device uint32 tensor with
+    perm[i] = new label of node i."""
+    torch = _torch()
+    perm = torch.empty(max(A.size1(), 1), dtype=torch.int32, device="cuda")
+    A.be.check(A.be.lib.vclgbCuthillMcKee(A.be.h, A.h, tag.advanced, tag.a, tag.gmax, _ptr(perm)))
+    return perm[:A.size1()]
+
+
+def permute(A, perm):
+    """P A P^T as a new compressed_matrix (B(perm[i], perm[j]) = A(i, j))."""
+    p = _u32_dev(perm)
+    h = _P()
+    A.be.check(A.be.lib.vclgbCsrPermute(A.be.h, A.h, _ptr(p), ctypes.byref(h)))
+    return _Loaded(h, A.be)
+
+
+def bandwidth(A):
+    """max over rows of (largest - smallest column index)."""
+    bw = _U32()
+    A.be.check(A.be.lib.vclgbCsrBandwidth(A.be.h, A.h, ctypes.byref(bw)))
+    return int(bw.value)
 
 
 def prod(A, x, alpha=1.0, y=None, beta=0.0, x_start=0, x_stride=1, y_start=0, y_stride=1,
