@@ -416,12 +416,26 @@ __device__ __forceinline__ bool grid_reduce(T (&v)[NV], T *partials, unsigned *c
   __syncthreads();
   if (!am_last) return false;
   __threadfence();
+  // The other blocks' partials are read at L2 (ld.global.cg: no stale L1
+  // line), four at a time: loads issued together, then added in the fixed
+  // order b = tid, tid + blockDim, ...  (volatile loads would be issued one
+  // after another, a full L2 round trip each, on the kernel's serial tail).
   T acc[NV];
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
+    const T *src = partials + (size_t)i * gridDim.x;
     T s = 0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
-      s += ((volatile T *)partials)[(size_t)i * gridDim.x + b];
+    for (unsigned b0 = threadIdx.x; b0 < gridDim.x; b0 += 4 * blockDim.x) {
+      T q[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const unsigned b = b0 + k * blockDim.x;
+        q[k] = b < gridDim.x ? __ldcg(src + b) : T(0);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (b0 + k * blockDim.x < gridDim.x) s += q[k];
+    }
     acc[i] = s;
   }
   if constexpr (WIDE) block_sum_wide<NV>(acc, smem);
