@@ -214,8 +214,12 @@ __device__ __forceinline__ void pcg_check(St<T> *st, T new_ip) {
   else if (st->iters >= st->max_iters) st->done = kMaxIters;
 }
 
+// Jacobi: z = r / d is formed once per iteration here and stored; PcgP reads
+// it back.  An FP64 division is a software sequence of about ten FP64-pipe
+// instructions on GB300, so dividing again in PcgP cost more than the 8 bytes
+// per row of reading z (the write of z replaces PcgP's reads of r and d).
 template <typename T>
-struct PcgUpdate {  // x += a p; r -= a tmp; [z = r/d]; <r,z> (Jacobi) / z = r (generic)
+struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (generic)
   static constexpr int NDOT = 1;
   T *x, *r, *z; const T *p, *tmp, *dg; St<T> *st;
   bool jacobi;
@@ -227,8 +231,13 @@ struct PcgUpdate {  // x += a p; r -= a tmp; [z = r/d]; <r,z> (Jacobi) / z = r (
     x[i] += s.a * vp;
     T vr = r[i] - s.a * tmp[i];
     r[i] = vr;
-    if (jacobi) d[0] += vr * (vr / dg[i]);
-    else z[i] = vr;
+    if (jacobi) {
+      const T zi = vr / dg[i];
+      z[i] = zi;
+      d[0] += vr * zi;
+    } else {
+      z[i] = vr;
+    }
   }
   __device__ void finalize(const T (&s)[1]) const {
     if (jacobi) pcg_check(st, s[0]);
@@ -246,17 +255,13 @@ struct PcgDot {  // generic preconditioner: <r,z> after z = M^-1 r
 };
 
 template <typename T>
-struct PcgP {  // p = z + beta p, z = r/d (Jacobi) or z (generic)
+struct PcgP {  // p = z + beta p (z = r/d stored by PcgUpdate for Jacobi)
   static constexpr int NDOT = 0;
-  T *p; const T *r, *z, *dg; St<T> *st;
-  bool jacobi;
+  T *p; const T *z; St<T> *st;
   struct S { T b; };
   __device__ bool skip() const { return st->done != kRunning; }
   __device__ S load() const { return {st->beta}; }
-  __device__ void apply(size_t i, S s, T (&)[1]) const {
-    T zi = jacobi ? r[i] / dg[i] : z[i];
-    p[i] = zi + s.b * p[i];
-  }
+  __device__ void apply(size_t i, S s, T (&)[1]) const { p[i] = z[i] + s.b * p[i]; }
   __device__ void finalize(const T (&)[1]) const {}
 };
 
@@ -932,7 +937,7 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
         precond_apply(be, *P, z, done);
         vec_pass<T>(be, n, PcgDot<T>{r, z, st}, red);
       }
-      vec_pass<T>(be, n, PcgP<T>{p, r, z, dg, st, jac}, red);
+      vec_pass<T>(be, n, PcgP<T>{p, z, st}, red);
     });
   }
   set_tag_outputs(be, st, tag);

@@ -174,7 +174,7 @@ __device__ __forceinline__ void csr_rows_block(const CsrView<T> &A, const T *__r
 // most about twice the mean) run without any row classification: LANES
 // threads per row, MPL entries per lane and round, rows in order.
 template <int LANES, int MPL, typename T, class E>
-__global__ void __launch_bounds__(kSpmvThreads, (E::NDOT > 0 && E::NDOT <= 2) ? 8 : 1)
+__global__ void __launch_bounds__(kSpmvThreads, (E::NDOT > 0 && E::NDOT <= 2) ? 8 : 0)
     csr_fixed_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc, E epi,
                      T *partials, unsigned *counter) {
   if (epi.skip()) return;
