@@ -359,10 +359,13 @@ def secondaries(V, torch, peak, args):
     b = gen.rhs_uniform(n, 1)
     bd = torch.tensor(b, device="cuda")
     s = {}
-    for name, tag in (("bicgstab", V.bicgstab_tag(1e-10, 3000)), ("gmres30", V.gmres_tag(1e-10, 3000, 30))):
+    PJ = V.jacobi_precond(A)
+    for name, tag, P in (("bicgstab", V.bicgstab_tag(1e-10, 3000), None),
+                         ("gmres30", V.gmres_tag(1e-10, 3000, 30), None),
+                         ("bicgstab_jacobi", V.bicgstab_tag(1e-10, 3000), PJ)):
         torch.cuda.synchronize()
         t0 = time.time()
-        xx = V.solve(A, bd, tag)
+        xx = V.solve(A, bd, tag, P)
         torch.cuda.synchronize()
         s[name] = {"s": time.time() - t0, "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
                    "error_estimate": tag.error(),

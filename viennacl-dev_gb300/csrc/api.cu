@@ -102,6 +102,8 @@ VCLGB_API vclgbStatus vclgbBackendDestroy(vclgbBackend *h) {
   cudaStreamSynchronize(be->stream);
   if (be->host_flags) cudaFreeHost(be->host_flags);
   for (cudaEvent_t e : be->tev) cudaEventDestroy(e);
+  for (cudaEvent_t e : be->poll_ev)
+    if (e) cudaEventDestroy(e);
   if (be->own_stream) cudaStreamDestroy(be->stream);
   delete be;
   *h = nullptr;

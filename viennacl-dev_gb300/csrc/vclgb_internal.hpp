@@ -99,8 +99,10 @@ struct Backend {
   bool own_stream = false;
   std::string last_error;
   uint64_t launches = 0;
-  // pinned host word the solvers poll (convergence / status)
+  // pinned host words the solvers poll (convergence / status), two chunks
+  // in flight; the events mark when each status copy has landed
   int *host_flags = nullptr;
+  cudaEvent_t poll_ev[2] = {nullptr, nullptr};
   // persistent reduction scratch for the vector reductions
   DevBuf red_partials;
   DevBuf red_counter;

@@ -92,22 +92,50 @@ void run_iterations(Backend &be, const int *d_done, uint32_t max_chunks_hint, ui
   }
   uint64_t chunks = 0;
   const uint64_t limit = (uint64_t)max_chunks_hint + 4;
-  for (;;) {
+  // One chunk is kept in flight ahead of the status check: chunk k+1 is
+  // enqueued before the host waits for chunk k's status word, so the GPU
+  // never idles while the host polls.  The chunk enqueued after convergence
+  // costs only launches (its kernels return at their first instruction).
+  // With kernel timing on, chunks run one at a time (timing_collect waits
+  // for the stream and reads each replay's event pairs).
+  const bool ahead = !be.timing;
+  if (ahead && !be.poll_ev[0]) {
+    for (int k = 0; k < 2; ++k)
+      VCLGB_CUDA(cudaEventCreateWithFlags(&be.poll_ev[k], cudaEventDisableTiming));
+  }
+  auto enqueue = [&](uint64_t k) {
     if (exec) {
       VCLGB_CUDA(cudaGraphLaunch(exec, be.stream));
       be.launches += per_chunk;
     } else {
       for (uint32_t i = 0; i < check_every; ++i) one_iteration();
     }
-    VCLGB_CUDA(cudaMemcpyAsync(be.host_flags, d_done, sizeof(int), cudaMemcpyDeviceToHost,
-                               be.stream));
+    VCLGB_CUDA(cudaMemcpyAsync(be.host_flags + (k & 1), d_done, sizeof(int),
+                               cudaMemcpyDeviceToHost, be.stream));
+    if (ahead) VCLGB_CUDA(cudaEventRecord(be.poll_ev[k & 1], be.stream));
+  };
+  auto fail = [&]() {
+    if (exec) cudaGraphExecDestroy(exec);
+    throw Error(VCLGB_TIMEOUT, "solver did not report completion within its iteration bound");
+  };
+  if (ahead) {
+    enqueue(0);
+    for (uint64_t k = 0;; ++k) {
+      enqueue(k + 1);
+      VCLGB_CUDA(cudaEventSynchronize(be.poll_ev[k & 1]));
+      ++chunks;
+      if (be.host_flags[k & 1] != kRunning) break;
+      if (chunks > limit) fail();
+    }
     VCLGB_CUDA(cudaStreamSynchronize(be.stream));
-    timing_collect(be, exec != nullptr);  // graph events are replayed again
-    ++chunks;
-    if (*be.host_flags != kRunning) break;
-    if (chunks > limit) {
-      if (exec) cudaGraphExecDestroy(exec);
-      throw Error(VCLGB_TIMEOUT, "solver did not report completion within its iteration bound");
+  } else {
+    for (uint64_t k = 0;; ++k) {
+      enqueue(k);
+      VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+      timing_collect(be, exec != nullptr);  // graph events are replayed again
+      ++chunks;
+      if (be.host_flags[k & 1] != kRunning) break;
+      if (chunks > limit) fail();
     }
   }
   if (exec) VCLGB_CUDA(cudaGraphExecDestroy(exec));
