@@ -90,6 +90,33 @@ def test_refined_cg_reaches_fp64_residual(V):
     assert abs(tag.iters() - inner) <= 0.15 * inner + 5
 
 
+def test_refined_cg_banded_and_scrambled(V):
+    # the inner copy is stored by diagonal for a banded matrix and stays CSR
+    # when a scrambled numbering spreads the entries over many diagonals; both
+    # reach the FP64 tolerance and agree
+    rp, ci, v = gen.laplace2d(60, 50)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 8)
+    p = np.random.default_rng(8).permutation(n)
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    r2, c2 = p[rows], p[ci.astype(np.int64)]
+    order = np.lexsort((c2, r2))
+    rp2 = np.zeros(n + 1, np.int64)
+    np.add.at(rp2, r2 + 1, 1)
+    rp2, ci2, v2 = np.cumsum(rp2).astype(np.uint32), c2[order].astype(np.uint32), v[order]
+    b2 = np.empty(n)
+    b2[p] = b
+    xs = []
+    for (R, C, W, B) in ((rp, ci, v, b), (rp2, ci2, v2, b2)):
+        A = V.compressed_matrix(R, C, W)
+        tag = V.refined_cg_tag(1e-10, 100000, 1e-4)
+        x = _np(V.solve(A, B, tag))
+        assert tag.status() == V.SUCCESS
+        assert oracle.rel_residual(R, C, W, x, B) < 1e-10
+        xs.append(x)
+    assert rel_err(xs[1][p], xs[0]) < 1e-8
+
+
 def test_reference_cpu_case_laplace256(V):
     # 256x256 Laplacian (h = 1/257), b ~ U[-1,1] seed 0, Jacobi-PCG to 1e-8, max 2000
     rp, ci, v = gen.laplace2d(256, 256, scaled=True)

@@ -683,6 +683,110 @@ void coo_validate(Backend &be, const Matrix &m) {
   if (h & 4) throw Error(VCLGB_INVALID_MATRIX, "COO entries are not sorted by row");
 }
 
+// ---------------------------------------------------------------------------
+// DIA (internal): diagonal offsets by a hash set in global memory, then the
+// values by diagonal
+// ---------------------------------------------------------------------------
+constexpr int kDiaSlots = 64;
+constexpr int kDiaEmpty = INT32_MIN;
+
+__global__ void dia_offsets_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                   const uint32_t *__restrict__ ci, int *table, unsigned *count,
+                                   unsigned *overflow) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    if (*(volatile unsigned *)overflow) return;
+    for (uint32_t k = rp[r]; k < rp[r + 1]; ++k) {
+      const int64_t d = (int64_t)ci[k] - (int64_t)r;
+      if (d <= INT32_MIN || d > INT32_MAX) {
+        atomicOr(overflow, 1u);
+        return;
+      }
+      const int off = (int)d;
+      unsigned h = ((unsigned)off * 2654435761u) >> 26;  // 64 slots
+      for (int probe = 0; probe < kDiaSlots; ++probe, h = (h + 1) & (kDiaSlots - 1)) {
+        const int seen = *(volatile int *)(table + h);
+        if (seen == off) break;
+        if (seen == kDiaEmpty) {
+          const int prev = atomicCAS(table + h, kDiaEmpty, off);
+          if (prev == kDiaEmpty) {
+            if (atomicAdd(count, 1u) >= (unsigned)kMaxDiag) atomicOr(overflow, 1u);
+            break;
+          }
+          if (prev == off) break;
+        }
+      }
+    }
+  }
+}
+
+template <typename V>
+__global__ void dia_fill_kernel(uint32_t rows, const uint32_t *__restrict__ rp,
+                                const uint32_t *__restrict__ ci, const V *__restrict__ v,
+                                DiaOffsets offs, V *vals) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    for (uint32_t k = rp[r]; k < rp[r + 1]; ++k) {
+      const int off = (int)((int64_t)ci[k] - (int64_t)r);
+      int d = 0;
+      while (d < offs.n && offs.off[d] != off) ++d;
+      if (d < offs.n) vals[(size_t)d * rows + r] += v[k];  // repeated entries add up
+    }
+  }
+}
+
+std::unique_ptr<Matrix> try_convert_dia(Backend &be, const Matrix &csr, double max_fill) {
+  require(csr.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "conversion source must be CSR");
+  if (csr.rows == 0 || csr.nnz == 0) return nullptr;
+  if (csr.rows >= (1u << 31) || csr.cols >= (1u << 31)) return nullptr;  // 32-bit indexing
+  DevBuf table(kDiaSlots * sizeof(int), be.stream), flags(2 * sizeof(unsigned), be.stream);
+  std::vector<int> h(kDiaSlots, kDiaEmpty);
+  VCLGB_CUDA(cudaMemcpyAsync(table.ptr, h.data(), kDiaSlots * sizeof(int),
+                             cudaMemcpyHostToDevice, be.stream));
+  VCLGB_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, be.stream));
+  int g = waves_grid(be, 256, 8, csr.rows);
+  dia_offsets_kernel<<<g, 256, 0, be.stream>>>(csr.rows, csr.row_ptr, csr.col_idx,
+                                               table.as<int>(), flags.as<unsigned>(),
+                                               flags.as<unsigned>() + 1);
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  unsigned hf[2] = {0, 0};
+  VCLGB_CUDA(cudaMemcpyAsync(h.data(), table.ptr, kDiaSlots * sizeof(int),
+                             cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaMemcpyAsync(hf, flags.ptr, sizeof(hf), cudaMemcpyDeviceToHost, be.stream));
+  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  if (hf[1] || hf[0] > (unsigned)kMaxDiag) return nullptr;
+  std::vector<int> offs;
+  for (int x : h)
+    if (x != kDiaEmpty) offs.push_back(x);
+  std::sort(offs.begin(), offs.end());
+  const double stored = (double)offs.size() * csr.rows;
+  if (stored > max_fill * (double)csr.nnz || stored >= 4294967296.0) return nullptr;
+  auto out = std::make_unique<Matrix>();
+  copy_header(csr, *out, kFormatDia);
+  out->dia_ndiag = (uint32_t)offs.size();
+  DiaOffsets o;
+  o.n = (int)offs.size();
+  for (int d = 0; d < kMaxDiag; ++d) {
+    o.off[d] = d < o.n ? offs[d] : 0;
+    out->dia_off[d] = o.off[d];
+  }
+  const size_t vs = csr.vsize();
+  out->dia_vals.alloc((size_t)o.n * csr.rows * vs, be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(out->dia_vals.ptr, 0, out->dia_vals.bytes, be.stream));
+  if (vs == 8)
+    dia_fill_kernel<double><<<g, 256, 0, be.stream>>>(csr.rows, csr.row_ptr, csr.col_idx,
+                                                      static_cast<const double *>(csr.values), o,
+                                                      out->dia_vals.as<double>());
+  else
+    dia_fill_kernel<float><<<g, 256, 0, be.stream>>>(csr.rows, csr.row_ptr, csr.col_idx,
+                                                     static_cast<const float *>(csr.values), o,
+                                                     out->dia_vals.as<float>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  return out;
+}
+
 __global__ void tail_rows_kernel(uint32_t rows, const uint32_t *__restrict__ trp, uint32_t *trow) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
        r += (size_t)gridDim.x * blockDim.x)

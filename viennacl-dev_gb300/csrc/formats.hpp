@@ -11,6 +11,9 @@ void sell_wide_chunks(Backend &be, Matrix &m);
 std::unique_ptr<Matrix> convert_hyb(Backend &be, const Matrix &csr, double threshold);
 std::unique_ptr<Matrix> convert_f32(Backend &be, const Matrix &m);
 std::unique_ptr<Matrix> convert_coo(Backend &be, const Matrix &csr);
+// DIA form of a CSR matrix whose entries lie on at most kMaxDiag diagonals
+// and whose diagonals hold at most max_fill times its nonzeros; else null
+std::unique_ptr<Matrix> try_convert_dia(Backend &be, const Matrix &csr, double max_fill);
 // COO wrapped from reference arrays: checks the pairs, then derives the groups
 void coo_validate(Backend &be, const Matrix &m);
 void coo_groups(Backend &be, Matrix &m);

@@ -9,7 +9,10 @@
 //   symmetrically scaled matrix D^-1/2 A D^-1/2, so the inner solver is the
 //   two-kernel pipelined CG on a cached FP32 copy of that matrix: FP32 values
 //   and vectors halve the bytes of the memory-bound loop and no diagonal is
-//   read per iteration.  FP64 is used only for r = b - A x, x += d and ||r||.
+//   read per iteration.  When the matrix lies on at most 16 diagonals
+//   (stencils) the copy is stored by diagonal (DIA, no column indices), which
+//   halves the inner product's matrix bytes again.  FP64 is used only for
+//   r = b - A x, x += d and ||r||.
 #include <algorithm>
 #include <cmath>
 
@@ -331,6 +334,13 @@ void refined_cg_solve(Backend &be, Matrix &A, const double *b, double *x, vclgbS
   if (inner_tol <= 0) inner_tol = 1e-4;
   if (max_outer == 0) max_outer = 30;
   Matrix &Ah = f32_scaled(be, A);
+  // a banded matrix (stencil) runs its inner iterations on the DIA form of the
+  // scaled copy: no column indices, 4 bytes per stored slot
+  if (!A.f32_scaled_dia_tried) {
+    A.f32_scaled_dia = try_convert_dia(be, Ah, 1.25);
+    A.f32_scaled_dia_tried = true;
+  }
+  Matrix *Ad = A.f32_scaled_dia.get();
   size_t n1 = std::max<size_t>(n, 1);
   DevBuf r(n1 * 8, be.stream), rh(n1 * 4, be.stream), y(n1 * 4, be.stream),
       part(8 * kMaxSpmvGrid * 8, be.stream), cnt(64, be.stream), sc(16, be.stream);
@@ -358,7 +368,7 @@ void refined_cg_solve(Backend &be, Matrix &A, const double *b, double *x, vclgbS
     it.tol = itol;
     it.max_iters = tag->max_iters - inner_total;
     it.check_every = tag->check_every;
-    cg_solve<float>(be, Ah, rh.as<float>(), y.as<float>(), &it, nullptr);
+    cg_solve<float>(be, Ad ? *Ad : Ah, rh.as<float>(), y.as<float>(), &it, nullptr);
     inner_total += it.iters;
     vec_pass<double>(be, n, IrUpdate{x, y.as<float>(), A.inv_sqrt_diag.as<double>(), nr}, red);
     spmv_launch<double>(be, A, x, 0, 1, EpiIrResid{r.as<double>(), b, d_sc}, red);

@@ -437,6 +437,63 @@ __global__ void __launch_bounds__(kSpmvThreads)
 }
 
 // ---------------------------------------------------------------------------
+// DIA (internal format): thread per row; diagonal d contributes
+// vals[d*rows + row] * x[row + off[d]] where that column exists, in ascending
+// column order as a column-sorted CSR row.  ND > 0: the diagonal count is a
+// compile-time constant and every value and x load of the row is issued
+// before the first multiply (bounds tests only decide for boundary rows).
+// ND == 0:
+// any count up to kMaxDiag, one diagonal at a time.  x is contiguous (the
+// inner solver's own vector).
+// ---------------------------------------------------------------------------
+template <int ND, typename T, class E>
+__global__ void __launch_bounds__(kSpmvThreads)
+    dia_kernel(uint32_t rows, uint32_t cols, DiaOffsets offs, const T *__restrict__ vals,
+               const T *__restrict__ x, E epi, T *partials, unsigned *counter) {
+  if (epi.skip()) return;
+  __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
+  T dots[DotArr<E::NDOT>::n];
+#pragma unroll
+  for (int i = 0; i < DotArr<E::NDOT>::n; ++i) dots[i] = T(0);
+  // rows [lo, hi) have every diagonal inside the matrix
+  const int64_t lo = -(int64_t)offs.off[0];
+  const int64_t hi = (int64_t)cols - offs.off[offs.n - 1];
+#pragma unroll 1
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (size_t)gridDim.x * blockDim.x) {
+    const typename E::Pre pv = epi.pre((uint32_t)r);
+    // 32-bit indices: the DIA form is built only when rows, cols < 2^31 and
+    // ndiag * rows < 2^32, so r + off cannot wrap into the valid range
+    const uint32_t r32 = (uint32_t)r;
+    T acc = T(0);
+    if constexpr (ND > 0) {
+      T v[ND], xv[ND];
+      const bool inside = (int64_t)r >= lo && (int64_t)r < hi;
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        const uint32_t c = r32 + (uint32_t)offs.off[d];
+        const bool in = inside || c < cols;
+        v[d] = in ? __ldg(vals + (d * rows + r32)) : T(0);
+        xv[d] = in ? __ldg(x + c) : T(0);
+      }
+#pragma unroll
+      for (int d = 0; d < ND; ++d) acc += v[d] * xv[d];
+    } else {
+#pragma unroll 1
+      for (int d = 0; d < offs.n; ++d) {
+        const uint32_t c = r32 + (uint32_t)offs.off[d];
+        if (c < cols) acc += __ldg(vals + (d * rows + r32)) * __ldg(x + c);
+      }
+    }
+    epi.row((uint32_t)r, acc, pv, dots);
+  }
+  if constexpr (E::NDOT > 0) {
+    T sums[E::NDOT];
+    if (grid_reduce<E::NDOT>(dots, partials, counter, smem, sums)) epi.finalize(sums);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // SELL-C-sigma: thread per stored row position; slice s, lane l; element j of
 // the position at block_start[s] + j*C + l (sliced_ell_matrix.hpp layout).
 // ---------------------------------------------------------------------------
@@ -696,7 +753,9 @@ struct Reduction {
 
 // grid of the SpMV kernels (also the number of partials per dot)
 inline int spmv_grid(const Backend &be, const Matrix &m) {
-  size_t work = m.format == VCLGB_SELL || m.format == VCLGB_ELL ? m.rows : (m.rows + 3) / 4;
+  size_t work = m.format == VCLGB_SELL || m.format == VCLGB_ELL || m.format == kFormatDia
+                    ? m.rows
+                    : (m.rows + 3) / 4;
   if (m.format == VCLGB_CSR && m.nnz / 8 > work) work = m.nnz / 8;
   return waves_grid(be, kSpmvThreads, 8, work < 1 ? 1 : work);
 }
@@ -767,6 +826,30 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
     case VCLGB_ELL:
       ell_launch<T, E>(be, grid, m, x, xs, xinc, epi, partials, red.counter);
       break;
+    case kFormatDia: {
+      // the DIA form exists only as the refined solver's FP32 inner copy
+      if constexpr (std::is_same<T, float>::value) {
+        require(xs == 0 && xinc == 1, VCLGB_UNSUPPORTED, "DIA form takes a contiguous x");
+        DiaOffsets o;
+        o.n = (int)m.dia_ndiag;
+        for (int d = 0; d < kMaxDiag; ++d) o.off[d] = m.dia_off[d];
+#define VCLGB_DIA(ND)                                                                        \
+  dia_kernel<ND, T, E><<<one_wave<dia_kernel<ND, T, E>>(be, grid, kSpmvThreads), kSpmvThreads, \
+                         0, be.stream>>>(m.rows, m.cols, o, m.dia_vals.as<T>(), x, epi,       \
+                                         partials, red.counter)
+        switch (o.n) {
+          case 3: VCLGB_DIA(3); break;
+          case 5: VCLGB_DIA(5); break;
+          case 7: VCLGB_DIA(7); break;
+          case 9: VCLGB_DIA(9); break;
+          default: VCLGB_DIA(0); break;
+        }
+#undef VCLGB_DIA
+      } else {
+        throw Error(VCLGB_UNSUPPORTED, "DIA form is an FP32 inner format");
+      }
+      break;
+    }
     case VCLGB_SELL:
       if (m.C % 32 == 0)
         sell_kernel<true, T, E><<<one_wave<sell_kernel<true, T, E>>(be, grid, kSpmvThreads),

@@ -226,6 +226,18 @@ constexpr uint32_t kSellWide = 128;
 
 struct Transposed;  // adjoint.cu: A^T and its entry map
 
+// DIA: an internal format only (no ViennaCL counterpart), the refined
+// solver's FP32 inner copy of a matrix whose entries lie on a few diagonals
+// (stencils): values of diagonal d (column = row + off[d]) at vals[d*rows + row],
+// zero where the diagonal leaves the matrix or the pattern has no entry.  No
+// column indices are stored, so the inner product reads 4 bytes per slot.
+constexpr vclgbFormat kFormatDia = static_cast<vclgbFormat>(100);
+constexpr int kMaxDiag = 16;
+struct DiaOffsets {  // kernel argument: the diagonals' column offsets, ascending
+  int n;
+  int off[kMaxDiag];
+};
+
 struct Matrix {
   vclgbFormat format = VCLGB_CSR;
   vclgbPrecision prec = VCLGB_FLOAT64;
@@ -269,8 +281,16 @@ struct Matrix {
 
   // cached FP32 copy used by the mixed-precision solvers
   std::unique_ptr<Matrix> f32_copy;
-  // cached FP32 copy of D^-1/2 A D^-1/2 and D^-1/2 (FP64) for refined CG
+  // cached FP32 copy of D^-1/2 A D^-1/2 and D^-1/2 (FP64) for refined CG,
+  // and its DIA form when the matrix lies on at most kMaxDiag diagonals
   std::unique_ptr<Matrix> f32_scaled;
+  std::unique_ptr<Matrix> f32_scaled_dia;
+  bool f32_scaled_dia_tried = false;
+
+  // DIA (kFormatDia)
+  uint32_t dia_ndiag = 0;
+  int32_t dia_off[kMaxDiag] = {};
+  DevBuf dia_vals;
   DevBuf inv_sqrt_diag;
   // cached transpose for the adjoint solve
   std::shared_ptr<Transposed> transposed;
