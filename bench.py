@@ -38,8 +38,8 @@ import vclgb_gen as gen  # noqa: E402
 METRIC = "CG solve s @1e-10 FP64 resid: mixed/batched vs plain FP64 on GPU; SpMV GB/s"
 # DRAM bytes (read + write) of one launch of the CG SpMV phase kernel on the
 # 128^3 Laplacian, from the ncu capture summarised in
-# profiles/csr_fixed_laplace3d_128.md (200,180,736 read + 12,781,056 written)
-TRAFFIC_SPMV_CG = 212961792
+# profiles/csr_fixed_laplace3d_128.md (200,200,448 read + 12,884,736 written)
+TRAFFIC_SPMV_CG = 213085184
 WORKLOAD = "3D 7-point Laplacian 128^3 (2,097,152 rows, 14,581,760 nnz), FP64 CSR, pipelined CG to 1e-10"
 
 
@@ -562,8 +562,8 @@ def run_reference(args):
 
 def profile_kernels(args):
     """Small fixed workloads for ncu captures.  laplace: a few SpMVs per format
-    on the 128^3 Laplacian (about 300 MB on the device) and one short CG
-    solve; lognormal: a few SpMVs per format on a 1M-row lognormal random
+    on the 128^3 Laplacian (about 300 MB on the device), one short CG solve and
+    a short refined solve on 96^3 diffusion; lognormal: a few SpMVs per format on a 1M-row lognormal random
     matrix (about 21M nnz, 250 MB of CSR arrays)."""
     import torch
     import vclgb as V
@@ -588,6 +588,10 @@ def profile_kernels(args):
         for _ in range(3):
             V.prod(M, x, y=y)
     V.solve(A, x, V.cg_tag(1e-10, 20))
+    # a short refined solve (FP32 inner iterations on the DIA copy) on 96^3 diffusion
+    rp2, ci2, v2, f2 = gen.diffusion3d(96)
+    A2 = V.compressed_matrix(rp2, ci2, v2)
+    V.solve(A2, f2, V.refined_cg_tag(1e-6, 60, 1e-4))
     torch.cuda.synchronize()
     print("profile workload done")
 

@@ -370,3 +370,21 @@ def test_permute_rejects_a_non_permutation(V):
     with pytest.raises(V.VclgbError) as e:
         V.permute(A, np.zeros(25, np.uint32))
     assert e.value.status == V.INVALID_ARGUMENT
+
+
+def test_coo_without_entries(V):
+    # an all-empty pattern: no stored entries, groups all zero, y = beta * y
+    import torch
+    n = 40
+    A = V.compressed_matrix(np.zeros(n + 1, np.uint32), np.zeros(0, np.uint32), np.zeros(0), n, n)
+    Co = V.coordinate_matrix(A)
+    inf = Co.info()
+    assert inf.nnz == 0 and inf.stored == 0
+    assert np.array_equal(Co.export(2, 65, torch.int32).cpu().numpy(), np.zeros(65, np.int32))
+    y0 = np.random.default_rng(1).uniform(-1, 1, n)
+    y = torch.tensor(y0, device="cuda")
+    V.prod(Co, np.ones(n), alpha=2.0, y=y, beta=-0.5)
+    assert np.array_equal(y.cpu().numpy(), -0.5 * y0)
+    y = torch.tensor(y0, device="cuda")
+    V.prod(Co, np.ones(n), y=y)
+    assert not y.cpu().numpy().any()

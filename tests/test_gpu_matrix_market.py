@@ -101,3 +101,13 @@ def test_writer_round_trip(V, tmp_path):
     C, _ = V.read_matrix_market_file(short)
     x = np.random.default_rng(1).uniform(-1, 1, 3000)
     assert rel_err(V.prod(C, x).cpu().numpy(), oracle.spmv(rp, ci, v, x)) < 1e-5
+
+
+def test_empty_matrix_file(V, tmp_path):
+    # "rows cols 0": an empty matrix (the reference reports a failure here,
+    # from its parse of the line after the size line)
+    path = str(tmp_path / "empty.mtx")
+    open(path, "w").write("%%MatrixMarket matrix coordinate real general\n% nothing\n7 5 0\n")
+    A, lines = V.read_matrix_market_file(path)
+    inf = A.info()
+    assert (inf.rows, inf.cols, inf.nnz, lines) == (7, 5, 0, 3)
