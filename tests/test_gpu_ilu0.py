@@ -46,11 +46,50 @@ def test_golden_factors_and_levels(V, golden):
     assert rel_err(z.cpu().numpy(), d["z"]) < 1e-13
 
 
-@pytest.mark.parametrize("case", ["lap3d", "diffusion2d"])
+def _scrambled(rp, ci, v, seed):
+    # P A P^T for a random P: each row's lower/upper entries then fall into
+    # several levels, so a row is updated at more than one level
+    sp = pytest.importorskip("scipy.sparse")
+    n = len(rp) - 1
+    perm = np.random.default_rng(seed).permutation(n)
+    B = sp.csr_matrix((v, ci, rp), shape=(n, n))[perm][:, perm].tocsr()
+    B.sort_indices()
+    return B.indptr.astype(np.uint32), B.indices.astype(np.uint32), B.data.astype(np.float64)
+
+
+def _random_dominant(n, per_row, seed):
+    # random pattern with up to per_row off-diagonals a row plus a dominant
+    # diagonal: rows with more entries in one level than the apply prefetches
+    sp = pytest.importorskip("scipy.sparse")
+    rng = np.random.default_rng(seed)
+    r = np.repeat(np.arange(n), per_row)
+    c = rng.integers(0, n, n * per_row)
+    M = sp.coo_matrix((rng.uniform(-1, 0, n * per_row), (r, c)), shape=(n, n)).tocsr()
+    M = M + M.T
+    M = M + sp.diags(np.asarray(abs(M).sum(axis=1)).ravel() + 1.0)
+    M = M.tocsr()
+    M.sum_duplicates()
+    M.sort_indices()
+    return M.indptr.astype(np.uint32), M.indices.astype(np.uint32), M.data.astype(np.float64)
+
+
+@pytest.mark.parametrize("case", ["lap3d", "lap3d_40", "diffusion2d", "scrambled2d",
+                                  "scrambled3d", "random"])
 def test_factors_match_oracle(V, case):
+    # lap3d_40 has levels above and below the single-block run size, so the
+    # apply mixes both kernels; the scrambled and random patterns have rows
+    # spread over several levels
     import torch
     if case == "lap3d":
         rp, ci, v = gen.laplace3d(20)
+    elif case == "lap3d_40":
+        rp, ci, v = gen.laplace3d(40)
+    elif case == "scrambled2d":
+        rp, ci, v = _scrambled(*gen.convdiff2d(40, 40, peclet=10.0, shift=0.01), seed=5)
+    elif case == "scrambled3d":
+        rp, ci, v = _scrambled(*gen.laplace3d(16), seed=6)
+    elif case == "random":
+        rp, ci, v = _random_dominant(3000, 8, seed=7)
     else:
         rp, ci, v, _ = gen.diffusion2d_edges(60)
     n = len(rp) - 1

@@ -419,15 +419,120 @@ std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_sc
   return P;
 }
 
+// A run of consecutive levels of at most kRunLevel rows each, substituted by
+// one block of kRunLevel threads: a level is one pass of the block, and a
+// __syncthreads() (the block's own writes to vec are visible to it after the
+// barrier) replaces the kernel launch between levels.  On a 2D grid every
+// level is an anti-diagonal of at most a few hundred rows, so the whole
+// triangle becomes one launch instead of 2*sqrt(n).
+//
+// A level holds, for each row, the entries whose columns lie in that level
+// (a row is updated at every level its columns reach), so vec[row] and
+// vec[cols] are read only after the barrier.  The pattern is not written: a
+// thread's row index and entry range are fetched two levels ahead and its
+// first kRunPre columns and values one level ahead, so that the critical path
+// of a level is one round of vec loads, one multiply-add chain, one store and
+// the barrier.  Each row is computed exactly as in level_substitute_kernel
+// (same entries, same order), so the results are identical.
+constexpr uint32_t kRunLevel = 1024;
+constexpr int kRunPre = 4;
+
+constexpr uint32_t kNoRow = 0xffffffffu;
+
+struct RunRow {
+  uint32_t row, jb, je;  // row == kNoRow when the thread has no row in the level
+};
+
+template <typename T>
+struct RunEntries {
+  RunRow r;
+  uint32_t c[kRunPre];
+  T v[kRunPre];
+};
+
+__device__ __forceinline__ RunRow run_fetch_row(uint32_t lev, uint32_t lev1,
+                                                const uint32_t *__restrict__ level_ptr,
+                                                const uint32_t *__restrict__ row_index,
+                                                const uint32_t *__restrict__ row_ptr) {
+  RunRow r{kNoRow, 0, 0};
+  if (lev < lev1) {
+    const uint32_t t = __ldg(level_ptr + lev) + threadIdx.x;
+    if (t < __ldg(level_ptr + lev + 1)) {
+      r.row = __ldg(row_index + t);
+      r.jb = __ldg(row_ptr + t);
+      r.je = __ldg(row_ptr + t + 1);
+    }
+  }
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ RunEntries<T> run_fetch_entries(RunRow r,
+                                                           const uint32_t *__restrict__ cols,
+                                                           const T *__restrict__ vals) {
+  RunEntries<T> e;
+  e.r = r;
+#pragma unroll
+  for (int k = 0; k < kRunPre; ++k) {
+    const bool on = r.jb + k < r.je;
+    e.c[k] = on ? __ldg(cols + r.jb + k) : 0u;
+    e.v[k] = on ? __ldg(vals + r.jb + k) : T(0);
+  }
+  return e;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRunLevel)
+    level_run_kernel(uint32_t lev0, uint32_t lev1, const uint32_t *__restrict__ level_ptr,
+                     const uint32_t *__restrict__ row_index, const uint32_t *__restrict__ row_ptr,
+                     const uint32_t *__restrict__ cols, const T *__restrict__ vals, T *vec,
+                     const int *skip) {
+  if (skip && *skip) return;
+  RunEntries<T> cur = run_fetch_entries<T>(
+      run_fetch_row(lev0, lev1, level_ptr, row_index, row_ptr), cols, vals);
+  RunRow next = run_fetch_row(lev0 + 1, lev1, level_ptr, row_index, row_ptr);
+  for (uint32_t lev = lev0; lev < lev1; ++lev) {
+    const RunRow r = cur.r;
+    const T x = r.row != kNoRow ? vec[r.row] : T(0);
+    T y[kRunPre];
+#pragma unroll
+    for (int k = 0; k < kRunPre; ++k) y[k] = r.jb + k < r.je ? vec[cur.c[k]] : T(0);
+    const RunRow after = run_fetch_row(lev + 2, lev1, level_ptr, row_index, row_ptr);
+    const RunEntries<T> upcoming = run_fetch_entries<T>(next, cols, vals);
+    if (r.row != kNoRow) {
+      T s = x;
+#pragma unroll
+      for (int k = 0; k < kRunPre; ++k)
+        if (r.jb + k < r.je) s -= y[k] * cur.v[k];
+      for (uint32_t j = r.jb + kRunPre; j < r.je; ++j) s -= vec[__ldg(cols + j)] * __ldg(vals + j);
+      vec[r.row] = s;
+    }
+    __syncthreads();
+    cur = upcoming;
+    next = after;
+  }
+}
+
 template <typename T>
 static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *skip) {
-  for (uint32_t L = 0; L < tri.levels; ++L) {
-    uint32_t r0 = tri.h_level_ptr[L], r1 = tri.h_level_ptr[L + 1];
+  for (uint32_t L = 0; L < tri.levels;) {
+    const uint32_t r0 = tri.h_level_ptr[L], r1 = tri.h_level_ptr[L + 1];
+    if (r1 - r0 <= kRunLevel) {
+      uint32_t L1 = L + 1;
+      while (L1 < tri.levels && tri.h_level_ptr[L1 + 1] - tri.h_level_ptr[L1] <= kRunLevel) ++L1;
+      level_run_kernel<T><<<1, kRunLevel, 0, be.stream>>>(
+          L, L1, tri.level_ptr.as<uint32_t>(), tri.row_index.as<uint32_t>(),
+          tri.row_ptr.as<uint32_t>(), tri.cols.as<uint32_t>(), tri.vals.as<T>(), vec, skip);
+      be.launches++;
+      L = L1;
+      continue;
+    }
     int g = waves_grid(be, 128, 16, r1 - r0);
     level_substitute_kernel<T><<<g, 128, 0, be.stream>>>(
         r0, r1, tri.row_index.as<uint32_t>(), tri.row_ptr.as<uint32_t>(), tri.cols.as<uint32_t>(),
         tri.vals.as<T>(), vec, skip);
     be.launches++;
+    ++L;
   }
   VCLGB_CHECK_LAUNCH();
 }
