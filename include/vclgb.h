@@ -270,6 +270,30 @@ VCLGB_API vclgbStatus vclgbRowScalingCreate(vclgbBackend be, vclgbMatrix A, uint
  * the device with the reference's elimination order (detail/ilu/common.hpp:50-187). */
 VCLGB_API vclgbStatus vclgbIlu0Create(vclgbBackend be, vclgbMatrix A, int use_level_scheduling,
                                       vclgbPrecond *out);
+/* chow_patel_ilu_precond<compressed_matrix>(A, chow_patel_tag(sweeps, jacobi_iters))
+ * and chow_patel_icc_precond (linalg/detail/ilu/chow_patel_ilu.hpp:44-70 tag,
+ * :77-150 setup, :170-300 apply; reference defaults sweeps 3, jacobi_iters 2).
+ * The setup runs on the device with the reference's operation order, so the
+ * Neumann matrices I - D^-1 L, I - D^-1 U and the diagonals are bit-identical
+ * to the host backend's.  A needs ascending, duplicate-free columns in every
+ * row (else VCLGB_INVALID_MATRIX: the reference's merge assumes them) and a
+ * nonzero diagonal entry in every row (else VCLGB_ZERO_ON_DIAGONAL, where the
+ * reference asserts). */
+VCLGB_API vclgbStatus vclgbChowPatelIluCreate(vclgbBackend be, vclgbMatrix A, uint32_t sweeps,
+                                              uint32_t jacobi_iters, vclgbPrecond *out);
+VCLGB_API vclgbStatus vclgbChowPatelIccCreate(vclgbBackend be, vclgbMatrix A, uint32_t sweeps,
+                                              uint32_t jacobi_iters, vclgbPrecond *out);
+typedef struct {
+  uint32_t kind;                 /* 0 ILU, 1 ICC */
+  uint32_t sweeps, jacobi_iters;
+  uint64_t nnz_L, nnz_U;         /* strictly triangular entries of the Neumann matrices */
+} vclgbChowPatelInfo;
+VCLGB_API vclgbStatus vclgbChowPatelGetInfo(vclgbPrecond P, vclgbChowPatelInfo *info);
+/* Exports, into device memory: 0 L row_ptr u32[rows+1], 1 L cols u32[nnz_L],
+ * 2 L values T[nnz_L] (I - D_L^-1 L without its zero diagonal), 3 D_L T[rows],
+ * 4..7 the same for U (ICC: L^T, and D_L again). */
+VCLGB_API vclgbStatus vclgbChowPatelExport(vclgbBackend be, vclgbPrecond P, int which,
+                                           void *d_dst);
 /* precond.apply(vec) in place on a contiguous device vector of length rows. */
 VCLGB_API vclgbStatus vclgbPrecondApply(vclgbBackend be, vclgbPrecond P, void *d_vec);
 VCLGB_API vclgbStatus vclgbPrecondDestroy(vclgbPrecond *P);

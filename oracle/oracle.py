@@ -32,7 +32,10 @@ class Tag(ctypes.Structure):
 
 class Precond(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("diag", ctypes.c_void_p), ("rp", ctypes.c_void_p),
-                ("ci", ctypes.c_void_p), ("lu", ctypes.c_void_p), ("udiag", ctypes.c_void_p)]
+                ("ci", ctypes.c_void_p), ("lu", ctypes.c_void_p), ("udiag", ctypes.c_void_p),
+                ("l_rp", ctypes.c_void_p), ("l_ci", ctypes.c_void_p), ("l_v", ctypes.c_void_p),
+                ("u_rp", ctypes.c_void_p), ("u_ci", ctypes.c_void_p), ("u_v", ctypes.c_void_p),
+                ("jacobi_iters", ctypes.c_uint32)]
 
 
 def build():
@@ -89,6 +92,12 @@ def lib():
                                      ctypes.POINTER(_U32), ctypes.POINTER(_U32),
                                      ctypes.POINTER(_D)]
         L.vo_ilu0_factor_d.argtypes = [_U32, _u32p, _u32p, _f64p]
+        L.vo_cp_counts.argtypes = [_U32, _u32p, _u32p, ctypes.c_void_p, ctypes.c_void_p]
+        L.vo_chow_patel_ilu_d.argtypes = [_U32, _u32p, _u32p, _f64p, _U32, _u32p, _u32p, _f64p,
+                                          _f64p, _u32p, _u32p, _f64p, _f64p]
+        L.vo_chow_patel_icc_d.argtypes = [_U32, _u32p, _u32p, _f64p, _U32, _u32p, _u32p, _f64p,
+                                          _u32p, _u32p, _f64p, _f64p]
+        L.vo_precond_apply_d.argtypes = [_U32, ctypes.c_void_p, _f64p]
         L.vo_level_setup_d.argtypes = [_U32, _u32p, _u32p, _f64p, ctypes.c_void_p, _I,
                                        ctypes.POINTER(_SZ), ctypes.POINTER(_SZ), ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -234,7 +243,13 @@ def coo_spmv(n, C, x, alpha=1.0, beta=0.0, y0=None):
 
 
 def _precond(kind, rp=None, ci=None, v=None):
+    """kind: none | jacobi | ilu0 | row0/1/2 | cpilu[:sweeps:iters] | cpicc[:sweeps:iters]"""
     P = Precond()
+    if kind.startswith("cp"):
+        parts = kind.split(":")
+        sweeps, iters = (int(parts[1]), int(parts[2])) if len(parts) == 3 else (3, 2)
+        F = (chow_patel_ilu if parts[0] == "cpilu" else chow_patel_icc)(rp, ci, v, sweeps)
+        return _cp_struct(F, iters)
     P.kind = {"none": 0, "jacobi": 1, "ilu0": 2, "row0": 1, "row1": 1, "row2": 1}[kind]
     keep = []
     if kind == "jacobi" or kind.startswith("row"):
@@ -330,6 +345,81 @@ def ilu0_apply(rp, ci, v, vec):
     z = level_substitute(L, vec)
     z = z / ud
     return level_substitute(U, z)
+
+
+def chow_patel_ilu(rp, ci, v, sweeps=3):
+    """chow_patel_ilu_precond setup (chow_patel_ilu.hpp:110-150): the Neumann
+    matrices I - D_L^-1 L and I - D_U^-1 U (diagonal entries kept as zeros) and
+    D_L, D_U."""
+    n = len(rp) - 1
+    rp, ci, v = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64)
+    nl, nu = _SZ(), _SZ()
+    lib().vo_cp_counts(n, rp, ci, ctypes.byref(nl), ctypes.byref(nu))
+    F = dict(l_rp=np.zeros(n + 1, np.uint32), l_ci=np.zeros(max(nl.value, 1), np.uint32),
+             l_v=np.zeros(max(nl.value, 1)), diag_l=np.zeros(max(n, 1)),
+             u_rp=np.zeros(n + 1, np.uint32), u_ci=np.zeros(max(nu.value, 1), np.uint32),
+             u_v=np.zeros(max(nu.value, 1)), diag_u=np.zeros(max(n, 1)))
+    lib().vo_chow_patel_ilu_d(n, rp, ci, v, sweeps, F["l_rp"], F["l_ci"], F["l_v"], F["diag_l"],
+                              F["u_rp"], F["u_ci"], F["u_v"], F["diag_u"])
+    return _cp_trim(F, n, nl.value, nu.value)
+
+
+def chow_patel_icc(rp, ci, v, sweeps=3):
+    """chow_patel_icc_precond setup (chow_patel_ilu.hpp:77-107): I - D_L^-1 L,
+    I - D_L^-1 L^T (as u_*) and D_L (as diag_l and diag_u)."""
+    n = len(rp) - 1
+    rp, ci, v = _c(rp, np.uint32), _c(ci, np.uint32), _c(v, np.float64)
+    nl, nu = _SZ(), _SZ()
+    lib().vo_cp_counts(n, rp, ci, ctypes.byref(nl), ctypes.byref(nu))
+    m = max(nl.value, 1)
+    F = dict(l_rp=np.zeros(n + 1, np.uint32), l_ci=np.zeros(m, np.uint32), l_v=np.zeros(m),
+             u_rp=np.zeros(n + 1, np.uint32), u_ci=np.zeros(m, np.uint32), u_v=np.zeros(m),
+             diag_l=np.zeros(max(n, 1)))
+    lib().vo_chow_patel_icc_d(n, rp, ci, v, sweeps, F["l_rp"], F["l_ci"], F["l_v"], F["u_rp"],
+                              F["u_ci"], F["u_v"], F["diag_l"])
+    F["diag_u"] = F["diag_l"]
+    return _cp_trim(F, n, nl.value, nl.value)
+
+
+def _cp_trim(F, n, nl, nu):
+    for k in ("l_ci", "l_v"):
+        F[k] = F[k][:nl]
+    for k in ("u_ci", "u_v"):
+        F[k] = F[k][:nu]
+    for k in ("diag_l", "diag_u"):
+        F[k] = F[k][:n]
+    return F
+
+
+def _cp_struct(F, iters):
+    P = Precond()
+    P.kind = 3
+    keep = {k: np.ascontiguousarray(a if len(a) else np.zeros(1, a.dtype)) for k, a in F.items()}
+    P.diag, P.udiag = keep["diag_l"].ctypes.data, keep["diag_u"].ctypes.data
+    for k in ("l_rp", "l_ci", "l_v", "u_rp", "u_ci", "u_v"):
+        setattr(P, k, keep[k].ctypes.data)
+    P.jacobi_iters = iters
+    return P, [keep]
+
+
+def chow_patel_apply(F, vec, jacobi_iters=2):
+    """precond.apply(vec) of either Chow-Patel preconditioner (chow_patel_ilu.hpp:190-222,
+    269-300)."""
+    vec = _c(vec, np.float64).copy()
+    P, keep = _cp_struct(F, jacobi_iters)
+    lib().vo_precond_apply_d(len(vec), ctypes.byref(P), vec)
+    del keep
+    return vec
+
+
+def strip_diagonal(rp, ci, v):
+    """CSR without its diagonal entries (the Neumann matrices' zeroed diagonals)."""
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    keep = ci != rows
+    nrp = np.zeros(n + 1, np.uint32)
+    np.cumsum(np.bincount(rows[keep], minlength=n), out=nrp[1:])
+    return nrp, ci[keep].astype(np.uint32), v[keep]
 
 
 def transpose(nrows, ncols, rp, ci, v):

@@ -150,6 +150,12 @@ void dump_levels(std::string const &prefix, Level const &row_index, Level const 
   save(prefix + "_vals.f64", vals.data(), vals.size());
 }
 
+void dump_csr(std::string const &prefix, viennacl::compressed_matrix<double> const &M, size_t n) {
+  save(prefix + "_rp.u32", raw<unsigned>(M.handle1()), n + 1);
+  save(prefix + "_ci.u32", raw<unsigned>(M.handle2()), M.nnz());
+  save(prefix + "_v.f64", raw<double>(M.handle()), M.nnz());
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -318,6 +324,18 @@ int main(int argc, char **argv) {
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag, P);
         t1 = now();
+      } else if (pc == "cpilu") {
+        viennacl::linalg::chow_patel_ilu_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::chow_patel_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc == "cpicc") {
+        viennacl::linalg::chow_patel_icc_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::chow_patel_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
       } else {
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag);
@@ -336,6 +354,18 @@ int main(int argc, char **argv) {
       } else if (pc.compare(0, 3, "row") == 0) {
         viennacl::linalg::row_scaling<viennacl::compressed_matrix<double> > P(
             M, viennacl::linalg::row_scaling_tag(static_cast<unsigned>(pc[3] - '0')));
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc == "cpilu") {
+        viennacl::linalg::chow_patel_ilu_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::chow_patel_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc == "cpicc") {
+        viennacl::linalg::chow_patel_icc_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::chow_patel_tag());
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag, P);
         t1 = now();
@@ -393,6 +423,44 @@ int main(int argc, char **argv) {
     P.apply(z);
     std::vector<double> zh = from_vcl(z);
     save("z.f64", zh.data(), n);
+  } else if (cmd == "chow_patel") {  // args: sweeps jacobi_iters -> cpl_*/cpu_* (ILU), icl_*/iclt_* (ICC), z
+    viennacl::linalg::chow_patel_tag tag(static_cast<std::size_t>(std::atol(argv[3])),
+                                         static_cast<std::size_t>(std::atol(argv[4])));
+    viennacl::compressed_matrix<double> M;
+    fill_matrix(A, M);
+    std::vector<double> bh = load<double>("b.f64", n);
+    {
+      viennacl::compressed_matrix<double> L, U;
+      viennacl::vector<double> dL(n), dU(n);
+      viennacl::linalg::detail::precondition(M, L, dL, U, dU, tag);
+      dump_csr("cpl", L, n);
+      dump_csr("cpu", U, n);
+      std::vector<double> h = from_vcl(dL);
+      save("cpl_diag.f64", h.data(), n);
+      h = from_vcl(dU);
+      save("cpu_diag.f64", h.data(), n);
+      viennacl::linalg::chow_patel_ilu_precond<viennacl::compressed_matrix<double> > P(M, tag);
+      viennacl::vector<double> z(n);
+      to_vcl(bh, z);
+      P.apply(z);
+      h = from_vcl(z);
+      save("cp_ilu_z.f64", h.data(), n);
+    }
+    {
+      viennacl::compressed_matrix<double> L, Lt;
+      viennacl::vector<double> dL(n);
+      viennacl::linalg::detail::precondition(M, L, dL, Lt, tag);
+      dump_csr("icl", L, n);
+      dump_csr("iclt", Lt, n);
+      std::vector<double> h = from_vcl(dL);
+      save("icl_diag.f64", h.data(), n);
+      viennacl::linalg::chow_patel_icc_precond<viennacl::compressed_matrix<double> > P(M, tag);
+      viennacl::vector<double> z(n);
+      to_vcl(bh, z);
+      P.apply(z);
+      h = from_vcl(z);
+      save("cp_icc_z.f64", h.data(), n);
+    }
   } else if (cmd == "row_norms") {  // -> norm0.f64, norm1.f64, norm2.f64 (row_info)
     viennacl::compressed_matrix<double> M;
     fill_matrix(A, M);

@@ -445,6 +445,233 @@ static void vo_ilu0_solve(vo_u32 n, const vo_precond *P, double *vec) {
 }
 
 /* jacobi_precond::apply = element_div(vec, diag) -- jacobi_precond.hpp:121-126 */
+/* ------------------------------------------------------------------------ */
+/* Chow-Patel parallel ILU0 / ICC0: linalg/detail/ilu/chow_patel_ilu.hpp     */
+/* (setup :77-150, apply :190-222 and :269-300) over the host kernels of     */
+/* linalg/host_based/ilu_operations.hpp.  Sweeps read the previous sweep's  */
+/* values only (the reference's backup copies), so they are deterministic.  */
+/* ------------------------------------------------------------------------ */
+void vo_cp_counts(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, size_t *nnz_l, size_t *nnz_u) {
+  size_t l = 0, u = 0;
+  for (vo_u32 r = 0; r < n; ++r)
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j) {
+      if (ci[j] <= r) ++l;
+      if (ci[j] >= r) ++u;
+    }
+  *nnz_l = l;
+  *nnz_u = u;
+}
+
+/* extract_L / extract_LU (ilu_operations.hpp:52-121, 257-345): a row's lower
+ * (col <= row) or upper (col >= row) entries in storage order */
+static void vo_cp_extract(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                          int upper, vo_u32 *orp, vo_u32 *oci, double *ov) {
+  size_t k = 0;
+  orp[0] = 0;
+  for (vo_u32 r = 0; r < n; ++r) {
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j)
+      if (upper ? ci[j] >= r : ci[j] <= r) {
+        oci[k] = ci[j];
+        ov[k] = v[j];
+        ++k;
+      }
+    orp[r + 1] = (vo_u32)k;
+  }
+}
+
+/* ilu_scale / icc_scale (:123-182, :348-428): D_r = 1 / sqrt(|a_rr|) from the
+ * row's first diagonal entry (0 without one), then m_ij *= D_i * D_j */
+static void vo_cp_scale_vector(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                               double *D) {
+  for (vo_u32 r = 0; r < n; ++r) {
+    D[r] = 0;
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j)
+      if (ci[j] == r) {
+        D[r] = 1.0 / sqrt(fabs(v[j]));
+        break;
+      }
+  }
+}
+
+static void vo_cp_scale(vo_u32 n, const vo_u32 *mrp, const vo_u32 *mci, double *mv,
+                        const double *D) {
+  for (vo_u32 r = 0; r < n; ++r) {
+    double dr = D[r];
+    for (vo_u32 j = mrp[r]; j < mrp[r + 1]; ++j) mv[j] *= dr * D[mci[j]];
+  }
+}
+
+/* ilu_transpose (:430-500): rows of the transpose in ascending source row */
+static void vo_cp_transpose(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                            vo_u32 *trp, vo_u32 *tci, double *tv) {
+  vo_u32 *cur = (vo_u32 *)calloc((size_t)n + 1, sizeof(vo_u32));
+  for (vo_u32 c = 0; c <= n; ++c) trp[c] = 0;
+  for (vo_u32 r = 0; r < n; ++r)
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j) trp[ci[j]] += 1;
+  vo_u32 off = 0;
+  for (vo_u32 c = 0; c < n; ++c) {
+    vo_u32 t = trp[c];
+    trp[c] = off;
+    off += t;
+  }
+  trp[n] = off;
+  for (vo_u32 r = 0; r < n; ++r)
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j) {
+      vo_u32 c = ci[j], k = trp[c] + cur[c]++;
+      tci[k] = r;
+      tv[k] = v[j];
+    }
+  free(cur);
+}
+
+/* ilu_chow_patel_sweep (:502-623): L from the previous L and U^T, U^T from the
+ * previous L and U^T; l_ij = (a_ij - sum_k l_ik u_kj) / u_jj, u_ij = a_ij - sum */
+static void vo_cp_ilu_sweep(vo_u32 n, const vo_u32 *lrp, const vo_u32 *lci, double *lv,
+                            const double *aL, const vo_u32 *utrp, const vo_u32 *utci, double *utv,
+                            const double *aU, double *Lb, double *Ub) {
+  long row;
+  memcpy(Lb, lv, sizeof(double) * lrp[n]);
+  memcpy(Ub, utv, sizeof(double) * utrp[n]);
+#pragma omp parallel for if (n > VO_OMP_MIN)
+  for (row = 0; row < (long)n; ++row) {
+    vo_u32 ls = lrp[row], le = lrp[row + 1];
+    for (vo_u32 j = ls; j < le; ++j) {
+      vo_u32 col = lci[j];
+      if (col == (vo_u32)row) continue;
+      vo_u32 us = utrp[col], ue = utrp[col + 1], iu = us;
+      vo_u32 cu = iu < ue ? utci[iu] : n;
+      double sum = 0;
+      for (vo_u32 k = ls; k < j; ++k) {
+        vo_u32 cl = lci[k];
+        while (cu < cl) cu = utci[++iu];
+        if (cu == cl) sum += Lb[k] * Ub[iu];
+      }
+      lv[j] = (aL[j] - sum) / Ub[ue - 1];
+    }
+    vo_u32 us = utrp[row], ue = utrp[row + 1];
+    for (vo_u32 j = us; j < ue; ++j) {
+      vo_u32 col = utci[j];
+      vo_u32 cs = lrp[col], ce = lrp[col + 1], il = cs;
+      vo_u32 cl = il < ce ? lci[il] : n;
+      double sum = 0;
+      for (vo_u32 k = us; k < j; ++k) {
+        vo_u32 cu = utci[k];
+        while (cl < cu) cl = lci[++il];
+        if (cu == cl) sum += Lb[il] * Ub[k];
+      }
+      utv[j] = aU[j] - sum;
+    }
+  }
+}
+
+/* icc_chow_patel_sweep (:184-255): l_ij = (a_ij - sum_k l_ik l_jk) / l_jj,
+ * l_ii = sqrt(a_ii - sum_k l_ik^2) */
+static void vo_cp_icc_sweep(vo_u32 n, const vo_u32 *lrp, const vo_u32 *lci, double *lv,
+                            const double *aL, double *Lb) {
+  long row;
+  memcpy(Lb, lv, sizeof(double) * lrp[n]);
+#pragma omp parallel for if (n > VO_OMP_MIN)
+  for (row = 0; row < (long)n; ++row) {
+    vo_u32 s0 = lrp[row], e0 = lrp[row + 1];
+    for (vo_u32 i = s0; i < e0; ++i) {
+      vo_u32 col = lci[i];
+      vo_u32 js = lrp[col], je = lrp[col + 1], ij = js;
+      vo_u32 cj = lci[ij];
+      double s = aL[i];
+      for (vo_u32 ii = s0; ii < i; ++ii) {
+        vo_u32 c = lci[ii];
+        while (cj < c) cj = lci[++ij];
+        if (cj == c) s -= Lb[ii] * Lb[ij];
+      }
+      lv[i] = col != (vo_u32)row ? s / Lb[je - 1] : sqrt(s);
+    }
+  }
+}
+
+/* ilu_form_neumann_matrix (:625-667): d = the row's first diagonal entry, which
+ * is set to 0; every entry of the row is then divided by -d */
+static void vo_cp_neumann(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, double *v, double *diag) {
+  for (vo_u32 r = 0; r < n; ++r) {
+    double d = 0;
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j)
+      if (ci[j] == r) {
+        d = v[j];
+        v[j] = 0;
+        break;
+      }
+    diag[r] = d;
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j) v[j] /= -d;
+  }
+}
+
+void vo_chow_patel_ilu_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                         vo_u32 sweeps, vo_u32 *l_rp, vo_u32 *l_ci, double *l_v, double *diag_l,
+                         vo_u32 *u_rp, vo_u32 *u_ci, double *u_v, double *diag_u) {
+  vo_cp_extract(n, rp, ci, v, 0, l_rp, l_ci, l_v);
+  vo_cp_extract(n, rp, ci, v, 1, u_rp, u_ci, u_v);
+  size_t nl = l_rp[n], nu = u_rp[n];
+  double *D = (double *)malloc(sizeof(double) * (n ? n : 1));
+  vo_cp_scale_vector(n, rp, ci, v, D);
+  vo_cp_scale(n, l_rp, l_ci, l_v, D);
+  vo_cp_scale(n, u_rp, u_ci, u_v, D);
+  vo_u32 *ut_rp = (vo_u32 *)malloc(sizeof(vo_u32) * ((size_t)n + 1));
+  vo_u32 *ut_ci = (vo_u32 *)malloc(sizeof(vo_u32) * (nu ? nu : 1));
+  double *ut_v = (double *)malloc(sizeof(double) * (nu ? nu : 1));
+  vo_cp_transpose(n, u_rp, u_ci, u_v, ut_rp, ut_ci, ut_v);
+  double *aL = (double *)malloc(sizeof(double) * (nl ? nl : 1));
+  double *aU = (double *)malloc(sizeof(double) * (nu ? nu : 1));
+  double *Lb = (double *)malloc(sizeof(double) * (nl ? nl : 1));
+  double *Ub = (double *)malloc(sizeof(double) * (nu ? nu : 1));
+  memcpy(aL, l_v, sizeof(double) * nl);
+  memcpy(aU, ut_v, sizeof(double) * nu);
+  for (vo_u32 s = 0; s < sweeps; ++s)
+    vo_cp_ilu_sweep(n, l_rp, l_ci, l_v, aL, ut_rp, ut_ci, ut_v, aU, Lb, Ub);
+  vo_cp_transpose(n, ut_rp, ut_ci, ut_v, u_rp, u_ci, u_v);
+  vo_cp_neumann(n, l_rp, l_ci, l_v, diag_l);
+  vo_cp_neumann(n, u_rp, u_ci, u_v, diag_u);
+  free(D); free(ut_rp); free(ut_ci); free(ut_v); free(aL); free(aU); free(Lb); free(Ub);
+}
+
+void vo_chow_patel_icc_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                         vo_u32 sweeps, vo_u32 *l_rp, vo_u32 *l_ci, double *l_v,
+                         vo_u32 *lt_rp, vo_u32 *lt_ci, double *lt_v, double *diag_l) {
+  vo_cp_extract(n, rp, ci, v, 0, l_rp, l_ci, l_v);
+  size_t nl = l_rp[n];
+  double *D = (double *)malloc(sizeof(double) * (n ? n : 1));
+  vo_cp_scale_vector(n, rp, ci, v, D);
+  vo_cp_scale(n, l_rp, l_ci, l_v, D);
+  double *aL = (double *)malloc(sizeof(double) * (nl ? nl : 1));
+  double *Lb = (double *)malloc(sizeof(double) * (nl ? nl : 1));
+  memcpy(aL, l_v, sizeof(double) * nl);
+  for (vo_u32 s = 0; s < sweeps; ++s) vo_cp_icc_sweep(n, l_rp, l_ci, l_v, aL, Lb);
+  vo_cp_transpose(n, l_rp, l_ci, l_v, lt_rp, lt_ci, lt_v);
+  vo_cp_neumann(n, l_rp, l_ci, l_v, diag_l);
+  vo_cp_neumann(n, lt_rp, lt_ci, lt_v, diag_l);
+  free(D); free(aL); free(Lb);
+}
+
+/* apply (chow_patel_ilu.hpp:269-300): y = L^-1 vec and then U^-1 y, each by
+ * jacobi_iters steps x <- (I - D^-1 M) x + D^-1 rhs from x = D^-1 rhs */
+static void vo_cp_apply(vo_u32 n, const vo_precond *P, double *vec) {
+  size_t bytes = sizeof(double) * (n ? n : 1);
+  double *b = (double *)malloc(bytes), *x = (double *)malloc(bytes);
+  for (int tri = 0; tri < 2; ++tri) {
+    const double *d = tri ? P->udiag : P->diag;
+    const vo_u32 *mrp = tri ? P->u_rp : P->l_rp, *mci = tri ? P->u_ci : P->l_ci;
+    const double *mv = tri ? P->u_v : P->l_v;
+    const double *src = tri ? x : vec;
+    for (vo_u32 i = 0; i < n; ++i) b[i] = src[i] / d[i];
+    memcpy(x, b, sizeof(double) * n);
+    for (vo_u32 it = 0; it < P->jacobi_iters; ++it) {
+      vo_csr_spmv_d(n, mrp, mci, mv, x, 1.0, 0.0, vec);
+      for (vo_u32 i = 0; i < n; ++i) x[i] = vec[i] + b[i];
+    }
+  }
+  memcpy(vec, x, sizeof(double) * n);
+  free(b);
+  free(x);
+}
+
 void vo_precond_apply_d(vo_u32 n, const vo_precond *P, double *vec) {
   if (!P || P->kind == VO_PRECOND_NONE) return;
   if (P->kind == VO_PRECOND_JACOBI) {
@@ -453,6 +680,8 @@ void vo_precond_apply_d(vo_u32 n, const vo_precond *P, double *vec) {
     for (i = 0; i < (long)n; ++i) vec[i] = vec[i] / P->diag[i];
   } else if (P->kind == VO_PRECOND_ILU0) {
     vo_ilu0_solve(n, P, vec);
+  } else if (P->kind == VO_PRECOND_CHOW_PATEL) {
+    vo_cp_apply(n, P, vec);
   }
 }
 

@@ -91,16 +91,23 @@ typedef struct {
   double   error;               /* out: the solver's own estimate */
 } vo_tag;
 
-enum { VO_PRECOND_NONE = 0, VO_PRECOND_JACOBI = 1, VO_PRECOND_ILU0 = 2 };
+enum { VO_PRECOND_NONE = 0, VO_PRECOND_JACOBI = 1, VO_PRECOND_ILU0 = 2, VO_PRECOND_CHOW_PATEL = 3 };
 
 typedef struct {
   int            kind;
-  const double  *diag;        /* Jacobi: diag(A) */
+  const double  *diag;        /* Jacobi: diag(A); Chow-Patel: D_L */
   /* ILU0: factors stored in A's pattern (unit L implicit), plus U diagonal */
   const vo_u32  *rp;
   const vo_u32  *ci;
   const double  *lu;
-  const double  *udiag;
+  const double  *udiag;       /* ILU0: U diagonal; Chow-Patel: D_U */
+  /* Chow-Patel: the Neumann matrices I - D_L^-1 L and I - D_U^-1 U in CSR
+   * (their diagonal entries stored as zeros, as the reference keeps them) */
+  const vo_u32  *l_rp, *l_ci;
+  const double  *l_v;
+  const vo_u32  *u_rp, *u_ci;
+  const double  *u_v;
+  vo_u32         jacobi_iters;
 } vo_precond;
 
 void vo_precond_apply_d(vo_u32 n, const vo_precond *P, double *vec);
@@ -141,6 +148,19 @@ size_t vo_level_setup_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const doub
 void vo_level_substitute_d(size_t nlev, const vo_u32 *level_ptr, const vo_u32 *row_index,
                            const vo_u32 *row_ptr, const vo_u32 *cols, const double *vals,
                            double *vec);
+
+/* ---- Chow-Patel ILU / ICC ----------------------------------------------- */
+/* Entries of A with col <= row (L) and col >= row (U). */
+void vo_cp_counts(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, size_t *nnz_l, size_t *nnz_u);
+/* chow_patel_ilu_precond setup: L (lower incl. diagonal, A's order) and U
+ * (upper incl. diagonal) as Neumann matrices with their diagonals D_L, D_U. */
+void vo_chow_patel_ilu_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                         vo_u32 sweeps, vo_u32 *l_rp, vo_u32 *l_ci, double *l_v, double *diag_l,
+                         vo_u32 *u_rp, vo_u32 *u_ci, double *u_v, double *diag_u);
+/* chow_patel_icc_precond setup: L and its transpose as Neumann matrices, D_L. */
+void vo_chow_patel_icc_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                         vo_u32 sweeps, vo_u32 *l_rp, vo_u32 *l_ci, double *l_v,
+                         vo_u32 *lt_rp, vo_u32 *lt_ci, double *lt_v, double *diag_l);
 
 /* ---- dense vector helpers ------------------------------------------------ */
 double vo_dot_d(size_t n, const double *a, const double *b);

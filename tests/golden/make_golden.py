@@ -5,8 +5,8 @@ inputs next to the reference outputs, so the tests need neither the reference
 tree nor a particular numpy random stream.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(python tests/golden/make_golden.py coo | row_scaling | matrix_market | cuthill_mckee
- writes only
+(python tests/golden/make_golden.py coo | row_scaling | matrix_market | cuthill_mckee |
+ chow_patel writes only
 that fixture; matrix_market also writes the input files under tests/golden/mm/)
 GMRES fixtures are produced with OMP_NUM_THREADS=1 (the host stage-1 kernel's
 result depends on the thread count).
@@ -143,6 +143,7 @@ def main():
     row_scaling_fixture()
     mm_fixture()
     cm_fixture()
+    chow_patel_fixture()
 
 
 def coo_fixture():
@@ -323,11 +324,40 @@ def cm_fixture():
          bw_cd=out["bw"], **res)
 
 
+def chow_patel_fixture():
+    """Chow-Patel ILU on a convection-diffusion matrix and Chow-Patel ICC on a
+    variable-coefficient diffusion matrix: the Neumann matrices and diagonals
+    of detail::precondition for two tags, the applies, and BiCGStab / CG
+    solves preconditioned by them (default tag)."""
+    cp, cc, cv = gen.convdiff2d(23, 19, peclet=10.0, shift=0.05)
+    sp, sc, sv, _ = gen.diffusion2d_edges(21, contrast=1e2, seed=43)
+    res = {}
+    for name, (rp, ci, v) in (("cd", (cp, cc, cv)), ("sd", (sp, sc, sv))):
+        n = len(rp) - 1
+        b = gen.rhs_uniform(n, 44)
+        res["b_" + name] = b
+        for sweeps, iters in ((3, 2), (1, 4)):
+            out = oracle.run_ref("chow_patel", rp, ci, v, args=(sweeps, iters), b=b)
+            tag = "%s_%d_%d_" % (name, sweeps, iters)
+            for k in ("cpl_rp", "cpl_ci", "cpl_v", "cpl_diag", "cpu_rp", "cpu_ci", "cpu_v",
+                      "cpu_diag", "cp_ilu_z", "icl_rp", "icl_ci", "icl_v", "icl_diag", "iclt_rp",
+                      "iclt_ci", "iclt_v", "cp_icc_z"):
+                res[tag + k] = out[k]
+    s = oracle.run_ref("bicgstab", cp, cc, cv, args=(1e-10, 2000, "cpilu"), b=res["b_cd"])
+    res.update(x_bicgstab_cpilu=s["x"], iters_bicgstab_cpilu=s["iters"],
+               error_bicgstab_cpilu=s["error"])
+    s = oracle.run_ref("cg", sp, sc, sv, args=(1e-10, 2000, "cpicc"), b=res["b_sd"])
+    res.update(x_cg_cpicc=s["x"], iters_cg_cpicc=s["iters"], error_cg_cpicc=s["error"])
+    save("chow_patel.npz", cp=cp, cc=cc, cv=cv, sp=sp, sc=sc, sv=sv, **res)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["coo"]:
         coo_fixture()
     elif sys.argv[1:] == ["row_scaling"]:
         row_scaling_fixture()
+    elif sys.argv[1:] == ["chow_patel"]:
+        chow_patel_fixture()
     elif sys.argv[1:] == ["matrix_market"]:
         mm_fixture()
     elif sys.argv[1:] == ["cuthill_mckee"]:

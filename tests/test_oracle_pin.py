@@ -75,6 +75,44 @@ def test_row_scaling_golden(golden):
         oracle.set_threads(oracle.max_threads())
 
 
+CP_ILU_KEYS = (("l_rp", "cpl_rp"), ("l_ci", "cpl_ci"), ("l_v", "cpl_v"), ("diag_l", "cpl_diag"),
+               ("u_rp", "cpu_rp"), ("u_ci", "cpu_ci"), ("u_v", "cpu_v"), ("diag_u", "cpu_diag"))
+CP_ICC_KEYS = (("l_rp", "icl_rp"), ("l_ci", "icl_ci"), ("l_v", "icl_v"), ("diag_l", "icl_diag"),
+               ("u_rp", "iclt_rp"), ("u_ci", "iclt_ci"), ("u_v", "iclt_v"))
+
+
+@pytest.mark.parametrize("mat", ["cd", "sd"])
+@pytest.mark.parametrize("sweeps,iters", [(3, 2), (1, 4)])
+def test_chow_patel_golden(golden, mat, sweeps, iters):
+    # detail::precondition's Neumann matrices and diagonals bit-exact, and both applies
+    d = golden("chow_patel.npz")
+    rp, ci, v = (d["cp"], d["cc"], d["cv"]) if mat == "cd" else (d["sp"], d["sc"], d["sv"])
+    t = "%s_%d_%d_" % (mat, sweeps, iters)
+    for fn, keys, z in ((oracle.chow_patel_ilu, CP_ILU_KEYS, "cp_ilu_z"),
+                        (oracle.chow_patel_icc, CP_ICC_KEYS, "cp_icc_z")):
+        F = fn(rp, ci, v, sweeps)
+        for mine, ref in keys:
+            assert np.array_equal(F[mine], d[t + ref]), (fn.__name__, mine)
+        assert np.array_equal(oracle.chow_patel_apply(F, d["b_" + mat], iters), d[t + z])
+
+
+def test_chow_patel_solves_golden(golden):
+    # BiCGStab + chow_patel_ilu_precond and CG + chow_patel_icc_precond, default
+    # tag (3 sweeps, 2 Jacobi iterations); single thread: identical iterations
+    d = golden("chow_patel.npz")
+    oracle.set_threads(1)
+    try:
+        x, it, err = oracle.solve("bicgstab", d["cp"], d["cc"], d["cv"], d["b_cd"], 1e-10, 2000,
+                                  "cpilu")
+        assert it == int(d["iters_bicgstab_cpilu"]) and err == float(d["error_bicgstab_cpilu"])
+        assert rel_err(x, d["x_bicgstab_cpilu"]) < 1e-12
+        x, it, err = oracle.solve("cg", d["sp"], d["sc"], d["sv"], d["b_sd"], 1e-10, 2000, "cpicc")
+        assert it == int(d["iters_cg_cpicc"]) and err == float(d["error_cg_cpicc"])
+        assert rel_err(x, d["x_cg_cpicc"]) < 1e-12
+    finally:
+        oracle.set_threads(oracle.max_threads())
+
+
 MM_CASES = [("general", 1), ("general_case", 1), ("symmetric", 1), ("pattern", 1), ("complex", 1),
             ("zero_based", 0), ("extra_lines", 1), ("bad_word", 1), ("bad_field", 1),
             ("bad_symmetry", 1), ("array", 1), ("out_of_range", 1), ("too_few", 1),

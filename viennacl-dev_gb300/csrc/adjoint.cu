@@ -72,6 +72,32 @@ struct Transposed {
   DevBuf map;
 };
 
+void csr_transpose_pattern(Backend &be, uint32_t rows, uint32_t cols, uint64_t nnz,
+                           const uint32_t *rp, const uint32_t *ci, DevBuf &trp, DevBuf &tci,
+                           DevBuf &map) {
+  trp.alloc(((size_t)cols + 1) * 4, be.stream);
+  tci.alloc(std::max<uint64_t>(nnz, 1) * 4, be.stream);
+  map.alloc(std::max<uint64_t>(nnz, 1) * 4, be.stream);
+  DevBuf cnt(std::max<size_t>(cols, 1) * 4, be.stream);
+  VCLGB_CUDA(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes, be.stream));
+  int g = waves_grid(be, 256, 8, std::max<uint64_t>(nnz, 1));
+  col_count_kernel<<<g, 256, 0, be.stream>>>(nnz, ci, cnt.as<uint32_t>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+  extern_scan_u32(be, cnt.as<uint32_t>(), cols, trp.as<uint32_t>());
+  DevBuf cursor(std::max<size_t>(cols, 1) * 4, be.stream);
+  VCLGB_CUDA(cudaMemcpyAsync(cursor.ptr, trp.ptr, (size_t)cols * 4, cudaMemcpyDeviceToDevice,
+                             be.stream));
+  int gr = waves_grid(be, 256, 8, rows);
+  t_scatter_kernel<<<gr, 256, 0, be.stream>>>(rows, rp, ci, cursor.as<uint32_t>(),
+                                              tci.as<uint32_t>(), map.as<uint32_t>());
+  int gc = waves_grid(be, 256, 8, cols);
+  t_sort_kernel<<<gc, 256, 0, be.stream>>>(cols, trp.as<uint32_t>(), tci.as<uint32_t>(),
+                                           map.as<uint32_t>());
+  be.launches += 2;
+  VCLGB_CHECK_LAUNCH();
+}
+
 static Transposed &transpose_of(Backend &be, Matrix &A) {
   static_assert(sizeof(Transposed) > 0, "");
   if (A.transposed) return *A.transposed;
@@ -83,26 +109,10 @@ static Transposed &transpose_of(Backend &be, Matrix &A) {
   m->rows = A.cols;
   m->cols = A.rows;
   m->nnz = A.nnz;
-  m->own_row_ptr.alloc(((size_t)A.cols + 1) * 4, be.stream);
-  m->own_col_idx.alloc(std::max<uint64_t>(A.nnz, 1) * 4, be.stream);
+  csr_transpose_pattern(be, A.rows, A.cols, A.nnz, A.row_ptr, A.col_idx, m->own_row_ptr,
+                        m->own_col_idx, tr->map);
   m->own_values.alloc(std::max<uint64_t>(A.nnz, 1) * A.vsize(), be.stream);
-  tr->map.alloc(std::max<uint64_t>(A.nnz, 1) * 4, be.stream);
-  DevBuf cnt(std::max<size_t>(A.cols, 1) * 4, be.stream);
-  VCLGB_CUDA(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes, be.stream));
   int g = waves_grid(be, 256, 8, std::max<uint64_t>(A.nnz, 1));
-  col_count_kernel<<<g, 256, 0, be.stream>>>(A.nnz, A.col_idx, cnt.as<uint32_t>());
-  be.launches++;
-  VCLGB_CHECK_LAUNCH();
-  extern_scan_u32(be, cnt.as<uint32_t>(), A.cols, m->own_row_ptr.as<uint32_t>());
-  DevBuf cursor(std::max<size_t>(A.cols, 1) * 4, be.stream);
-  VCLGB_CUDA(cudaMemcpyAsync(cursor.ptr, m->own_row_ptr.ptr, (size_t)A.cols * 4,
-                             cudaMemcpyDeviceToDevice, be.stream));
-  int gr = waves_grid(be, 256, 8, A.rows);
-  t_scatter_kernel<<<gr, 256, 0, be.stream>>>(A.rows, A.row_ptr, A.col_idx, cursor.as<uint32_t>(),
-                                              m->own_col_idx.as<uint32_t>(), tr->map.as<uint32_t>());
-  int gc = waves_grid(be, 256, 8, A.cols);
-  t_sort_kernel<<<gc, 256, 0, be.stream>>>(A.cols, m->own_row_ptr.as<uint32_t>(),
-                                           m->own_col_idx.as<uint32_t>(), tr->map.as<uint32_t>());
   if (A.vsize() == 8)
     t_gather_kernel<uint64_t><<<g, 256, 0, be.stream>>>(
         A.nnz, tr->map.as<uint32_t>(), static_cast<const uint64_t *>(A.values),
@@ -111,7 +121,7 @@ static Transposed &transpose_of(Backend &be, Matrix &A) {
     t_gather_kernel<uint32_t><<<g, 256, 0, be.stream>>>(
         A.nnz, tr->map.as<uint32_t>(), static_cast<const uint32_t *>(A.values),
         m->own_values.as<uint32_t>());
-  be.launches += 3;
+  be.launches++;
   VCLGB_CHECK_LAUNCH();
   m->row_ptr = m->own_row_ptr.as<uint32_t>();
   m->col_idx = m->own_col_idx.as<uint32_t>();

@@ -568,6 +568,61 @@ VCLGB_API vclgbStatus vclgbIlu0Create(vclgbBackend h, vclgbMatrix A, int lvl, vc
   });
 }
 
+static vclgbStatus chow_patel_create_api(vclgbBackend h, vclgbMatrix A, bool icc, uint32_t sweeps,
+                                         uint32_t iters, vclgbPrecond *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    auto P = chow_patel_create(*be, *M(A), icc, sweeps, iters);
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbPrecond>(P.release());
+  });
+}
+
+VCLGB_API vclgbStatus vclgbChowPatelIluCreate(vclgbBackend h, vclgbMatrix A, uint32_t sweeps,
+                                              uint32_t iters, vclgbPrecond *out) {
+  return chow_patel_create_api(h, A, false, sweeps, iters, out);
+}
+
+VCLGB_API vclgbStatus vclgbChowPatelIccCreate(vclgbBackend h, vclgbMatrix A, uint32_t sweeps,
+                                              uint32_t iters, vclgbPrecond *out) {
+  return chow_patel_create_api(h, A, true, sweeps, iters, out);
+}
+
+VCLGB_API vclgbStatus vclgbChowPatelGetInfo(vclgbPrecond p, vclgbChowPatelInfo *info) {
+  if (!p || !info) return VCLGB_INVALID_ARGUMENT;
+  const Precond &P = *vclgb::P(p);
+  if (P.kind != 3 && P.kind != 4) return VCLGB_INVALID_ARGUMENT;
+  info->kind = P.kind == 4 ? 1u : 0u;
+  info->sweeps = P.sweeps;
+  info->jacobi_iters = P.jacobi_iters;
+  info->nnz_L = P.cp_l->nnz;
+  info->nnz_U = P.cp_u->nnz;
+  return VCLGB_SUCCESS;
+}
+
+VCLGB_API vclgbStatus vclgbChowPatelExport(vclgbBackend h, vclgbPrecond p, int which, void *dst) {
+  if (!h || !p || !dst) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    const Precond &P = *vclgb::P(p);
+    require(P.kind == 3 || P.kind == 4, VCLGB_INVALID_ARGUMENT, "not a Chow-Patel preconditioner");
+    require(which >= 0 && which <= 7, VCLGB_INVALID_ARGUMENT, "no such Chow-Patel array");
+    const Matrix &m = which < 4 ? *P.cp_l : *P.cp_u;
+    const size_t vs = P.prec == VCLGB_FLOAT64 ? 8 : 4;
+    const void *src = nullptr;
+    size_t bytes = 0;
+    switch (which & 3) {
+      case 0: src = m.row_ptr; bytes = ((size_t)P.rows + 1) * 4; break;
+      case 1: src = m.col_idx; bytes = m.nnz * 4; break;
+      case 2: src = m.values; bytes = m.nnz * vs; break;
+      default: src = which < 4 ? P.diag.ptr : P.diag_u.ptr; bytes = (size_t)P.rows * vs; break;
+    }
+    if (bytes) VCLGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, be->stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+  });
+}
+
 VCLGB_API vclgbStatus vclgbPrecondApply(vclgbBackend h, vclgbPrecond P, void *vec) {
   if (!h || !P || !vec) return VCLGB_INVALID_ARGUMENT;
   Backend *be = B(h);

@@ -36,10 +36,19 @@ void cuthill_mckee_perm(Backend &be, const Matrix &A, bool advanced, double a, u
 std::unique_ptr<Matrix> csr_permute(Backend &be, const Matrix &A, const uint32_t *d_perm);
 uint32_t csr_bandwidth(Backend &be, const Matrix &A);
 
-// preconditioners (precond.cu)
+// transpose of a CSR pattern: rows of the transpose list their source rows in
+// ascending order; map[k] = position in (rp, ci) of transposed entry k (adjoint.cu)
+void csr_transpose_pattern(Backend &be, uint32_t rows, uint32_t cols, uint64_t nnz,
+                           const uint32_t *rp, const uint32_t *ci, DevBuf &trp, DevBuf &tci,
+                           DevBuf &map);
+
+// preconditioners (precond.cu, chow_patel.cu)
 std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A);
 std::unique_ptr<Precond> row_scaling_create(Backend &be, const Matrix &A, uint32_t norm);
 std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_scheduling);
+std::unique_ptr<Precond> chow_patel_create(Backend &be, const Matrix &A, bool icc,
+                                           uint32_t sweeps, uint32_t jacobi_iters);
+void chow_patel_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);
 // z = M^-1 z in place; skipped on the device when *skip_flag != 0
 void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);
 // diag(A) into a device buffer of the matrix precision; returns 1 in *zero_found

@@ -538,6 +538,10 @@ static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *s
 }
 
 void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag) {
+  if (P.kind == 3 || P.kind == 4) {
+    chow_patel_apply(be, P, d_vec, skip_flag);
+    return;
+  }
   if (P.kind == 1) {
     int g = waves_grid(be, 256, 8, P.rows);
     if (P.prec == VCLGB_FLOAT64)

@@ -300,7 +300,7 @@ struct Matrix {
 };
 
 struct Precond {
-  int kind = 0;  // 1 jacobi, 2 ilu0
+  int kind = 0;  // 1 jacobi / row scaling, 2 ilu0, 3 Chow-Patel ILU, 4 Chow-Patel ICC
   vclgbPrecision prec = VCLGB_FLOAT64;
   uint32_t rows = 0;
   DevBuf diag;   // jacobi: diag(A); ilu0: U diagonal
@@ -315,6 +315,12 @@ struct Precond {
     std::vector<uint32_t> h_level_ptr;
     DevBuf level_ptr, row_index, row_ptr, cols, vals;
   } L, U;
+  // Chow-Patel: I - D_L^-1 L and I - D_U^-1 U (ICC: U = L^T) without their
+  // diagonal entries, which the reference stores as zeros; diag = D_L,
+  // diag_u = D_U (ICC: D_L); four work vectors for the apply
+  std::unique_ptr<Matrix> cp_l, cp_u;
+  DevBuf diag_u, work;
+  uint32_t sweeps = 0, jacobi_iters = 0;
 };
 
 // ---------------------------------------------------------------------------

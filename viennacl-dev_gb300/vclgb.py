@@ -56,6 +56,12 @@ class SolverTag(ctypes.Structure):
                 ("error", ctypes.c_double)]
 
 
+class ChowPatelInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("sweeps", ctypes.c_uint32),
+                ("jacobi_iters", ctypes.c_uint32), ("nnz_L", ctypes.c_uint64),
+                ("nnz_U", ctypes.c_uint64)]
+
+
 class Ilu0Info(ctypes.Structure):
     _fields_ = [("num_levels_L", ctypes.c_uint32), ("num_levels_U", ctypes.c_uint32),
                 ("rows_L", ctypes.c_uint64), ("rows_U", ctypes.c_uint64),
@@ -121,6 +127,10 @@ SIGNATURES = {
     "vclgbPrecondDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbIlu0GetInfo": (_I32, [_P, ctypes.POINTER(Ilu0Info)]),
     "vclgbIlu0Export": (_I32, [_P, _P, _I32, _P]),
+    "vclgbChowPatelIluCreate": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
+    "vclgbChowPatelIccCreate": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
+    "vclgbChowPatelGetInfo": (_I32, [_P, ctypes.POINTER(ChowPatelInfo)]),
+    "vclgbChowPatelExport": (_I32, [_P, _P, _I32, _P]),
     "vclgbSolverTagInit": (None, [ctypes.POINTER(SolverTag), _I32]),
     "vclgbSolveCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
     "vclgbSolveBiCGStab": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
@@ -668,6 +678,60 @@ class ilu0_precond(_Precond):
         out = torch.empty(max(int(count), 1), dtype=dtype, device="cuda")
         self.be.check(self.be.lib.vclgbIlu0Export(self.be.h, self.h, which, _ptr(out)))
         return out[:int(count)]
+
+
+class chow_patel_tag:
+    """chow_patel_tag(num_sweeps=3, num_jacobi_iters=2) (chow_patel_ilu.hpp:44-70)."""
+
+    def __init__(self, num_sweeps=3, num_jacobi_iters=2):
+        self._sweeps = int(num_sweeps)
+        self._iters = int(num_jacobi_iters)
+
+    def sweeps(self, num=None):
+        if num is None:
+            return self._sweeps
+        self._sweeps = int(num)
+
+    def jacobi_iters(self, num=None):
+        if num is None:
+            return self._iters
+        self._iters = int(num)
+
+
+class _ChowPatel(_Precond):
+    _create = None
+
+    def __init__(self, A, tag=None):
+        tag = tag or chow_patel_tag()
+        super().__init__(A, getattr(load_library(), self._create), tag.sweeps(),
+                         tag.jacobi_iters())
+
+    def info(self):
+        inf = ChowPatelInfo()
+        self.be.check(self.be.lib.vclgbChowPatelGetInfo(self.h, ctypes.byref(inf)))
+        return inf
+
+    def export(self, which):
+        """0..3: L row_ptr, cols, values (I - D_L^-1 L without its diagonal), D_L;
+        4..7: the same for U (ICC: L^T)."""
+        torch = _torch()
+        inf = self.info()
+        n = self._A.size1()
+        count = [n + 1, inf.nnz_L, inf.nnz_L, n, n + 1, inf.nnz_U, inf.nnz_U, n][which]
+        dtype = torch.int32 if which % 4 in (0, 1) else self._A.dtype
+        out = torch.empty(max(int(count), 1), dtype=dtype, device="cuda")
+        self.be.check(self.be.lib.vclgbChowPatelExport(self.be.h, self.h, which, _ptr(out)))
+        return out[:int(count)]
+
+
+class chow_patel_ilu_precond(_ChowPatel):
+    """chow_patel_ilu_precond<compressed_matrix>(A, chow_patel_tag()) (Chow-Patel parallel ILU0)."""
+    _create = "vclgbChowPatelIluCreate"
+
+
+class chow_patel_icc_precond(_ChowPatel):
+    """chow_patel_icc_precond<compressed_matrix>(A, chow_patel_tag()) (Chow-Patel parallel IC0)."""
+    _create = "vclgbChowPatelIccCreate"
 
 
 def solve(A, b, tag, precond=None, x=None):
