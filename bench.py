@@ -394,6 +394,7 @@ def secondaries(V, torch, peak, args):
     sec["diffusion3d_192_mixed_vs_plain"] = res
     del A, P
     sec["ilu0_convdiff2d_512"] = bench_ilu0(V, torch)
+    sec["chow_patel"] = bench_chow_patel(V, torch, peak)
     sec["batched_4096"] = bench_batched(V, torch)
     sec["adjoint_diffusion2d_512"] = bench_adjoint(V, torch)
     # the reference's CPU-runnable case: 256^2 Laplacian, Jacobi-PCG to 1e-8
@@ -440,6 +441,78 @@ def bench_ilu0(V, torch):
         torch.cuda.synchronize()
         out[name] = {"s": time.time() - t0, "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
                      "true_rel_residual": true_rel_residual(rp, ci, v, x.cpu().numpy(), b)}
+    return out
+
+
+def bench_chow_patel(V, torch, peak):
+    """Chow-Patel preconditioners, default tag (3 sweeps, 2 Jacobi steps):
+    ILU on the 512^2 convection-diffusion matrix (setup, apply with its
+    algorithmic bytes, BiCGStab to 1e-10) and IC0 on the 128^3 Laplacian
+    (CG to 1e-10 against the pipelined CG without a preconditioner)."""
+    out = {}
+    rp, ci, v = gen.convdiff2d(512, 512, peclet=10.0, shift=0.01)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 5)
+    A = V.compressed_matrix(rp, ci, v)
+    bd = torch.tensor(b, device="cuda")
+    V.chow_patel_ilu_precond(A)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    P = V.chow_patel_ilu_precond(A)
+    torch.cuda.synchronize()
+    t_setup = time.time() - t0
+    inf = P.info()
+    z = bd.clone()
+    t_apply = time_events(lambda: P.apply(z), 20)
+    # div: v, D_L read, b_L written; per Jacobi step: N (12 B/entry + row_ptr),
+    # x and b read, x written; the last L step also reads D_U
+    steps = 2
+    nb = inf.nnz_L * 12 + inf.nnz_U * 12 + 2 * (n + 1) * 4
+    apply_bytes = 24 * n + steps * nb + 2 * steps * 24 * n + 8 * n
+    r = {"rows": n, "setup_s": t_setup, "nnz_L": int(inf.nnz_L), "nnz_U": int(inf.nnz_U),
+         "apply_us": t_apply * 1e6, "apply_bytes": int(apply_bytes),
+         "apply_GBs": apply_bytes / t_apply / 1e9,
+         "apply_frac_of_peak": apply_bytes / t_apply / 1e9 / peak}
+    tag = V.bicgstab_tag(1e-10, 5000)
+    V.solve(A, bd, V.bicgstab_tag(1e-10, 5000), P)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    x = V.solve(A, bd, tag, P)
+    torch.cuda.synchronize()
+    r["bicgstab"] = {"s": time.time() - t0, "iters": tag.iters(),
+                     "status": V.STATUS_NAMES[tag.status()],
+                     "true_rel_residual": true_rel_residual(rp, ci, v, x.cpu().numpy(), b)}
+    out["ilu_convdiff2d_512"] = r
+    del A, P
+    rp, ci, v = gen.laplace3d(128)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 1)
+    A = V.compressed_matrix(rp, ci, v)
+    bd = torch.tensor(b, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.time()
+    P = V.chow_patel_icc_precond(A)
+    torch.cuda.synchronize()
+    r = {"rows": n, "setup_s": time.time() - t0}
+    inf = P.info()
+    z = bd.clone()
+    t_apply = time_events(lambda: P.apply(z), 20)
+    nb = inf.nnz_L * 12 + inf.nnz_U * 12 + 2 * (n + 1) * 4
+    apply_bytes = 24 * n + steps * nb + 2 * steps * 24 * n + 8 * n
+    r.update(apply_us=t_apply * 1e6, apply_bytes=int(apply_bytes),
+             apply_GBs=apply_bytes / t_apply / 1e9,
+             apply_frac_of_peak=apply_bytes / t_apply / 1e9 / peak)
+    for name, pc in (("cg_ic0", P), ("cg_pipelined", None)):
+        tag = V.cg_tag(1e-10, 5000)
+        V.solve(A, bd, V.cg_tag(1e-10, 5000), pc)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        x = V.solve(A, bd, tag, pc)
+        torch.cuda.synchronize()
+        r[name] = {"s": time.time() - t0, "iters": tag.iters(),
+                   "status": V.STATUS_NAMES[tag.status()],
+                   "true_rel_residual": true_rel_residual(rp, ci, v, x.cpu().numpy(), b)}
+    out["ic0_laplace3d_128"] = r
     return out
 
 
