@@ -270,6 +270,17 @@ VCLGB_API vclgbStatus vclgbRowScalingCreate(vclgbBackend be, vclgbMatrix A, uint
  * the device with the reference's elimination order (detail/ilu/common.hpp:50-187). */
 VCLGB_API vclgbStatus vclgbIlu0Create(vclgbBackend be, vclgbMatrix A, int use_level_scheduling,
                                       vclgbPrecond *out);
+/* block_ilu_precond<compressed_matrix, ilu0_tag>(A, ilu0_tag(), num_blocks) and the
+ * block_boundaries constructor (linalg/detail/ilu/block_ilu.hpp:301-365): ILU0 of A
+ * restricted to its diagonal blocks, factorised and applied on the device as
+ * ilu0_precond is (vclgbIlu0GetInfo / vclgbIlu0Export work on it; the factors
+ * lie in the block-diagonal pattern and equal the reference's per-block
+ * factors).  h_bounds NULL: the reference's split [i*rows/num_blocks,
+ * (i+1)*rows/num_blocks); else 2*num_blocks host values [start, stop) that must
+ * tile [0, rows) (VCLGB_INVALID_ARGUMENT otherwise).  The reference's apply skips
+ * the last column of U (its U^T row pointer ends at 0); this one applies it. */
+VCLGB_API vclgbStatus vclgbBlockIlu0Create(vclgbBackend be, vclgbMatrix A, uint32_t num_blocks,
+                                           const uint32_t *h_bounds, vclgbPrecond *out);
 /* chow_patel_ilu_precond<compressed_matrix>(A, chow_patel_tag(sweeps, jacobi_iters))
  * and chow_patel_icc_precond (linalg/detail/ilu/chow_patel_ilu.hpp:44-70 tag,
  * :77-150 setup, :170-300 apply; reference defaults sweeps 3, jacobi_iters 2).

@@ -98,6 +98,8 @@ def lib():
         L.vo_chow_patel_icc_d.argtypes = [_U32, _u32p, _u32p, _f64p, _U32, _u32p, _u32p, _f64p,
                                           _u32p, _u32p, _f64p, _f64p]
         L.vo_precond_apply_d.argtypes = [_U32, ctypes.c_void_p, _f64p]
+        L.vo_block_ilu0_apply_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p]
+        L.vo_set_block_ilu_host_quirk.argtypes = [_I]
         L.vo_level_setup_d.argtypes = [_U32, _u32p, _u32p, _f64p, ctypes.c_void_p, _I,
                                        ctypes.POINTER(_SZ), ctypes.POINTER(_SZ), ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -250,6 +252,11 @@ def _precond(kind, rp=None, ci=None, v=None):
         sweeps, iters = (int(parts[1]), int(parts[2])) if len(parts) == 3 else (3, 2)
         F = (chow_patel_ilu if parts[0] == "cpilu" else chow_patel_icc)(rp, ci, v, sweeps)
         return _cp_struct(F, iters)
+    if kind.startswith("bilu"):
+        B = block_ilu0(rp, ci, v, num_blocks=int(kind[4:]))
+        P.kind = 4
+        P.rp, P.ci, P.lu = B["rp"].ctypes.data, B["ci"].ctypes.data, B["lu"].ctypes.data
+        return P, [B]
     P.kind = {"none": 0, "jacobi": 1, "ilu0": 2, "row0": 1, "row1": 1, "row2": 1}[kind]
     keep = []
     if kind == "jacobi" or kind.startswith("row"):
@@ -345,6 +352,44 @@ def ilu0_apply(rp, ci, v, vec):
     z = level_substitute(L, vec)
     z = z / ud
     return level_substitute(U, z)
+
+
+def block_bounds(n, num_blocks):
+    """block_ilu_precond's default split (block_ilu.hpp:325-333): [i n / N, (i+1) n / N)."""
+    return [((i * n) // num_blocks, ((i + 1) * n) // num_blocks) for i in range(num_blocks)]
+
+
+def block_ilu0(rp, ci, v, bounds=None, num_blocks=8):
+    """block_ilu_precond<compressed_matrix, ilu0_tag> setup (block_ilu.hpp:322-365,
+    extract_block_matrix :69-113): A restricted to its diagonal blocks (entries
+    whose column lies outside the row's block dropped, order kept), factorised by
+    ILU0 -- the per-block factorisations, stored side by side."""
+    n = len(rp) - 1
+    bounds = block_bounds(n, num_blocks) if bounds is None else bounds
+    rp64 = np.asarray(rp, np.int64)
+    rows = np.repeat(np.arange(n), np.diff(rp64))
+    lo, hi = np.zeros(n, np.int64), np.zeros(n, np.int64)
+    for a, b in bounds:
+        lo[a:b], hi[a:b] = a, b
+    c = np.asarray(ci, np.int64)
+    keep = (c >= lo[rows]) & (c < hi[rows])
+    brp = np.zeros(n + 1, np.uint32)
+    np.cumsum(np.bincount(rows[keep], minlength=n), out=brp[1:])
+    bci = np.ascontiguousarray(np.asarray(ci, np.uint32)[keep])
+    bv = np.asarray(v, np.float64)[keep]
+    return {"rp": brp, "ci": bci if len(bci) else np.zeros(1, np.uint32),
+            "lu": ilu0_factor(brp, bci, bv) if len(bv) else np.zeros(1), "nnz": int(keep.sum())}
+
+
+def set_block_ilu_host_quirk(on):
+    """Reproduce the reference apply's skipped last column of U (pinning only)."""
+    lib().vo_set_block_ilu_host_quirk(int(bool(on)))
+
+
+def block_ilu0_apply(B, vec):
+    vec = _c(vec, np.float64).copy()
+    lib().vo_block_ilu0_apply_d(len(vec), B["rp"], B["ci"], _c(B["lu"], np.float64), vec)
+    return vec
 
 
 def chow_patel_ilu(rp, ci, v, sweeps=3):

@@ -330,6 +330,13 @@ int main(int argc, char **argv) {
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag, P);
         t1 = now();
+      } else if (pc.compare(0, 4, "bilu") == 0) {
+        viennacl::linalg::block_ilu_precond<viennacl::compressed_matrix<double>,
+                                            viennacl::linalg::ilu0_tag>
+            P(M, viennacl::linalg::ilu0_tag(), static_cast<std::size_t>(std::atol(pc.c_str() + 4)));
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
       } else if (pc == "cpicc") {
         viennacl::linalg::chow_patel_icc_precond<viennacl::compressed_matrix<double> > P(
             M, viennacl::linalg::chow_patel_tag());
@@ -360,6 +367,13 @@ int main(int argc, char **argv) {
       } else if (pc == "cpilu") {
         viennacl::linalg::chow_patel_ilu_precond<viennacl::compressed_matrix<double> > P(
             M, viennacl::linalg::chow_patel_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc.compare(0, 4, "bilu") == 0) {
+        viennacl::linalg::block_ilu_precond<viennacl::compressed_matrix<double>,
+                                            viennacl::linalg::ilu0_tag>
+            P(M, viennacl::linalg::ilu0_tag(), static_cast<std::size_t>(std::atol(pc.c_str() + 4)));
         t0 = now();
         x = viennacl::linalg::solve(M, b, tag, P);
         t1 = now();
@@ -461,6 +475,29 @@ int main(int argc, char **argv) {
       h = from_vcl(z);
       save("cp_icc_z.f64", h.data(), n);
     }
+  } else if (cmd == "block_ilu") {  // args: num_blocks -> bilu_lu.f64 (blocks' LU side by side), bilu_z.f64
+    std::size_t nb = static_cast<std::size_t>(std::atol(argv[3]));
+    viennacl::compressed_matrix<double> M;
+    fill_matrix(A, M);
+    std::vector<double> lu_all;
+    for (std::size_t i = 0; i < nb; ++i) {
+      std::size_t s0 = (i * n) / nb, s1 = ((i + 1) * n) / nb;
+      std::size_t bnnz = A.rp[s1] - A.rp[s0];
+      viennacl::compressed_matrix<double> blk(s1 - s0, s1 - s0, bnnz);
+      viennacl::linalg::detail::extract_block_matrix(M, blk, s0, s1);
+      viennacl::linalg::precondition(blk, viennacl::linalg::ilu0_tag());
+      double const *e = raw<double>(blk.handle());
+      lu_all.insert(lu_all.end(), e, e + raw<unsigned>(blk.handle1())[s1 - s0]);
+    }
+    save("bilu_lu.f64", lu_all.data(), lu_all.size());
+    viennacl::linalg::block_ilu_precond<viennacl::compressed_matrix<double>, viennacl::linalg::ilu0_tag>
+        P(M, viennacl::linalg::ilu0_tag(), nb);
+    std::vector<double> bh = load<double>("b.f64", n);
+    viennacl::vector<double> z(n);
+    to_vcl(bh, z);
+    P.apply(z);
+    std::vector<double> zh = from_vcl(z);
+    save("bilu_z.f64", zh.data(), n);
   } else if (cmd == "row_norms") {  // -> norm0.f64, norm1.f64, norm2.f64 (row_info)
     viennacl::compressed_matrix<double> M;
     fill_matrix(A, M);

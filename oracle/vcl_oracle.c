@@ -446,6 +446,40 @@ static void vo_ilu0_solve(vo_u32 n, const vo_precond *P, double *vec) {
 
 /* jacobi_precond::apply = element_div(vec, diag) -- jacobi_precond.hpp:121-126 */
 /* ------------------------------------------------------------------------ */
+/* block ILU0: block_ilu_precond<compressed_matrix, ilu0_tag>                */
+/* (linalg/detail/ilu/block_ilu.hpp:322-573) keeps each block's LU as both   */
+/* L and U, moves it into L^T / U^T / D and solves column by column          */
+/* (host_based/sparse_matrix_operations.hpp:868-896, 968-1000).  Restated    */
+/* by rows: x_r -= x_c l_rc for c < r ascending, then from the last row up   */
+/* x_r -= x_c u_rc for c > r descending and x_r /= d_r -- the same           */
+/* operations in the same order as the column sweeps.                        */
+/* ------------------------------------------------------------------------ */
+/* The reference never writes U^T's last row pointer (the exclusive scans of
+ * block_ilu.hpp:460-475 stop at size1 - 1 and reserve() leaves the end at 0),
+ * so its column sweep skips U's last column.  The quirk switch reproduces that
+ * to pin this restatement against the reference's outputs; off (the default),
+ * every entry of U is applied, as the engine does. */
+static int vo_block_ilu_quirk = 0;
+void vo_set_block_ilu_host_quirk(int on) { vo_block_ilu_quirk = on; }
+
+void vo_block_ilu0_apply_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *lu,
+                           double *vec) {
+  const vo_u32 skip_col = vo_block_ilu_quirk && n ? n - 1 : 0xffffffffu;
+  for (vo_u32 r = 0; r < n; ++r)
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j)
+      if (ci[j] < r) vec[r] -= vec[ci[j]] * lu[j];
+  for (vo_u32 r2 = 0; r2 < n; ++r2) {
+    vo_u32 r = n - 1 - r2;
+    double d = 0; /* D stays 0 for a row without a diagonal entry */
+    for (vo_u32 j = rp[r]; j < rp[r + 1]; ++j)
+      if (ci[j] == r) d = lu[j];
+    for (vo_u32 j = rp[r + 1]; j > rp[r]; --j)
+      if (ci[j - 1] > r && ci[j - 1] != skip_col) vec[r] -= vec[ci[j - 1]] * lu[j - 1];
+    vec[r] = vec[r] / d;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Chow-Patel parallel ILU0 / ICC0: linalg/detail/ilu/chow_patel_ilu.hpp     */
 /* (setup :77-150, apply :190-222 and :269-300) over the host kernels of     */
 /* linalg/host_based/ilu_operations.hpp.  Sweeps read the previous sweep's  */
@@ -682,6 +716,8 @@ void vo_precond_apply_d(vo_u32 n, const vo_precond *P, double *vec) {
     vo_ilu0_solve(n, P, vec);
   } else if (P->kind == VO_PRECOND_CHOW_PATEL) {
     vo_cp_apply(n, P, vec);
+  } else if (P->kind == VO_PRECOND_BLOCK_ILU0) {
+    vo_block_ilu0_apply_d(n, P->rp, P->ci, P->lu, vec);
   }
 }
 

@@ -91,7 +91,8 @@ typedef struct {
   double   error;               /* out: the solver's own estimate */
 } vo_tag;
 
-enum { VO_PRECOND_NONE = 0, VO_PRECOND_JACOBI = 1, VO_PRECOND_ILU0 = 2, VO_PRECOND_CHOW_PATEL = 3 };
+enum { VO_PRECOND_NONE = 0, VO_PRECOND_JACOBI = 1, VO_PRECOND_ILU0 = 2, VO_PRECOND_CHOW_PATEL = 3,
+       VO_PRECOND_BLOCK_ILU0 = 4 };
 
 typedef struct {
   int            kind;
@@ -148,6 +149,14 @@ size_t vo_level_setup_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const doub
 void vo_level_substitute_d(size_t nlev, const vo_u32 *level_ptr, const vo_u32 *row_index,
                            const vo_u32 *row_ptr, const vo_u32 *cols, const double *vals,
                            double *vec);
+
+/* ---- block ILU0 ---------------------------------------------------------- */
+/* block_ilu_precond<compressed_matrix, ilu0_tag>::apply: rp/ci/lu hold the
+ * ILU0 factors of A's block-diagonal part (columns ascending in every row). */
+void vo_block_ilu0_apply_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *lu,
+                           double *vec);
+/* 1: skip U's last column as the reference's apply does (pinning only) */
+void vo_set_block_ilu_host_quirk(int on);
 
 /* ---- Chow-Patel ILU / ICC ----------------------------------------------- */
 /* Entries of A with col <= row (L) and col >= row (U). */

@@ -6,7 +6,7 @@ tree nor a particular numpy random stream.
 
 Run from the repository root:  python tests/golden/make_golden.py
 (python tests/golden/make_golden.py coo | row_scaling | matrix_market | cuthill_mckee |
- chow_patel writes only
+ chow_patel | block_ilu writes only
 that fixture; matrix_market also writes the input files under tests/golden/mm/)
 GMRES fixtures are produced with OMP_NUM_THREADS=1 (the host stage-1 kernel's
 result depends on the thread count).
@@ -144,6 +144,7 @@ def main():
     mm_fixture()
     cm_fixture()
     chow_patel_fixture()
+    block_ilu_fixture()
 
 
 def coo_fixture():
@@ -351,6 +352,23 @@ def chow_patel_fixture():
     save("chow_patel.npz", cp=cp, cc=cc, cv=cv, sp=sp, sc=sc, sv=sv, **res)
 
 
+def block_ilu_fixture():
+    """block_ilu_precond<compressed_matrix, ilu0_tag> with 1, 8 and 37 blocks
+    (the default split, n not divisible by the count) on a convection-diffusion
+    matrix: the blocks' ILU0 factors side by side and the apply; BiCGStab
+    preconditioned by it (8 blocks)."""
+    rp, ci, v = gen.convdiff2d(29, 23, peclet=10.0, shift=0.02)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 47)
+    res = {}
+    for nb in (1, 8, 37):
+        out = oracle.run_ref("block_ilu", rp, ci, v, args=(nb,), b=b)
+        res["lu_%d" % nb], res["z_%d" % nb] = out["bilu_lu"], out["bilu_z"]
+    s = oracle.run_ref("bicgstab", rp, ci, v, args=(1e-10, 2000, "bilu8"), b=b)
+    save("block_ilu.npz", rp=rp, ci=ci, v=v, b=b, x_bicgstab_bilu8=s["x"],
+         iters_bicgstab_bilu8=s["iters"], error_bicgstab_bilu8=s["error"], **res)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["coo"]:
         coo_fixture()
@@ -358,6 +376,8 @@ if __name__ == "__main__":
         row_scaling_fixture()
     elif sys.argv[1:] == ["chow_patel"]:
         chow_patel_fixture()
+    elif sys.argv[1:] == ["block_ilu"]:
+        block_ilu_fixture()
     elif sys.argv[1:] == ["matrix_market"]:
         mm_fixture()
     elif sys.argv[1:] == ["cuthill_mckee"]:

@@ -113,6 +113,42 @@ def test_chow_patel_solves_golden(golden):
         oracle.set_threads(oracle.max_threads())
 
 
+@pytest.mark.parametrize("nb", [1, 8, 37])
+def test_block_ilu_golden(golden, nb):
+    # block_ilu_precond<compressed_matrix, ilu0_tag>: the blocks' factors
+    # bit-exact; the apply bit-exact with the reference's skipped last column
+    # of U reproduced, and different from it only through that column without
+    d = golden("block_ilu.npz")
+    B = oracle.block_ilu0(d["rp"], d["ci"], d["v"], num_blocks=nb)
+    assert np.array_equal(B["lu"][:B["nnz"]], d["lu_%d" % nb])
+    oracle.set_block_ilu_host_quirk(True)
+    try:
+        assert np.array_equal(oracle.block_ilu0_apply(B, d["b"]), d["z_%d" % nb])
+    finally:
+        oracle.set_block_ilu_host_quirk(False)
+    z = oracle.block_ilu0_apply(B, d["b"])
+    assert not np.array_equal(z, d["z_%d" % nb])
+    # zeroing U's last column reproduces the reference exactly
+    n = len(d["rp"]) - 1
+    rows = np.repeat(np.arange(n), np.diff(B["rp"].astype(np.int64)))
+    lu = B["lu"][:B["nnz"]].copy()
+    lu[(B["ci"][:B["nnz"]] == n - 1) & (rows < n - 1)] = 0.0
+    assert np.array_equal(oracle.block_ilu0_apply(dict(B, lu=lu), d["b"]), d["z_%d" % nb])
+
+
+def test_block_ilu_solve_golden(golden):
+    d = golden("block_ilu.npz")
+    oracle.set_threads(1)
+    oracle.set_block_ilu_host_quirk(True)
+    try:
+        x, it, err = oracle.solve("bicgstab", d["rp"], d["ci"], d["v"], d["b"], 1e-10, 2000, "bilu8")
+        assert it == int(d["iters_bicgstab_bilu8"]) and err == float(d["error_bicgstab_bilu8"])
+        assert rel_err(x, d["x_bicgstab_bilu8"]) < 1e-12
+    finally:
+        oracle.set_block_ilu_host_quirk(False)
+        oracle.set_threads(oracle.max_threads())
+
+
 MM_CASES = [("general", 1), ("general_case", 1), ("symmetric", 1), ("pattern", 1), ("complex", 1),
             ("zero_based", 0), ("extra_lines", 1), ("bad_word", 1), ("bad_field", 1),
             ("bad_symmetry", 1), ("array", 1), ("out_of_range", 1), ("too_few", 1),

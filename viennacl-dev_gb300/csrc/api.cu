@@ -568,6 +568,17 @@ VCLGB_API vclgbStatus vclgbIlu0Create(vclgbBackend h, vclgbMatrix A, int lvl, vc
   });
 }
 
+VCLGB_API vclgbStatus vclgbBlockIlu0Create(vclgbBackend h, vclgbMatrix A, uint32_t num_blocks,
+                                           const uint32_t *h_bounds, vclgbPrecond *out) {
+  if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    auto P = block_ilu0_create(*be, *M(A), num_blocks, h_bounds);
+    VCLGB_CUDA(cudaStreamSynchronize(be->stream));
+    *out = reinterpret_cast<vclgbPrecond>(P.release());
+  });
+}
+
 static vclgbStatus chow_patel_create_api(vclgbBackend h, vclgbMatrix A, bool icc, uint32_t sweeps,
                                          uint32_t iters, vclgbPrecond *out) {
   if (!h || !A || !out) return VCLGB_INVALID_ARGUMENT;

@@ -46,6 +46,8 @@ void csr_transpose_pattern(Backend &be, uint32_t rows, uint32_t cols, uint64_t n
 std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A);
 std::unique_ptr<Precond> row_scaling_create(Backend &be, const Matrix &A, uint32_t norm);
 std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_scheduling);
+std::unique_ptr<Precond> block_ilu0_create(Backend &be, const Matrix &A, uint32_t num_blocks,
+                                           const uint32_t *h_bounds);
 std::unique_ptr<Precond> chow_patel_create(Backend &be, const Matrix &A, bool icc,
                                            uint32_t sweeps, uint32_t jacobi_iters);
 void chow_patel_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);

@@ -419,6 +419,131 @@ std::unique_ptr<Precond> ilu0_create(Backend &be, const Matrix &A, bool level_sc
   return P;
 }
 
+// ---------------------------------------------------------------------------
+// block_ilu_precond<compressed_matrix, ilu0_tag> (linalg/detail/ilu/block_ilu.hpp:
+// 322-365, extract_block_matrix :69-113): ILU0 of A restricted to its diagonal
+// blocks.  The reference factorises every block on the host and solves block
+// by block; here the block-diagonal part of A (an entry whose column lies
+// outside its row's block is dropped, order kept) goes through the device
+// ILU0 above.  A row's elimination never leaves its block, so the factors are
+// the reference's per-block factors side by side, bit for bit, and the level
+// schedule runs all blocks at once.  `starts` holds the blocks' first rows and
+// n at the end; the blocks tile [0, n).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_of_row(uint32_t r, const uint32_t *starts, uint32_t nb,
+                                             uint32_t &lo, uint32_t &hi) {
+  uint32_t a = 0, b = nb;  // last block whose start is <= r (empty blocks skipped)
+  while (a + 1 < b) {
+    const uint32_t m = (a + b) / 2;
+    if (starts[m] <= r) a = m; else b = m;
+  }
+  lo = starts[a];
+  hi = starts[a + 1];
+}
+
+__global__ void block_count_kernel(uint32_t n, const uint32_t *__restrict__ rp,
+                                   const uint32_t *__restrict__ ci,
+                                   const uint32_t *__restrict__ starts, uint32_t nb,
+                                   uint32_t *cnt) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (size_t)gridDim.x * blockDim.x) {
+    uint32_t lo, hi, c = 0;
+    block_of_row((uint32_t)r, starts, nb, lo, hi);
+    for (uint32_t j = rp[r]; j < rp[r + 1]; ++j) c += ci[j] >= lo && ci[j] < hi;
+    cnt[r] = c;
+  }
+}
+
+template <typename W>
+__global__ void block_fill_kernel(uint32_t n, const uint32_t *__restrict__ rp,
+                                  const uint32_t *__restrict__ ci, const W *__restrict__ v,
+                                  const uint32_t *__restrict__ starts, uint32_t nb,
+                                  const uint32_t *__restrict__ brp, uint32_t *bci, W *bv) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (size_t)gridDim.x * blockDim.x) {
+    uint32_t lo, hi, k = brp[r];
+    block_of_row((uint32_t)r, starts, nb, lo, hi);
+    for (uint32_t j = rp[r]; j < rp[r + 1]; ++j)
+      if (ci[j] >= lo && ci[j] < hi) {
+        bci[k] = ci[j];
+        bv[k] = v[j];
+        ++k;
+      }
+  }
+}
+
+std::unique_ptr<Precond> block_ilu0_create(Backend &be, const Matrix &A, uint32_t num_blocks,
+                                           const uint32_t *h_bounds) {
+  require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "block_ilu_precond is built from CSR");
+  require(A.rows == A.cols, VCLGB_INVALID_ARGUMENT, "block ILU needs a square matrix");
+  require(num_blocks > 0, VCLGB_INVALID_ARGUMENT, "block ILU needs at least one block");
+  const uint32_t n = A.rows;
+  std::vector<uint32_t> starts(num_blocks + 1);
+  if (!h_bounds) {
+    // the reference's default split (block_ilu.hpp:325-333)
+    for (uint32_t i = 0; i <= num_blocks; ++i)
+      starts[i] = (uint32_t)(((uint64_t)i * n) / num_blocks);
+  } else {
+    std::vector<std::pair<uint32_t, uint32_t>> b(num_blocks);
+    for (uint32_t i = 0; i < num_blocks; ++i) b[i] = {h_bounds[2 * i], h_bounds[2 * i + 1]};
+    std::sort(b.begin(), b.end());
+    // rows outside every block would be divided by a zero D in the reference's
+    // apply; blocks that overlap would be solved twice: both are rejected
+    uint32_t at = 0;
+    for (uint32_t i = 0; i < num_blocks; ++i) {
+      require(b[i].first == at && b[i].second >= b[i].first, VCLGB_INVALID_ARGUMENT,
+              "block boundaries must tile [0, rows) without gaps or overlaps");
+      starts[i] = at;
+      at = b[i].second;
+    }
+    require(at == n, VCLGB_INVALID_ARGUMENT,
+            "block boundaries must tile [0, rows) without gaps or overlaps");
+    starts[num_blocks] = n;
+  }
+  auto m = std::make_unique<Matrix>();
+  m->format = VCLGB_CSR;
+  m->prec = A.prec;
+  m->rows = m->cols = n;
+  m->own_row_ptr.alloc(((size_t)n + 1) * 4, be.stream);
+  if (n) {
+    DevBuf d_starts, cnt(((size_t)n) * 4, be.stream);
+    upload(be, d_starts, starts);
+    const int g = waves_grid(be, 256, 8, n);
+    block_count_kernel<<<g, 256, 0, be.stream>>>(n, A.row_ptr, A.col_idx,
+                                                 d_starts.as<uint32_t>(), num_blocks,
+                                                 cnt.as<uint32_t>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+    m->nnz = extern_scan_u32(be, cnt.as<uint32_t>(), n, m->own_row_ptr.as<uint32_t>());
+    m->own_col_idx.alloc(std::max<uint64_t>(m->nnz, 1) * 4, be.stream);
+    m->own_values.alloc(std::max<uint64_t>(m->nnz, 1) * A.vsize(), be.stream);
+    if (A.vsize() == 8)
+      block_fill_kernel<uint64_t><<<g, 256, 0, be.stream>>>(
+          n, A.row_ptr, A.col_idx, static_cast<const uint64_t *>(A.values),
+          d_starts.as<uint32_t>(), num_blocks, m->own_row_ptr.as<uint32_t>(),
+          m->own_col_idx.as<uint32_t>(), m->own_values.as<uint64_t>());
+    else
+      block_fill_kernel<uint32_t><<<g, 256, 0, be.stream>>>(
+          n, A.row_ptr, A.col_idx, static_cast<const uint32_t *>(A.values),
+          d_starts.as<uint32_t>(), num_blocks, m->own_row_ptr.as<uint32_t>(),
+          m->own_col_idx.as<uint32_t>(), m->own_values.as<uint32_t>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // d_starts/cnt freed after use
+  } else {
+    VCLGB_CUDA(cudaMemsetAsync(m->own_row_ptr.ptr, 0, 4, be.stream));
+    m->own_col_idx.alloc(4, be.stream);
+    m->own_values.alloc(8, be.stream);
+  }
+  m->row_ptr = m->own_row_ptr.as<uint32_t>();
+  m->col_idx = m->own_col_idx.as<uint32_t>();
+  m->values = m->own_values.ptr;
+  auto P = ilu0_create(be, *m, true);
+  P->blocks = num_blocks;
+  P->owned = std::move(m);
+  return P;
+}
+
 // A run of consecutive levels of at most kRunLevel rows each, substituted by
 // one block of kRunLevel threads: a level is one pass of the block, and a
 // __syncthreads() (the block's own writes to vec are visible to it after the

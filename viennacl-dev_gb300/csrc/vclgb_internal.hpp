@@ -321,6 +321,9 @@ struct Precond {
   std::unique_ptr<Matrix> cp_l, cp_u;
   DevBuf diag_u, work;
   uint32_t sweeps = 0, jacobi_iters = 0;
+  // block ILU0: the block-diagonal part of A, whose pattern the factors borrow
+  std::unique_ptr<Matrix> owned;
+  uint32_t blocks = 0;
 };
 
 // ---------------------------------------------------------------------------

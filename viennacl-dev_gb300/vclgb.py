@@ -127,6 +127,7 @@ SIGNATURES = {
     "vclgbPrecondDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbIlu0GetInfo": (_I32, [_P, ctypes.POINTER(Ilu0Info)]),
     "vclgbIlu0Export": (_I32, [_P, _P, _I32, _P]),
+    "vclgbBlockIlu0Create": (_I32, [_P, _P, _U32, _P, ctypes.POINTER(_P)]),
     "vclgbChowPatelIluCreate": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
     "vclgbChowPatelIccCreate": (_I32, [_P, _P, _U32, _U32, ctypes.POINTER(_P)]),
     "vclgbChowPatelGetInfo": (_I32, [_P, ctypes.POINTER(ChowPatelInfo)]),
@@ -678,6 +679,22 @@ class ilu0_precond(_Precond):
         out = torch.empty(max(int(count), 1), dtype=dtype, device="cuda")
         self.be.check(self.be.lib.vclgbIlu0Export(self.be.h, self.h, which, _ptr(out)))
         return out[:int(count)]
+
+
+class block_ilu_precond(ilu0_precond):
+    """block_ilu_precond<compressed_matrix, ilu0_tag>(A, ilu0_tag(), num_blocks) or
+    (A, ilu0_tag(), block_boundaries=[(start, stop), ...])."""
+
+    def __init__(self, A, tag=None, num_blocks=8, block_boundaries=None):
+        if block_boundaries is not None:
+            num_blocks = len(block_boundaries)
+            self._bounds = np.ascontiguousarray(
+                np.asarray(block_boundaries, dtype=np.uint32).reshape(-1))
+            bp = _P(self._bounds.ctypes.data) if self._bounds.size else _P(0)
+        else:
+            bp = _P(0)
+        self.num_blocks = int(num_blocks)
+        _Precond.__init__(self, A, load_library().vclgbBlockIlu0Create, int(num_blocks), bp)
 
 
 class chow_patel_tag:
