@@ -17,7 +17,10 @@
 // Apply: x = D^-1 v, then jacobi_iters steps x <- N x + D^-1 v per triangle.
 // A step is one SpMV over the strictly triangular Neumann matrix (the zero
 // diagonal the reference stores is left out) with "+ D^-1 v" -- and, closing
-// the L phase, the division by D_U that starts the U phase -- in its epilogue.
+// the L phase, the scaling by D_U^-1 that starts the U phase -- in its
+// epilogue.  The apply multiplies by reciprocals of D formed once at setup (an
+// FP64 division is a long software sequence on GB300), so it agrees with the
+// reference's divisions to rounding, like its fused multiply-add SpMV.
 #include <algorithm>
 
 #include "formats.hpp"
@@ -236,15 +239,27 @@ __global__ void cp_neumann_kernel(uint32_t n, const uint32_t *__restrict__ rp,
   }
 }
 
-// b = v / d (element_div), or (v / d) / d2 when a triangle takes no Jacobi step
+// the reciprocals of D_L and D_U, formed once so that the apply multiplies
 template <typename T>
-__global__ void cp_div_kernel(size_t n, const T *src, const T *__restrict__ d,
-                              const T *__restrict__ d2, T *dst, const int *skip) {
+__global__ void cp_recip_kernel(uint32_t n, const T *__restrict__ dl, const T *__restrict__ du,
+                                T *rl, T *ru) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    rl[i] = T(1) / dl[i];
+    ru[i] = T(1) / du[i];
+  }
+}
+
+// b = v D_L^-1 (element_div), or (v D_L^-1) D_U^-1 when a triangle takes no
+// Jacobi step; TWO is a template argument so that no path carries the other
+template <typename T, bool TWO>
+__global__ void cp_scale_kernel(size_t n, const T *src, const T *__restrict__ r1,
+                                const T *__restrict__ r2, T *dst, const int *skip) {
   if (skip && *skip) return;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    T b = src[i] / d[i];
-    if (d2) b = b / d2[i];
+    T b = src[i] * r1[i];
+    if (TWO) b = b * r2[i];
     dst[i] = b;
   }
 }
@@ -252,17 +267,19 @@ __global__ void cp_div_kernel(size_t n, const T *src, const T *__restrict__ d,
 }  // namespace
 
 // x_{k+1} = N x_k + D^-1 rhs (chow_patel_ilu.hpp:281-285): out = acc + rhs,
-// divided by d when the step closes the L phase (b_U = x_L / D_U)
-template <typename T>
+// times D_U^-1 when the step closes the L phase (b_U = x_L / D_U).  SCALE is a
+// template argument: as a runtime flag the compiler kept the scaling work in
+// every step.
+template <typename T, bool SCALE>
 struct EpiCpStep {
   static constexpr int NDOT = 0;
-  T *out; const T *rhs; const T *d; const int *flag;
-  struct Pre { T rhs, d; };
+  T *out; const T *rhs; const T *r; const int *flag;
+  struct Pre { T rhs, r; };
   __device__ bool skip() const { return flag && *flag; }
-  __device__ Pre pre(uint32_t i) const { return {rhs[i], d ? d[i] : T(1)}; }
+  __device__ Pre pre(uint32_t i) const { return {rhs[i], SCALE ? r[i] : T(1)}; }
   __device__ void row(uint32_t i, T acc, const Pre &p, T (&)[1]) const {
     const T v = acc + p.rhs;
-    out[i] = d ? v / p.d : v;
+    out[i] = SCALE ? v * p.r : v;
   }
   __device__ void finalize(const T (&)[1]) const {}
 };
@@ -406,7 +423,12 @@ static void cp_build(Backend &be, const Matrix &A, bool icc, Precond &P) {
   VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // temporaries freed after use
   csr_analyse(be, *P.cp_l);
   csr_analyse(be, *P.cp_u);
-  P.work.alloc(std::max<size_t>(n, 1) * vs * 4, be.stream);
+  P.work.alloc((size_t)n * vs * 6, be.stream);
+  T *w = P.work.as<T>();
+  cp_recip_kernel<T><<<g, 256, 0, be.stream>>>(n, P.diag.as<T>(), P.diag_u.as<T>(), w + 4 * (size_t)n,
+                                               w + 5 * (size_t)n);
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
 }
 
 std::unique_ptr<Precond> chow_patel_create(Backend &be, const Matrix &A, bool icc,
@@ -431,36 +453,40 @@ template <typename T>
 static void cp_apply(Backend &be, const Precond &P, T *vec, const int *skip) {
   const size_t n = P.rows;
   if (n == 0) return;
-  const T *dl = P.diag.as<T>(), *du = P.diag_u.as<T>();
   T *w = P.work.as<T>();
   T *bL = w, *bU = w + n, *x0 = w + 2 * n, *x1 = w + 3 * n;
+  const T *rl = w + 4 * n, *ru = w + 5 * n;  // D_L^-1, D_U^-1
   const int g = waves_grid(be, 256, 8, n);
   const uint32_t J = P.jacobi_iters;
   Reduction red{nullptr, nullptr};
   if (J == 0) {  // x_L = D_L^-1 v; result = D_U^-1 x_L
-    cp_div_kernel<T><<<g, 256, 0, be.stream>>>(n, vec, dl, du, vec, skip);
+    cp_scale_kernel<T, true><<<g, 256, 0, be.stream>>>(n, vec, rl, ru, vec, skip);
     be.launches++;
     VCLGB_CHECK_LAUNCH();
     return;
   }
-  cp_div_kernel<T><<<g, 256, 0, be.stream>>>(n, vec, dl, nullptr, bL, skip);
+  cp_scale_kernel<T, false><<<g, 256, 0, be.stream>>>(n, vec, rl, nullptr, bL, skip);
   be.launches++;
   VCLGB_CHECK_LAUNCH();
-  // L phase: x_1 = N_L b_L + b_L, ..., the last step writes b_U = x_J / D_U
+  // L phase: x_1 = N_L b_L + b_L, ..., the last step writes b_U = x_J D_U^-1
   const T *x = bL;
   for (uint32_t k = 0; k < J; ++k) {
-    const bool last = k + 1 == J;
-    T *out = last ? bU : (k & 1 ? x1 : x0);
-    spmv_launch<T>(be, *P.cp_l, x, 0, 1, EpiCpStep<T>{out, bL, last ? du : nullptr, skip}, red,
-                   out, 0, 1, T(1), T(0), skip);
-    x = out;
+    if (k + 1 == J) {
+      spmv_launch<T>(be, *P.cp_l, x, 0, 1, EpiCpStep<T, true>{bU, bL, ru, skip}, red, bU, 0, 1,
+                     T(1), T(0), skip);
+    } else {
+      T *out = k & 1 ? x1 : x0;
+      spmv_launch<T>(be, *P.cp_l, x, 0, 1, EpiCpStep<T, false>{out, bL, nullptr, skip}, red, out,
+                     0, 1, T(1), T(0), skip);
+      x = out;
+    }
   }
   // U phase from x = b_U; the last step writes the result into vec
   x = bU;
   for (uint32_t k = 0; k < J; ++k) {
     T *out = k + 1 == J ? vec : (k & 1 ? x1 : x0);
-    spmv_launch<T>(be, *P.cp_u, x, 0, 1, EpiCpStep<T>{out, bU, nullptr, skip}, red, out, 0, 1,
-                   T(1), T(0), skip);
+    spmv_launch<T>(be, *P.cp_u, x, 0, 1, EpiCpStep<T, false>{out, bU, nullptr, skip}, red, out, 0,
+                   1, T(1), T(0), skip);
     x = out;
   }
 }

@@ -133,11 +133,14 @@ struct EpiCg {  // Ap = A p, <Ap,Ap>, <p,Ap>; convergence test; next alpha/beta
 // ===========================================================================
 // preconditioned CG (cg.hpp:257-322)
 // ===========================================================================
-template <typename T>
+// JAC: Jacobi fused (z = r / d); otherwise the preconditioner runs between
+// kernels.  A compile-time choice: a runtime flag let the compiler predicate
+// the FP64 division sequence into the non-Jacobi path.
+template <typename T, bool JAC>
 struct PcgInit {  // x = 0; r = b; z = b/d (or z = b); p = z; <r,z>
   static constexpr int NDOT = 1;
+  static constexpr bool jacobi = JAC;
   const T *b, *dg; T *x, *r, *z, *p; St<T> *st;
-  bool jacobi;
   __device__ bool skip() const { return false; }
   __device__ NoScal load() const { return {}; }
   __device__ void apply(size_t i, NoScal, T (&d)[1]) const {
@@ -218,11 +221,11 @@ __device__ __forceinline__ void pcg_check(St<T> *st, T new_ip) {
 // it back.  An FP64 division is a software sequence of about ten FP64-pipe
 // instructions on GB300, so dividing again in PcgP cost more than the 8 bytes
 // per row of reading z (the write of z replaces PcgP's reads of r and d).
-template <typename T>
+template <typename T, bool JAC>
 struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (generic)
   static constexpr int NDOT = 1;
+  static constexpr bool jacobi = JAC;
   T *x, *r, *z; const T *p, *tmp, *dg; St<T> *st;
-  bool jacobi;
   struct S { T a; };
   __device__ bool skip() const { return st->done != kRunning; }
   __device__ S load() const { return {st->alpha}; }
@@ -412,11 +415,11 @@ __device__ __forceinline__ void gb_restart_done(St<T> *st, T rr) {
   st->last_restart = st->iters;
 }
 
-template <typename T>
+template <typename T, bool JAC>
 struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0* = r; ||r||^2
   static constexpr int NDOT = 1;
+  static constexpr bool jacobi = JAC;
   T *r, *p, *r0; const T *b, *dg; St<T> *st;
-  bool jacobi;
   struct Pre { T b, d; };
   __device__ bool skip() const { return st->restart_skip != 0; }
   __device__ Pre pre(uint32_t i) const { return {b[i], jacobi ? dg[i] : T(1)}; }
@@ -451,15 +454,12 @@ struct GbRestartFinish {  // generic preconditioner: p = r0* = r (already M^-1 a
 };
 
 template <typename T>
-struct EpiStore {  // y = acc (optionally / d)
+struct EpiStore {  // y = acc
   static constexpr int NDOT = 0;
-  T *y; const T *dg; const int *flag;
-  struct Pre { T d; };
+  T *y; const int *flag;
+  VCLGB_NO_PRE
   __device__ bool skip() const { return flag && *flag != kRunning; }
-  __device__ Pre pre(uint32_t i) const { return {dg ? dg[i] : T(1)}; }
-  __device__ void row(uint32_t i, T acc, const Pre &v, T (&)[1]) const {
-    y[i] = dg ? acc / v.d : acc;
-  }
+  __device__ void row(uint32_t i, T acc, const Pre &, T (&)[1]) const { y[i] = acc; }
   __device__ void finalize(const T (&)[1]) const {}
 };
 
@@ -925,14 +925,19 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
   } else {
     const bool jac = diag_needed(P);
     const T *dg = jac ? P->diag.as<T>() : nullptr;
-    vec_pass<T>(be, n, PcgInit<T>{b, dg, x, r, z, p, st, jac}, red);
-    if (!jac) {
+    if (jac) {
+      vec_pass<T>(be, n, PcgInit<T, true>{b, dg, x, r, z, p, st}, red);
+    } else {
+      vec_pass<T>(be, n, PcgInit<T, false>{b, dg, x, r, z, p, st}, red);
       precond_apply(be, *P, z, nullptr);
       vec_pass<T>(be, n, PcgInitFinish<T>{r, z, p, st}, red);
     }
     run_iterations(be, done, chunks, every, true, [&]() {
       spmv_launch<T>(be, A, p, 0, 1, EpiPcg<T>{q, p, st}, red, q, 0, 1, T(1), T(0), done, hyb);
-      vec_pass<T>(be, n, PcgUpdate<T>{x, r, z, p, q, dg, st, jac}, red);
+      if (jac)
+        vec_pass<T>(be, n, PcgUpdate<T, true>{x, r, z, p, q, dg, st}, red);
+      else
+        vec_pass<T>(be, n, PcgUpdate<T, false>{x, r, z, p, q, dg, st}, red);
       if (!jac) {
         precond_apply(be, *P, z, done);
         vec_pass<T>(be, n, PcgDot<T>{r, z, st}, red);
@@ -983,12 +988,16 @@ void bicgstab_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *ta
     vec_pass<T>(be, n, GbInit<T>{b, x, st}, red);
     const int *rskip = &st->restart_skip;
     run_iterations(be, done, chunks, every, true, [&]() {
-      spmv_launch<T>(be, A, x, 0, 1, EpiGbRestart<T>{r, p, r0, b, dg, st, jac}, red, r, 0, 1,
-                     T(1), T(0), rskip, hyb);
+      if (jac)
+        spmv_launch<T>(be, A, x, 0, 1, EpiGbRestart<T, true>{r, p, r0, b, dg, st}, red, r, 0, 1,
+                       T(1), T(0), rskip, hyb);
+      else
+        spmv_launch<T>(be, A, x, 0, 1, EpiGbRestart<T, false>{r, p, r0, b, dg, st}, red, r, 0,
+                       1, T(1), T(0), rskip, hyb);
       if (!jac) {
         precond_apply(be, *P, r, rskip);
         vec_pass<T>(be, n, GbRestartFinish<T>{p, r0, r, st}, red);
-        spmv_launch<T>(be, A, p, 0, 1, EpiStore<T>{Ap, nullptr, done}, red, Ap, 0, 1, T(1), T(0), done, hyb);
+        spmv_launch<T>(be, A, p, 0, 1, EpiStore<T>{Ap, done}, red, Ap, 0, 1, T(1), T(0), done, hyb);
         precond_apply(be, *P, Ap, done);
         vec_pass<T>(be, n, GbDot1<T>{Ap, r0, st}, red);
       } else {
@@ -996,7 +1005,7 @@ void bicgstab_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *ta
       }
       vec_pass<T>(be, n, GbS<T>{s, r, Ap, st}, red);
       if (!jac) {
-        spmv_launch<T>(be, A, s, 0, 1, EpiStore<T>{As, nullptr, done}, red, As, 0, 1, T(1), T(0), done, hyb);
+        spmv_launch<T>(be, A, s, 0, 1, EpiStore<T>{As, done}, red, As, 0, 1, T(1), T(0), done, hyb);
         precond_apply(be, *P, As, done);
         vec_pass<T>(be, n, GbDot2<T>{As, s, st}, red);
       } else {
