@@ -312,6 +312,210 @@ static LevelPlan plan_levels(uint32_t n, const std::vector<uint32_t> &rp,
   return p;
 }
 
+// Runs of small levels (level_run_kernel): consecutive levels of at most
+// kRunLevel rows each are substituted by one block; the values written in the
+// last kRing levels of a run stay in a shared-memory ring of kRing x kRunLevel
+// slots (level e's row at position p in slot (e mod kRing) * kRunLevel + p).
+constexpr uint32_t kRunLevel = 1024;
+constexpr uint32_t kRing = 16;
+constexpr uint32_t kRingSlots = kRing * kRunLevel;
+static_assert((kRingSlots & (kRingSlots - 1)) == 0, "ring slots index by mask");
+
+// first level at or after L with more than kRunLevel rows (L itself if L has)
+static uint32_t run_end(const std::vector<uint32_t> &level_ptr, uint32_t L, bool runs) {
+  const uint32_t levels = (uint32_t)level_ptr.size() - 1;
+  if (!runs) return L;
+  while (L < levels && level_ptr[L + 1] - level_ptr[L] <= kRunLevel) ++L;
+  return L;
+}
+
+// the widest level of levels [L, L1)
+static uint32_t widest_level(const std::vector<uint32_t> &level_ptr, uint32_t L, uint32_t L1) {
+  uint32_t w = 0;
+  for (uint32_t e = L; e < L1; ++e) w = std::max(w, level_ptr[e + 1] - level_ptr[e]);
+  return w;
+}
+
+// Where each read of a run finds its value: a code < 0 is ring slot ~code
+// (the row was last written at most kRing - 1 levels earlier in the same run),
+// a code >= 0 is the row to read from the vector in global memory (written
+// before the run, by a large level, or at least kRing levels earlier -- so
+// the value is final there, a barrier at least one level back).  ecode per
+// entry (the column's value), xcode per level row (the row's own value).
+static void plan_ring_codes(const std::vector<uint32_t> &level_ptr,
+                            const std::vector<uint32_t> &row_index,
+                            const std::vector<uint32_t> &row_ptr, const std::vector<uint32_t> &cols,
+                            uint32_t n, std::vector<int32_t> &ecode, std::vector<int32_t> &xcode) {
+  const uint32_t levels = (uint32_t)level_ptr.size() - 1;
+  ecode.resize(cols.size());
+  xcode.resize(row_index.size());
+  std::vector<uint32_t> wlev(n, 0), wpos(n, 0), wrun(n, 0);  // run 0: none
+  uint32_t run = 0;
+  for (uint32_t L = 0; L < levels;) {
+    uint32_t L1 = run_end(level_ptr, L, true);
+    const bool small = L1 > L;
+    if (!small) L1 = L + 1;
+    ++run;
+    for (uint32_t e = L; e < L1; ++e) {
+      auto code = [&](uint32_t r) -> int32_t {
+        if (small && wrun[r] == run && e - wlev[r] < kRing)
+          return ~(int32_t)((wlev[r] % kRing) * kRunLevel + wpos[r]);
+        return (int32_t)r;
+      };
+      for (uint32_t t = level_ptr[e]; t < level_ptr[e + 1]; ++t) {
+        xcode[t] = code(row_index[t]);
+        for (uint32_t j = row_ptr[t]; j < row_ptr[t + 1]; ++j) ecode[j] = code(cols[j]);
+      }
+      for (uint32_t t = level_ptr[e]; t < level_ptr[e + 1]; ++t) {
+        const uint32_t r = row_index[t];
+        wlev[r] = e;
+        wpos[r] = t - level_ptr[e];
+        wrun[r] = small ? run : 0;
+      }
+    }
+    L = L1;
+  }
+}
+
+// level_run_kernel: a run of consecutive small levels, one block; a level is
+// one pass of the block and a __syncthreads() replaces the kernel launch
+// between levels.  On a 2D grid every level is an anti-diagonal of at most a
+// few hundred rows, so a whole triangle is one launch instead of 2*sqrt(n).
+//
+// A level holds, for each row, the entries whose columns lie in it (a row is
+// updated at every level its columns reach).  The values the level reads come
+// from the ring when they were written in the last kRing levels of the run
+// (on a stencil: all of them, one level back), else from global memory, where
+// they are final since at least one barrier -- which is why a global read of
+// the row's own value can be issued early.  The pattern is read-only: with NT
+// threads, a level's entries (first kRunPre codes and values, the row's own
+// global value) are fetched DE levels ahead and its row information 2 DE
+// levels ahead.  DE = 1 fits 1024 threads in 64 registers; runs whose levels
+// hold at most 512 rows take 512 threads and DE = 4, which gives every
+// pattern load four levels to arrive (an early global read of the row's own
+// value is safe while DE < kRing).  Each row subtracts the same entries in the
+// same order as level_substitute_kernel, so the results do not depend on
+// which kernel ran.
+constexpr int kRunPre = 3;
+constexpr uint32_t kNoRow = 0xffffffffu;
+
+struct RunRow {
+  uint32_t row, jb, je;  // row == kNoRow when the thread has no row in the level
+  int32_t xc;            // where the row's own value is (plan_ring_codes)
+};
+
+template <typename T>
+struct RunEntries {
+  RunRow r;
+  int32_t c[kRunPre];
+  T v[kRunPre];
+  T xg;  // the row's value, prefetched when it lies in global memory
+};
+
+__device__ __forceinline__ RunRow run_fetch_row(uint32_t lev, uint32_t lev1,
+                                                const uint32_t *__restrict__ level_ptr,
+                                                const uint32_t *__restrict__ row_index,
+                                                const int32_t *__restrict__ xcode,
+                                                const uint32_t *__restrict__ row_ptr) {
+  RunRow r{kNoRow, 0, 0, 0};
+  if (lev < lev1) {
+    const uint32_t t = __ldg(level_ptr + lev) + threadIdx.x;
+    if (t < __ldg(level_ptr + lev + 1)) {
+      r.row = __ldg(row_index + t);
+      r.jb = __ldg(row_ptr + t);
+      r.je = __ldg(row_ptr + t + 1);
+      r.xc = __ldg(xcode + t);
+    }
+  }
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ RunEntries<T> run_fetch_entries(RunRow r,
+                                                           const int32_t *__restrict__ ecode,
+                                                           const T *__restrict__ vals,
+                                                           const T *vec) {
+  RunEntries<T> e;
+  e.r = r;
+#pragma unroll
+  for (int k = 0; k < kRunPre; ++k) {
+    const bool on = r.jb + k < r.je;
+    e.c[k] = on ? __ldg(ecode + r.jb + k) : 0;
+    e.v[k] = on ? __ldg(vals + r.jb + k) : T(0);
+  }
+  e.xg = (r.row != kNoRow && r.xc >= 0) ? vec[r.xc] : T(0);
+  return e;
+}
+
+template <typename T>
+__device__ __forceinline__ T run_read(int32_t code, const T *ring, const T *vec) {
+  return code < 0 ? ring[(uint32_t)~code & (kRingSlots - 1)] : vec[code];
+}
+
+// one level of a run: consume the entries of level lev from `ent`, refill it
+// with level lev + DE (its row information is in `row`) and refill `row` with
+// level lev + 2 DE.  The caller unrolls its level loop by DE, so that every
+// stage keeps its registers (stage lev mod DE) and nothing is moved between
+// levels.
+template <typename T, int DE>
+__device__ __forceinline__ void run_level(uint32_t lev, uint32_t lev1, RunEntries<T> &ent,
+                                          RunRow &row, const uint32_t *__restrict__ level_ptr,
+                                          const uint32_t *__restrict__ row_index,
+                                          const int32_t *__restrict__ xcode,
+                                          const uint32_t *__restrict__ row_ptr,
+                                          const int32_t *__restrict__ ecode,
+                                          const T *__restrict__ vals, T *vec, T *ring) {
+  const RunRow r = ent.r;
+  T x = T(0), y[kRunPre];
+  if (r.row != kNoRow) x = r.xc >= 0 ? ent.xg : ring[(uint32_t)~r.xc & (kRingSlots - 1)];
+#pragma unroll
+  for (int k = 0; k < kRunPre; ++k) y[k] = r.jb + k < r.je ? run_read(ent.c[k], ring, vec) : T(0);
+  T s = x;
+  if (r.row != kNoRow) {
+#pragma unroll
+    for (int k = 0; k < kRunPre; ++k)
+      if (r.jb + k < r.je) s -= y[k] * ent.v[k];
+    for (uint32_t j = r.jb + kRunPre; j < r.je; ++j)
+      s -= run_read(__ldg(ecode + j), ring, vec) * __ldg(vals + j);
+    ring[(lev & (kRing - 1)) * kRunLevel + threadIdx.x] = s;
+  }
+  ent = run_fetch_entries<T>(row, ecode, vals, vec);
+  row = run_fetch_row(lev + 2 * DE, lev1, level_ptr, row_index, xcode, row_ptr);
+  __syncthreads();
+  // the global copy is read only kRing levels later (or after the kernel),
+  // so it is stored after the barrier, off the level's critical path
+  if (r.row != kNoRow) vec[r.row] = s;
+}
+
+template <typename T, uint32_t NT, int DE>
+__global__ void __launch_bounds__(NT)
+    level_run_kernel(uint32_t lev0, uint32_t lev1, const uint32_t *__restrict__ level_ptr,
+                     const uint32_t *__restrict__ row_index, const int32_t *__restrict__ xcode,
+                     const uint32_t *__restrict__ row_ptr, const int32_t *__restrict__ ecode,
+                     const T *__restrict__ vals, T *vec, const int *skip) {
+  static_assert(DE >= 1 && DE < (int)kRing && NT <= kRunLevel, "pipeline depth and width");
+  extern __shared__ __align__(16) unsigned char ring_bytes[];
+  T *ring = reinterpret_cast<T *>(ring_bytes);
+  if (skip && *skip) return;
+  RunEntries<T> ents[DE];  // stage k: level lev0 + k, then every DE levels on
+  RunRow rows[DE];         // stage k: DE levels ahead of ents[k]
+#pragma unroll
+  for (int k = 0; k < DE; ++k)
+    ents[k] = run_fetch_entries<T>(
+        run_fetch_row(lev0 + k, lev1, level_ptr, row_index, xcode, row_ptr), ecode, vals, vec);
+#pragma unroll
+  for (int k = 0; k < DE; ++k)
+    rows[k] = run_fetch_row(lev0 + DE + k, lev1, level_ptr, row_index, xcode, row_ptr);
+  for (uint32_t lev = lev0; lev < lev1; lev += DE) {
+#pragma unroll
+    for (int k = 0; k < DE; ++k) {
+      if (lev + k >= lev1) break;  // uniform over the block
+      run_level<T, DE>(lev + k, lev1, ents[k], rows[k], level_ptr, row_index, xcode, row_ptr,
+                       ecode, vals, vec, ring);
+    }
+  }
+}
+
 template <typename X>
 static void upload(Backend &be, DevBuf &dst, const std::vector<X> &src) {
   dst.alloc(std::max<size_t>(src.size(), 1) * sizeof(X), be.stream);
@@ -375,6 +579,20 @@ static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
     tri.rows = pl.row_index.size();
     tri.nnz = pl.cols.size();
     tri.h_level_ptr = pl.level_ptr;
+    tri.runs = n < 0x80000000u;  // codes hold a row index in an int32
+    if (tri.runs) {
+      std::vector<int32_t> ecode, xcode;
+      plan_ring_codes(pl.level_ptr, pl.row_index, pl.row_ptr, pl.cols, n, ecode, xcode);
+      upload(be, tri.ecode, ecode);
+      upload(be, tri.xcode, xcode);
+      VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // host codes freed after use
+      VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel, 1>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(kRingSlots * sizeof(T))));
+      VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel / 2, 4>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(kRingSlots * sizeof(T))));
+    }
     upload(be, tri.level_ptr, pl.level_ptr);
     upload(be, tri.row_index, pl.row_index);
     upload(be, tri.row_ptr, pl.row_ptr);
@@ -544,110 +762,23 @@ std::unique_ptr<Precond> block_ilu0_create(Backend &be, const Matrix &A, uint32_
   return P;
 }
 
-// A run of consecutive levels of at most kRunLevel rows each, substituted by
-// one block of kRunLevel threads: a level is one pass of the block, and a
-// __syncthreads() (the block's own writes to vec are visible to it after the
-// barrier) replaces the kernel launch between levels.  On a 2D grid every
-// level is an anti-diagonal of at most a few hundred rows, so the whole
-// triangle becomes one launch instead of 2*sqrt(n).
-//
-// A level holds, for each row, the entries whose columns lie in that level
-// (a row is updated at every level its columns reach), so vec[row] and
-// vec[cols] are read only after the barrier.  The pattern is not written: a
-// thread's row index and entry range are fetched two levels ahead and its
-// first kRunPre columns and values one level ahead, so that the critical path
-// of a level is one round of vec loads, one multiply-add chain, one store and
-// the barrier.  Each row is computed exactly as in level_substitute_kernel
-// (same entries, same order), so the results are identical.
-constexpr uint32_t kRunLevel = 1024;
-constexpr int kRunPre = 4;
-
-constexpr uint32_t kNoRow = 0xffffffffu;
-
-struct RunRow {
-  uint32_t row, jb, je;  // row == kNoRow when the thread has no row in the level
-};
-
-template <typename T>
-struct RunEntries {
-  RunRow r;
-  uint32_t c[kRunPre];
-  T v[kRunPre];
-};
-
-__device__ __forceinline__ RunRow run_fetch_row(uint32_t lev, uint32_t lev1,
-                                                const uint32_t *__restrict__ level_ptr,
-                                                const uint32_t *__restrict__ row_index,
-                                                const uint32_t *__restrict__ row_ptr) {
-  RunRow r{kNoRow, 0, 0};
-  if (lev < lev1) {
-    const uint32_t t = __ldg(level_ptr + lev) + threadIdx.x;
-    if (t < __ldg(level_ptr + lev + 1)) {
-      r.row = __ldg(row_index + t);
-      r.jb = __ldg(row_ptr + t);
-      r.je = __ldg(row_ptr + t + 1);
-    }
-  }
-  return r;
-}
-
-template <typename T>
-__device__ __forceinline__ RunEntries<T> run_fetch_entries(RunRow r,
-                                                           const uint32_t *__restrict__ cols,
-                                                           const T *__restrict__ vals) {
-  RunEntries<T> e;
-  e.r = r;
-#pragma unroll
-  for (int k = 0; k < kRunPre; ++k) {
-    const bool on = r.jb + k < r.je;
-    e.c[k] = on ? __ldg(cols + r.jb + k) : 0u;
-    e.v[k] = on ? __ldg(vals + r.jb + k) : T(0);
-  }
-  return e;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kRunLevel)
-    level_run_kernel(uint32_t lev0, uint32_t lev1, const uint32_t *__restrict__ level_ptr,
-                     const uint32_t *__restrict__ row_index, const uint32_t *__restrict__ row_ptr,
-                     const uint32_t *__restrict__ cols, const T *__restrict__ vals, T *vec,
-                     const int *skip) {
-  if (skip && *skip) return;
-  RunEntries<T> cur = run_fetch_entries<T>(
-      run_fetch_row(lev0, lev1, level_ptr, row_index, row_ptr), cols, vals);
-  RunRow next = run_fetch_row(lev0 + 1, lev1, level_ptr, row_index, row_ptr);
-  for (uint32_t lev = lev0; lev < lev1; ++lev) {
-    const RunRow r = cur.r;
-    const T x = r.row != kNoRow ? vec[r.row] : T(0);
-    T y[kRunPre];
-#pragma unroll
-    for (int k = 0; k < kRunPre; ++k) y[k] = r.jb + k < r.je ? vec[cur.c[k]] : T(0);
-    const RunRow after = run_fetch_row(lev + 2, lev1, level_ptr, row_index, row_ptr);
-    const RunEntries<T> upcoming = run_fetch_entries<T>(next, cols, vals);
-    if (r.row != kNoRow) {
-      T s = x;
-#pragma unroll
-      for (int k = 0; k < kRunPre; ++k)
-        if (r.jb + k < r.je) s -= y[k] * cur.v[k];
-      for (uint32_t j = r.jb + kRunPre; j < r.je; ++j) s -= vec[__ldg(cols + j)] * __ldg(vals + j);
-      vec[r.row] = s;
-    }
-    __syncthreads();
-    cur = upcoming;
-    next = after;
-  }
-}
-
 template <typename T>
 static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *skip) {
   for (uint32_t L = 0; L < tri.levels;) {
     const uint32_t r0 = tri.h_level_ptr[L], r1 = tri.h_level_ptr[L + 1];
-    if (r1 - r0 <= kRunLevel) {
-      uint32_t L1 = L + 1;
-      while (L1 < tri.levels && tri.h_level_ptr[L1 + 1] - tri.h_level_ptr[L1] <= kRunLevel) ++L1;
-      level_run_kernel<T><<<1, kRunLevel, 0, be.stream>>>(
-          L, L1, tri.level_ptr.as<uint32_t>(), tri.row_index.as<uint32_t>(),
-          tri.row_ptr.as<uint32_t>(), tri.cols.as<uint32_t>(), tri.vals.as<T>(), vec, skip);
+    const uint32_t L1 = run_end(tri.h_level_ptr, L, tri.runs);
+    if (L1 > L) {
+      const size_t smem = kRingSlots * sizeof(T);
+      if (widest_level(tri.h_level_ptr, L, L1) <= kRunLevel / 2)
+        level_run_kernel<T, kRunLevel / 2, 4><<<1, kRunLevel / 2, smem, be.stream>>>(
+            L, L1, tri.level_ptr.as<uint32_t>(), tri.row_index.as<uint32_t>(),
+            tri.xcode.as<int32_t>(), tri.row_ptr.as<uint32_t>(), tri.ecode.as<int32_t>(),
+            tri.vals.as<T>(), vec, skip);
+      else
+        level_run_kernel<T, kRunLevel, 1><<<1, kRunLevel, smem, be.stream>>>(
+            L, L1, tri.level_ptr.as<uint32_t>(), tri.row_index.as<uint32_t>(),
+            tri.xcode.as<int32_t>(), tri.row_ptr.as<uint32_t>(), tri.ecode.as<int32_t>(),
+            tri.vals.as<T>(), vec, skip);
       be.launches++;
       L = L1;
       continue;

@@ -314,6 +314,9 @@ struct Precond {
     uint64_t rows = 0, nnz = 0;
     std::vector<uint32_t> h_level_ptr;
     DevBuf level_ptr, row_index, row_ptr, cols, vals;
+    // where a run of small levels finds each value (precond.cu, level_run_kernel)
+    DevBuf ecode, xcode;
+    bool runs = false;
   } L, U;
   // Chow-Patel: I - D_L^-1 L and I - D_U^-1 U (ICC: U = L^T) without their
   // diagonal entries, which the reference stores as zeros; diag = D_L,
