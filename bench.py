@@ -690,6 +690,25 @@ def profile_kernels(args):
     matrix (about 21M nnz, 250 MB of CSR arrays)."""
     import torch
     import vclgb as V
+    if args.profile_case == "preconditioners":
+        # three applies each of ILU0, block ILU0 (8 blocks) and Chow-Patel ILU on
+        # the 512^2 convection-diffusion matrix, of Chow-Patel IC0 on 128^3
+        rp, ci, v = gen.convdiff2d(512, 512, peclet=10.0, shift=0.01)
+        A = V.compressed_matrix(rp, ci, v)
+        z = torch.tensor(gen.rhs_uniform(len(rp) - 1, 5), device="cuda")
+        for P in (V.ilu0_precond(A), V.block_ilu_precond(A, num_blocks=8),
+                  V.chow_patel_ilu_precond(A)):
+            for _ in range(3):
+                P.apply(z)
+        rp, ci, v = gen.laplace3d(128)
+        A = V.compressed_matrix(rp, ci, v)
+        z = torch.tensor(gen.rhs_uniform(len(rp) - 1, 1), device="cuda")
+        P = V.chow_patel_icc_precond(A)
+        for _ in range(3):
+            P.apply(z)
+        torch.cuda.synchronize()
+        print("profile workload done")
+        return
     if args.profile_case == "lognormal":
         rp, ci, v = gen.lognormal_random(1 << 20, mu=2.5, sigma=1.0, hi=2000, seed=1)
         n = len(rp) - 1
@@ -723,7 +742,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-kernels", action="store_true",
                     help="run the small fixed workload used for ncu captures")
-    ap.add_argument("--profile-case", default="laplace", choices=["laplace", "lognormal"])
+    ap.add_argument("--profile-case", default="laplace",
+                    choices=["laplace", "lognormal", "preconditioners"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

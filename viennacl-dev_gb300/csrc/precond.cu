@@ -8,11 +8,13 @@
 // the per-level substitution lists follow level_scheduling_setup_impl
 // (detail/ilu/common.hpp:50-187) and are built from the pattern on the host,
 // as the reference does; the numeric factorisation then runs on the device,
-// one kernel per L level (rows of one level are independent), with the same
+// level by level (rows of one level are independent; a run of small levels is
+// one single-block launch with a barrier between levels), with the same
 // per-row IKJ operation order and no fused multiply-add, so the factors are
 // bit-identical to the reference's sequential host loop (ilu0.hpp:77-140).
-// The apply runs one substitution kernel per level
-// (linalg/cuda/misc_operations.hpp:41-83 semantics).
+// The apply substitutes level by level (linalg/cuda/misc_operations.hpp:41-83
+// semantics): a run of small levels is one block (level_run_kernel), a large
+// level one grid-wide launch (level_substitute_kernel).
 #include <algorithm>
 #include <map>
 
@@ -152,32 +154,55 @@ __device__ __forceinline__ double sub_rn<double>(double a, double b) { return __
 template <>
 __device__ __forceinline__ float sub_rn<float>(float a, float b) { return __fsub_rn(a, b); }
 
+// the factorisation of one row, in the reference's IKJ order (ilu0.hpp:77-140)
+template <typename T>
+__device__ __forceinline__ void ilu0_row(uint32_t i, const uint32_t *__restrict__ rp,
+                                         const uint32_t *__restrict__ ci, T *lu) {
+  const uint32_t ib = rp[i], ie = rp[i + 1];
+  for (uint32_t bk = ib; bk < ie; ++bk) {
+    const uint32_t k = ci[bk];
+    if (k >= i) continue;
+    const uint32_t kb = rp[k], ke = rp[k + 1];
+    T a_kk = 0;
+    for (uint32_t q = kb; q < ke; ++q)
+      if (ci[q] == k) { a_kk = lu[q]; break; }
+    const T a_ik = lu[bk] / a_kk;
+    lu[bk] = a_ik;
+    for (uint32_t bj = ib; bj < ie; ++bj) {
+      const uint32_t j = ci[bj];
+      if (j <= k) continue;
+      T a_kj = 0;
+      for (uint32_t q = kb; q < ke; ++q)
+        if (ci[q] == j) { a_kj = lu[q]; break; }
+      lu[bj] = sub_rn(lu[bj], mul_rn(a_ik, a_kj));
+    }
+  }
+}
+
 template <typename T>
 __global__ void ilu0_level_kernel(uint32_t count, const uint32_t *__restrict__ rows_of_level,
                                   const uint32_t *__restrict__ rp,
                                   const uint32_t *__restrict__ ci, T *lu) {
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < count;
-       t += (size_t)gridDim.x * blockDim.x) {
-    const uint32_t i = rows_of_level[t];
-    const uint32_t ib = rp[i], ie = rp[i + 1];
-    for (uint32_t bk = ib; bk < ie; ++bk) {
-      const uint32_t k = ci[bk];
-      if (k >= i) continue;
-      const uint32_t kb = rp[k], ke = rp[k + 1];
-      T a_kk = 0;
-      for (uint32_t q = kb; q < ke; ++q)
-        if (ci[q] == k) { a_kk = lu[q]; break; }
-      const T a_ik = lu[bk] / a_kk;
-      lu[bk] = a_ik;
-      for (uint32_t bj = ib; bj < ie; ++bj) {
-        const uint32_t j = ci[bj];
-        if (j <= k) continue;
-        T a_kj = 0;
-        for (uint32_t q = kb; q < ke; ++q)
-          if (ci[q] == j) { a_kj = lu[q]; break; }
-        lu[bj] = sub_rn(lu[bj], mul_rn(a_ik, a_kj));
-      }
-    }
+       t += (size_t)gridDim.x * blockDim.x)
+    ilu0_row<T>(rows_of_level[t], rp, ci, lu);
+}
+
+// consecutive levels [e0, e1) of at most kFactorRun rows each in one block,
+// a barrier between levels: a row reads only rows of earlier levels, which
+// this block finished before a barrier.  Level e's rows are
+// order[off[e] .. off[e + 1]).
+constexpr uint32_t kFactorRun = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(kFactorRun)
+    ilu0_run_kernel(uint32_t e0, uint32_t e1, const uint32_t *__restrict__ off,
+                    const uint32_t *__restrict__ order, const uint32_t *__restrict__ rp,
+                    const uint32_t *__restrict__ ci, T *lu) {
+  for (uint32_t e = e0; e < e1; ++e) {
+    const uint32_t t = __ldg(off + e) + threadIdx.x;
+    if (t < __ldg(off + e + 1)) ilu0_row<T>(__ldg(order + t), rp, ci, lu);
+    __syncthreads();
   }
 }
 
@@ -550,15 +575,26 @@ static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
   if (A.nnz)
     VCLGB_CUDA(cudaMemcpyAsync(P.lu.ptr, A.values, A.nnz * sizeof(T), cudaMemcpyDeviceToDevice,
                                be.stream));
-  DevBuf d_order;
+  DevBuf d_order, d_off;
   upload(be, d_order, order);
-  for (uint32_t e = 1; e <= maxlev; ++e) {
+  upload(be, d_off, lvl_off);
+  for (uint32_t e = 1; e <= maxlev;) {
     uint32_t c = lvl_cnt[e];
-    if (!c) continue;
+    if (c <= kFactorRun) {  // a run of small levels: one block
+      uint32_t e1 = e + 1;
+      while (e1 <= maxlev && lvl_cnt[e1] <= kFactorRun) ++e1;
+      ilu0_run_kernel<T><<<1, kFactorRun, 0, be.stream>>>(
+          e, e1, d_off.as<uint32_t>(), d_order.as<uint32_t>(), A.row_ptr, A.col_idx,
+          P.lu.as<T>());
+      be.launches++;
+      e = e1;
+      continue;
+    }
     int g = waves_grid(be, 128, 16, c);
     ilu0_level_kernel<T><<<g, 128, 0, be.stream>>>(c, d_order.as<uint32_t>() + lvl_off[e],
                                                    A.row_ptr, A.col_idx, P.lu.as<T>());
     be.launches++;
+    ++e;
   }
   VCLGB_CHECK_LAUNCH();
   // U diagonal of the factors
