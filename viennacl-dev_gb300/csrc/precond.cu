@@ -156,8 +156,8 @@ __device__ __forceinline__ float sub_rn<float>(float a, float b) { return __fsub
 
 // the factorisation of one row, in the reference's IKJ order (ilu0.hpp:77-140)
 template <typename T>
-__device__ __forceinline__ void ilu0_row(uint32_t i, const uint32_t *__restrict__ rp,
-                                         const uint32_t *__restrict__ ci, T *lu) {
+__device__ __forceinline__ void ilu0_row_generic(uint32_t i, const uint32_t *__restrict__ rp,
+                                                 const uint32_t *__restrict__ ci, T *lu) {
   const uint32_t ib = rp[i], ie = rp[i + 1];
   for (uint32_t bk = ib; bk < ie; ++bk) {
     const uint32_t k = ci[bk];
@@ -179,6 +179,76 @@ __device__ __forceinline__ void ilu0_row(uint32_t i, const uint32_t *__restrict_
   }
 }
 
+// The same row with row i and the first kRowCache entries of each row k in
+// registers: each row is read in one round of independent loads instead of a
+// chain of dependent ones, row i is written back once at the end (no other
+// thread reads it while its level runs), and a value of row k is the first
+// match in storage order -- cached entries first, the rest of a longer row k
+// from memory -- so every operation and its operands are the generic path's.
+constexpr int kRowCache = 8;
+
+template <typename T>
+__device__ __forceinline__ T ilu0_lookup(uint32_t j, const uint32_t (&kc)[kRowCache],
+                                         const T (&kv)[kRowCache], uint32_t kb, uint32_t ke,
+                                         const uint32_t *__restrict__ ci, const T *lu) {
+  bool found = false;
+  T v = T(0);
+#pragma unroll
+  for (int q = 0; q < kRowCache; ++q)
+    if (!found && kc[q] == j) {
+      v = kv[q];
+      found = true;
+    }
+  if (!found)
+    for (uint32_t q = kb + kRowCache; q < ke; ++q)
+      if (ci[q] == j) { v = lu[q]; break; }
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ void ilu0_row(uint32_t i, const uint32_t *__restrict__ rp,
+                                         const uint32_t *__restrict__ ci, T *lu) {
+  const uint32_t ib = rp[i], ie = rp[i + 1], len = ie - ib;
+  if (len > (uint32_t)kRowCache) {
+    ilu0_row_generic<T>(i, rp, ci, lu);
+    return;
+  }
+  uint32_t c[kRowCache];
+  T a[kRowCache];
+#pragma unroll
+  for (int t = 0; t < kRowCache; ++t) {
+    const bool on = (uint32_t)t < len;
+    c[t] = on ? ci[ib + t] : 0xffffffffu;
+    a[t] = on ? lu[ib + t] : T(0);
+  }
+#pragma unroll
+  for (int tk = 0; tk < kRowCache; ++tk) {
+    const uint32_t k = c[tk];
+    if ((uint32_t)tk >= len || k >= i) continue;
+    const uint32_t kb = rp[k], ke = rp[k + 1];
+    uint32_t kc[kRowCache];
+    T kv[kRowCache];
+#pragma unroll
+    for (int q = 0; q < kRowCache; ++q) {
+      const bool on = kb + q < ke;
+      kc[q] = on ? ci[kb + q] : 0xffffffffu;
+      kv[q] = on ? lu[kb + q] : T(0);
+    }
+    const T a_kk = ilu0_lookup<T>(k, kc, kv, kb, ke, ci, lu);
+    const T a_ik = a[tk] / a_kk;
+    a[tk] = a_ik;
+#pragma unroll
+    for (int tj = 0; tj < kRowCache; ++tj) {
+      const uint32_t j = c[tj];
+      if ((uint32_t)tj >= len || j <= k) continue;
+      a[tj] = sub_rn(a[tj], mul_rn(a_ik, ilu0_lookup<T>(j, kc, kv, kb, ke, ci, lu)));
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kRowCache; ++t)
+    if ((uint32_t)t < len) lu[ib + t] = a[t];
+}
+
 template <typename T>
 __global__ void ilu0_level_kernel(uint32_t count, const uint32_t *__restrict__ rows_of_level,
                                   const uint32_t *__restrict__ rp,
@@ -191,11 +261,12 @@ __global__ void ilu0_level_kernel(uint32_t count, const uint32_t *__restrict__ r
 // consecutive levels [e0, e1) of at most kFactorRun rows each in one block,
 // a barrier between levels: a row reads only rows of earlier levels, which
 // this block finished before a barrier.  Level e's rows are
-// order[off[e] .. off[e + 1]).
-constexpr uint32_t kFactorRun = 1024;
+// order[off[e] .. off[e + 1]).  512 threads leave the cached row update room
+// for its registers (at 1024 threads the FP64 version spills).
+constexpr uint32_t kFactorRun = 512;
 
 template <typename T>
-__global__ void __launch_bounds__(kFactorRun)
+__global__ void __launch_bounds__(kFactorRun, 1)
     ilu0_run_kernel(uint32_t e0, uint32_t e1, const uint32_t *__restrict__ off,
                     const uint32_t *__restrict__ order, const uint32_t *__restrict__ rp,
                     const uint32_t *__restrict__ ci, T *lu) {
