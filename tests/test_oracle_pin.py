@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
+import vclgb_gen as gen
 from conftest import rel_err
 
 
@@ -310,3 +311,48 @@ def test_live_reference_cg_jacobi_laplace256():
     x, it, err = oracle.solve("cg", rp, ci, v, b, 1e-8, 2000, "jacobi")
     assert abs(it - r["iters"]) <= 1
     assert rel_err(x, r["x"]) < 1e-10
+
+
+def test_block_ilu_one_block_is_ilu0():
+    # one block covering every row: block ILU0's factors are ILU0's, and its
+    # column-sweep apply equals the level-scheduled apply up to rounding
+    rp, ci, v = gen.convdiff2d(17, 13, peclet=8.0, shift=0.05)
+    B = oracle.block_ilu0(rp, ci, v, num_blocks=1)
+    assert np.array_equal(B["rp"], np.asarray(rp, np.uint32))
+    assert np.array_equal(B["lu"][:B["nnz"]], oracle.ilu0_factor(rp, ci, v))
+    b = gen.rhs_uniform(len(rp) - 1, 3)
+    assert rel_err(oracle.block_ilu0_apply(B, b), oracle.ilu0_apply(rp, ci, v, b)) < 1e-14
+
+
+def test_block_ilu_drops_couplings_between_blocks():
+    # the block-diagonal pattern keeps exactly the entries whose row and column
+    # share a block, in storage order
+    rp, ci, v = gen.lognormal_random(500, mu=1.5, sigma=0.7, hi=40, seed=4)
+    bounds = oracle.block_bounds(500, 7)
+    B = oracle.block_ilu0(rp, ci, v, num_blocks=7)
+    blk = np.zeros(500, np.int64)
+    for i, (a, b) in enumerate(bounds):
+        blk[a:b] = i
+    rows = np.repeat(np.arange(500), np.diff(np.asarray(rp, np.int64)))
+    keep = blk[rows] == blk[np.asarray(ci, np.int64)]
+    assert np.array_equal(B["ci"][:B["nnz"]], np.asarray(ci)[keep])
+
+
+def test_chow_patel_properties():
+    # no sweep: L and U are A's scaled triangles (unit-modulus diagonals); the
+    # ICC transpose holds L's entries; a matrix that is already triangular-free
+    # (diagonal) makes the apply a division by the scaled diagonal
+    rp, ci, v = gen.laplace2d(9, 7)
+    n = len(rp) - 1
+    F = oracle.chow_patel_ilu(rp, ci, v, 0)
+    assert np.allclose(np.abs(F["diag_l"]), 1.0) and np.allclose(np.abs(F["diag_u"]), 1.0)
+    G = oracle.chow_patel_icc(rp, ci, v, 2)
+    assert len(G["u_ci"]) == len(G["l_ci"])
+    lr = np.repeat(np.arange(n), np.diff(G["l_rp"].astype(np.int64)))
+    ur = np.repeat(np.arange(n), np.diff(G["u_rp"].astype(np.int64)))
+    assert sorted(zip(lr, G["l_ci"])) == sorted(zip(G["u_ci"], ur))
+    drp, dci = np.arange(n + 1, dtype=np.uint32), np.arange(n, dtype=np.uint32)
+    dv = np.linspace(2.0, 9.0, n)
+    D = oracle.chow_patel_ilu(drp, dci, dv, 3)
+    b = gen.rhs_uniform(n, 2)
+    assert np.allclose(oracle.chow_patel_apply(D, b, 2), b / D["diag_l"] / D["diag_u"], rtol=1e-15)
