@@ -310,6 +310,10 @@ def run_ours(args):
     # ---- CPU baseline (rank 0, N=1): the reference algorithm on host cores ---
     if rank == 0 and ws == 1 and not args.quick:
         out["cpu_baseline"] = cpu_baseline_cg(rp, ci, v, b, tol, maxit)
+        try:
+            out["cpu_baseline"]["preconditioners"] = cpu_baseline_preconditioners()
+        except Exception as e:  # a side figure: it never takes the bench line with it
+            out["cpu_baseline"]["preconditioners"] = {"error": str(e)}
     else:
         out["cpu_baseline"] = None
     if rank == 0:
@@ -649,6 +653,49 @@ def cpu_baseline_cg(rp, ci, v, b, tol, maxit):
     return {"value": t, "unit": "s", "cores": cores, "kind": "port",
             "sample": "one full pipelined-CG solve of the headline workload (%d iterations)" % it,
             "iters": it}
+
+
+def cpu_baseline_preconditioners():
+    """The reference's host algorithms (C restatement, OpenMP on all host cores)
+    for the preconditioner figures of the secondary section, on the same
+    matrices: ILU0 (factorisation + level sets, level-scheduled apply), block
+    ILU0 with 8 blocks, Chow-Patel ILU (3 sweeps, 2 Jacobi steps) on the 512^2
+    convection-diffusion matrix, Chow-Patel IC0 on the 128^3 Laplacian.  Each
+    apply is the mean of 5."""
+    import oracle
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+
+    def timed(fn, reps=1):
+        t0 = time.time()
+        for _ in range(reps):
+            r = fn()
+        return (time.time() - t0) / reps, r
+
+    out = {"cores": cores, "kind": "port", "unit": "s"}
+    rp, ci, v = gen.convdiff2d(512, 512, peclet=10.0, shift=0.01)
+    b = gen.rhs_uniform(len(rp) - 1, 5)
+
+    def ilu0_setup():
+        lu = oracle.ilu0_factor(rp, ci, v)
+        ud = oracle.diag(rp, ci, lu)
+        return lu, ud, oracle.level_setup(rp, ci, lu, ud, False), oracle.level_setup(rp, ci, lu, ud, True)
+
+    t_set, (lu, ud, L, U) = timed(ilu0_setup)
+    t_app, _ = timed(lambda: oracle.level_substitute(U, oracle.level_substitute(L, b) / ud), 5)
+    out["ilu0_convdiff2d_512"] = {"setup_s": t_set, "apply_s": t_app}
+    t_set, B = timed(lambda: oracle.block_ilu0(rp, ci, v, num_blocks=8))
+    t_app, _ = timed(lambda: oracle.block_ilu0_apply(B, b), 5)
+    out["block_ilu8_convdiff2d_512"] = {"setup_s": t_set, "apply_s": t_app}
+    t_set, F = timed(lambda: oracle.chow_patel_ilu(rp, ci, v, 3))
+    t_app, _ = timed(lambda: oracle.chow_patel_apply(F, b, 2), 5)
+    out["chow_patel_ilu_convdiff2d_512"] = {"setup_s": t_set, "apply_s": t_app}
+    rp, ci, v = gen.laplace3d(128)
+    b = gen.rhs_uniform(len(rp) - 1, 1)
+    t_set, F = timed(lambda: oracle.chow_patel_icc(rp, ci, v, 3))
+    t_app, _ = timed(lambda: oracle.chow_patel_apply(F, b, 2), 5)
+    out["chow_patel_ic0_laplace3d_128"] = {"setup_s": t_set, "apply_s": t_app}
+    return out
 
 
 def run_reference(args):
