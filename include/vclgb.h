@@ -321,6 +321,23 @@ VCLGB_API vclgbStatus vclgbIlu0GetInfo(vclgbPrecond P, vclgbIlu0Info *info);
  *      by the row's U diagonal, as detail/ilu/common.hpp:162 does). */
 VCLGB_API vclgbStatus vclgbIlu0Export(vclgbBackend be, vclgbPrecond P, int which, void *d_dst);
 
+/* ---- triangular solves --------------------------------------------------------
+ * inplace_solve(A, vec, tag) and, transposed != 0, inplace_solve(trans(A), vec, tag)
+ * for a square compressed_matrix (host backend linalg/host_based/
+ * sparse_matrix_operations.hpp:537-1090; CUDA backend linalg/cuda/
+ * sparse_matrix_operations.hpp:780-1008).  tag: VCLGB_LOWER / VCLGB_UPPER divide by
+ * the row's diagonal entry, VCLGB_UNIT_LOWER / VCLGB_UNIT_UPPER take a unit
+ * diagonal; entries outside the tag's strict triangle are ignored, as in the
+ * reference (a missing diagonal entry divides by zero there and here).  d_vec
+ * is a contiguous device vector of length rows, overwritten by the solution.
+ * The rows run level by level on the device; the levels depend on the
+ * pattern only and are built on the first call for each (triangle,
+ * orientation) and kept with the matrix, so the pattern must not change
+ * afterwards (the values may). */
+typedef enum { VCLGB_LOWER = 0, VCLGB_UPPER = 1, VCLGB_UNIT_LOWER = 2, VCLGB_UNIT_UPPER = 3 } vclgbTriTag;
+VCLGB_API vclgbStatus vclgbCsrInplaceSolve(vclgbBackend be, vclgbMatrix A, int tag, int transposed,
+                                           void *d_vec);
+
 /* ---- iterative solvers ------------------------------------------------------ */
 /* Mirrors cg_tag / bicgstab_tag / gmres_tag (linalg/cg.hpp:48-87,
  * linalg/bicgstab.hpp:47-90, linalg/gmres.hpp:49-101); iters and error are
@@ -356,11 +373,18 @@ VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend be, vclgbMatrix A, const void *d
  * without, generic (bicgstab.hpp:398-489) with a preconditioner. */
 VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend be, vclgbMatrix A, const void *d_b,
                                          void *d_x, vclgbSolverTag *tag, vclgbPrecond precond);
-/* linalg::solve(A, b, gmres_tag): pipelined "simpler GMRES" with classical
- * Gram-Schmidt (gmres.hpp:181-367).  The restart bookkeeping (triangular
- * solve of size krylov_dim) runs on the device too. */
+/* linalg::solve(A, b, gmres_tag[, precond]).  precond == NULL runs the
+ * pipelined "simpler GMRES" with classical Gram-Schmidt (gmres.hpp:181-367);
+ * with a preconditioner (any of the objects above) it follows the reference's
+ * Householder variant (gmres.hpp:449-631): r = M^-1 (b - A x) and the
+ * restart test rho_0/||b|| < tol, one iteration per Krylov step, the clamped
+ * projection and the test |rho rho_0/||b||| < tol after every step.  Its
+ * orthonormal basis is formed by classical Gram-Schmidt with one repeated
+ * pass when the first cancelled more than half of the vector's norm squared
+ * (the same basis as the reflections', up to rounding).  The restart
+ * bookkeeping (triangular solve of size krylov_dim) runs on the device too. */
 VCLGB_API vclgbStatus vclgbSolveGMRES(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
-                                      vclgbSolverTag *tag);
+                                      vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, mixed_precision_cg_tag(tol, max_iters, inner_tol))
  * (mixed_precision_cg.hpp:99-186): FP32 CG restarted from an FP64 residual. */
 VCLGB_API vclgbStatus vclgbSolveMixedCG(vclgbBackend be, vclgbMatrix A, const void *d_b,
@@ -406,7 +430,8 @@ VCLGB_API vclgbStatus vclgbBatchDestroy(vclgbBatch *batch);
 /* ---- adjoint (backward) solve (no reference counterpart) ------------------
  * For x = A^-1 b (the forward solve) and dL/dx: solves A^T lambda = dL/dx with
  * solver 0 = CG, 1 = BiCGStab, 2 = GMRES (tag as for the forward solvers;
- * precond: NULL or a Jacobi preconditioner of A, which is also one of A^T),
+ * precond: NULL or a Jacobi preconditioner of A, which is also one of A^T;
+ * GMRES with Jacobi runs the preconditioned variant of vclgbSolveGMRES),
  * writes dL/db = lambda (length rows) and, if d_dLdA != NULL, the gradient
  * on the sparsity pattern dL/dA_ij = -lambda_i x_j (length nnz, in A's entry
  * order).  symmetric != 0 uses A itself; otherwise A^T is built once on the

@@ -85,7 +85,8 @@ def lib():
         for name in ("vo_cg_d", "vo_bicgstab_d"):
             getattr(L, name).argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p,
                                          ctypes.POINTER(Tag), ctypes.POINTER(Precond)]
-        L.vo_gmres_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, ctypes.POINTER(Tag)]
+        L.vo_gmres_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, ctypes.POINTER(Tag),
+                                 ctypes.POINTER(Precond)]
         L.vo_mixed_cg_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, ctypes.POINTER(Tag),
                                     ctypes.c_float]
         L.vo_ir_jacobi_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _f64p, _D, _U32, _D, _U32,
@@ -113,6 +114,8 @@ def lib():
         L.vo_csr_transpose_d.argtypes = [_U32, _U32, _u32p, _u32p, _f64p, _u32p, _u32p, _f64p,
                                          _u32p]
         L.vo_set_gmres_host_quirk.argtypes = [_I]
+        L.vo_set_gmres_clamp_restart.argtypes = [_I]
+        L.vo_csr_inplace_solve_d.argtypes = [_U32, _u32p, _u32p, _f64p, _f64p, _I, _I]
         L.vo_max_threads.restype = _I
         L.vo_set_threads.argtypes = [_I]
         _lib = L
@@ -286,13 +289,24 @@ def solve(kind, rp, ci, v, b, tol, max_iters, precond="none", krylov_dim=30,
     elif kind == "bicgstab":
         lib().vo_bicgstab_d(n, rp, ci, v, b, x, ctypes.byref(t), ctypes.byref(P))
     elif kind == "gmres":
-        lib().vo_gmres_d(n, rp, ci, v, b, x, ctypes.byref(t))
+        lib().vo_gmres_d(n, rp, ci, v, b, x, ctypes.byref(t), ctypes.byref(P))
     elif kind == "mixed_cg":
         lib().vo_mixed_cg_d(n, rp, ci, v, b, x, ctypes.byref(t), inner_tol)
     else:
         raise ValueError(kind)
     del keep
     return x, t.iters, t.error
+
+
+TRI_TAGS = {"lower": 0, "upper": 1, "unit_lower": 2, "unit_upper": 3}
+
+
+def inplace_solve(rp, ci, v, vec, tag, trans=False):
+    """inplace_solve(A or trans(A), vec, <tag>_tag) of the host backend; returns the result."""
+    out = _c(vec, np.float64).copy()
+    lib().vo_csr_inplace_solve_d(len(rp) - 1, _c(rp, np.uint32), _c(ci, np.uint32),
+                                 _c(v, np.float64), out, TRI_TAGS[tag], int(bool(trans)))
+    return out
 
 
 def refined_cg(rp, ci, v, b, tol=1e-10, max_outer=30, inner_tol=1e-4, max_inner=100000):

@@ -393,9 +393,35 @@ int main(int argc, char **argv) {
     } else if (cmd == "gmres") {
       unsigned kdim = argc > 6 ? static_cast<unsigned>(std::atoi(argv[6])) : 30;
       viennacl::linalg::gmres_tag tag(tol, maxit, kdim);
-      t0 = now();
-      x = viennacl::linalg::solve(M, b, tag);
-      t1 = now();
+      if (pc == "jacobi") {
+        viennacl::linalg::jacobi_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::jacobi_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc == "ilu0") {
+        viennacl::linalg::ilu0_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::ilu0_tag(true));
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc.compare(0, 3, "row") == 0) {
+        viennacl::linalg::row_scaling<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::row_scaling_tag(static_cast<unsigned>(pc[3] - '0')));
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else if (pc == "cpilu") {
+        viennacl::linalg::chow_patel_ilu_precond<viennacl::compressed_matrix<double> > P(
+            M, viennacl::linalg::chow_patel_tag());
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag, P);
+        t1 = now();
+      } else {
+        t0 = now();
+        x = viennacl::linalg::solve(M, b, tag);
+        t1 = now();
+      }
       iters = tag.iters();
       err = tag.error();
     } else {
@@ -410,6 +436,31 @@ int main(int argc, char **argv) {
     std::vector<double> xh = from_vcl(x);
     save("x.f64", xh.data(), n);
     write_info(iters, err, t1 - t0);
+  } else if (cmd == "trisolve") {  // -> tri_<tag>_<0|1>.f64: inplace_solve of b with A / trans(A)
+    viennacl::compressed_matrix<double> M;
+    fill_matrix(A, M);
+    std::vector<double> bh = load<double>("b.f64", n);
+    const char *names[4] = {"lower", "upper", "unit_lower", "unit_upper"};
+    for (int t = 0; t < 2; ++t)
+      for (int tg = 0; tg < 4; ++tg) {
+        viennacl::vector<double> z(n);
+        to_vcl(bh, z);
+        if (t == 0) {
+          if (tg == 0) viennacl::linalg::inplace_solve(M, z, viennacl::linalg::lower_tag());
+          if (tg == 1) viennacl::linalg::inplace_solve(M, z, viennacl::linalg::upper_tag());
+          if (tg == 2) viennacl::linalg::inplace_solve(M, z, viennacl::linalg::unit_lower_tag());
+          if (tg == 3) viennacl::linalg::inplace_solve(M, z, viennacl::linalg::unit_upper_tag());
+        } else {
+          if (tg == 0) viennacl::linalg::inplace_solve(trans(M), z, viennacl::linalg::lower_tag());
+          if (tg == 1) viennacl::linalg::inplace_solve(trans(M), z, viennacl::linalg::upper_tag());
+          if (tg == 2)
+            viennacl::linalg::inplace_solve(trans(M), z, viennacl::linalg::unit_lower_tag());
+          if (tg == 3)
+            viennacl::linalg::inplace_solve(trans(M), z, viennacl::linalg::unit_upper_tag());
+        }
+        std::vector<double> zh = from_vcl(z);
+        save(std::string("tri_") + names[tg] + "_" + char('0' + t) + ".f64", zh.data(), n);
+      }
   } else if (cmd == "ilu0") {  // -> lu.f64, udiag.f64, L_*/U_* level arrays, z.f64 (apply to b)
     viennacl::compressed_matrix<double> LU;
     fill_matrix(A, LU);

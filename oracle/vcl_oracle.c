@@ -1010,8 +1010,8 @@ static vo_u32 vo_gmres_max_restarts(const vo_tag *t) {
   return ret;
 }
 
-void vo_gmres_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, const double *b,
-                double *x, vo_tag *tag) {
+static void vo_gmres_pipelined(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                               const double *b, double *x, vo_tag *tag) {
   vo_u32 K = tag->krylov_dim;
   size_t bytes = sizeof(double) * (n ? n : 1);
   double *r = (double *)malloc(bytes);
@@ -1104,6 +1104,232 @@ void vo_gmres_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, c
     tag->error = fabs(rho * rho_0 / norm_rhs);
   }
   free(r); free(V); free(R); free(xi); free(eta); free(h);
+}
+
+/* ------------------------------------------------------------------------ */
+/* GMRES with a preconditioner -- the Householder "simpler GMRES" of        */
+/* gmres.hpp:449-631 (detail::solve_impl for any preconditioner), with the  */
+/* reflector set-up of gmres.hpp:131-157 and the reflection of :161-166.    */
+/* Every reflection is an inner product followed by an axpy, one after the  */
+/* other, as the reference applies them.                                    */
+/* ------------------------------------------------------------------------ */
+static void vo_hh_reflect(vo_u32 n, double *xv, const double *h, double beta) {
+  double s = beta * vo_dot_d(n, h, xv);
+  long i;
+#pragma omp parallel for if (n > VO_OMP_MIN)
+  for (i = 0; i < (long)n; ++i) xv[i] -= s * h[i];
+}
+
+/* gmres_setup_householder_vector: h = (0..0, 1, v[j+1..]/h0), beta, mu */
+static void vo_hh_setup(vo_u32 n, const double *vin, double *h, double *beta, double *mu,
+                        vo_u32 j) {
+  double input_j = vin[j];
+  memset(h, 0, sizeof(double) * n);
+  for (vo_u32 i = j + 1; i < n; ++i) h[i] = vin[i];
+  double sigma = sqrt(vo_dot_d(n, h, h));
+  sigma *= sigma;
+  if (sigma <= 0) {
+    *beta = 0;
+    *mu = input_j;
+  } else {
+    *mu = sqrt(sigma + input_j * input_j);
+    double h0 = (input_j <= 0) ? (input_j - *mu) : (-sigma / (input_j + *mu));
+    *beta = 2.0 * h0 * h0 / (sigma + h0 * h0);
+    long i;
+#pragma omp parallel for if (n > VO_OMP_MIN)
+    for (i = 0; i < (long)n; ++i) h[i] /= h0;
+    h[j] = 1.0;
+  }
+}
+
+/* When set, a clamp of res[k] to +-rho (gmres.hpp:575-578) ends the cycle
+ * without the convergence verdict that rho = 0 gives in the reference; the
+ * next restart's residual, computed from x, decides (the engine's rule). */
+static int vo_gmres_clamp_restart = 0;
+void vo_set_gmres_clamp_restart(int on) { vo_gmres_clamp_restart = on; }
+
+static void vo_gmres_householder(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                                 const double *b, double *x, vo_tag *tag, const vo_precond *P) {
+  vo_u32 K = tag->krylov_dim < n ? tag->krylov_dim : n;
+  size_t nn = n ? n : 1;
+  double *res = (double *)malloc(sizeof(double) * nn);
+  double *vk = (double *)malloc(sizeof(double) * nn);
+  double *tmp = (double *)malloc(sizeof(double) * nn);
+  double *H = (double *)calloc(nn * (K ? K : 1), sizeof(double));
+  double *R = (double *)calloc((size_t)(K ? K : 1) * (K ? K : 1), sizeof(double));
+  double *proj = (double *)calloc(K ? K : 1, sizeof(double));
+  double *betas = (double *)calloc(K ? K : 1, sizeof(double));
+  long i;
+  memset(x, 0, sizeof(double) * n);
+  double norm_rhs = sqrt(vo_dot_d(n, b, b));
+  tag->error = 0;
+  if (norm_rhs <= tag->abs_tol) goto done;
+  tag->iters = 0;
+  for (vo_u32 it = 0; it <= vo_gmres_max_restarts(tag); ++it) {
+    vo_csr_spmv_d(n, rp, ci, v, x, 1.0, 0.0, res);
+#pragma omp parallel for if (n > VO_OMP_MIN)
+    for (i = 0; i < (long)n; ++i) res[i] = b[i] - res[i];
+    vo_precond_apply_d(n, P, res);
+    double rho_0 = sqrt(vo_dot_d(n, res, res));
+    if (rho_0 / norm_rhs < tag->tol || rho_0 < tag->abs_tol) {
+      tag->error = rho_0 / norm_rhs;
+      goto done;
+    }
+#pragma omp parallel for if (n > VO_OMP_MIN)
+    for (i = 0; i < (long)n; ++i) res[i] /= rho_0;
+    double rho = 1.0;
+    int lost = 0;
+    vo_u32 k;
+    for (k = 0; k < K; ++k) {
+      tag->iters += 1;
+      double *Rk = R + (size_t)k * K, *Hk = H + (size_t)k * nn;
+      memset(Rk, 0, sizeof(double) * K);
+      memset(Hk, 0, sizeof(double) * nn);
+      if (k == 0) {
+        vo_csr_spmv_d(n, rp, ci, v, res, 1.0, 0.0, vk);
+        vo_precond_apply_d(n, P, vk);
+      } else {
+        memset(vk, 0, sizeof(double) * n);
+        vk[k - 1] = 1.0;
+        for (int q = (int)k - 1; q > -1; --q) vo_hh_reflect(n, vk, H + (size_t)q * nn, betas[q]);
+        vo_csr_spmv_d(n, rp, ci, v, vk, 1.0, 0.0, tmp);
+        vo_precond_apply_d(n, P, tmp);
+        memcpy(vk, tmp, sizeof(double) * n);
+        for (vo_u32 q = 0; q < k; ++q) vo_hh_reflect(n, vk, H + (size_t)q * nn, betas[q]);
+      }
+      double rho_kk = 0;
+      vo_hh_setup(n, vk, Hk, &betas[k], &rho_kk, k);
+      for (vo_u32 q = 0; q < k; ++q) Rk[q] = vk[q];
+      Rk[k] = rho_kk;
+      vo_hh_reflect(n, res, Hk, betas[k]);
+      int clamped = res[k] >= rho || res[k] <= -rho;
+      if (res[k] > rho) res[k] = rho;
+      if (res[k] < -rho) res[k] = -rho;
+      proj[k] = res[k];
+      rho *= sin(acos(proj[k] / rho));
+      if (clamped && vo_gmres_clamp_restart) {
+        lost = 1;
+        ++k;
+        break;
+      }
+      if (fabs(rho * rho_0 / norm_rhs) < tag->tol) {
+        tag->error = fabs(rho * rho_0 / norm_rhs);
+        ++k;
+        break;
+      }
+    }
+    /* triangular solve with R stored by columns (R[j][i] = row i of column j) */
+    for (int i2 = (int)k - 1; i2 > -1; --i2) {
+      vo_u32 q = (vo_u32)i2;
+      for (vo_u32 j = q + 1; j < k; ++j) proj[q] -= R[(size_t)j * K + q] * proj[j];
+      proj[q] /= R[(size_t)q * K + q];
+    }
+#pragma omp parallel for if (n > VO_OMP_MIN)
+    for (i = 0; i < (long)n; ++i) res[i] *= proj[0];
+    if (k > 0)
+      for (vo_u32 q = 0; q + 1 < k; ++q) res[q] += proj[q + 1];
+    for (int q = (int)k - 1; q >= 0; --q) vo_hh_reflect(n, res, H + (size_t)q * nn, betas[q]);
+#pragma omp parallel for if (n > VO_OMP_MIN)
+    for (i = 0; i < (long)n; ++i) x[i] += res[i] * rho_0;
+    tag->error = fabs(rho * rho_0 / norm_rhs);
+    if (tag->error < tag->tol && !lost) goto done;
+  }
+done:
+  free(res); free(vk); free(tmp); free(H); free(R); free(proj); free(betas);
+}
+
+/* linalg::solve(A, b, gmres_tag[, precond]): the pipelined variant without a
+ * preconditioner (gmres.hpp:369-433 dispatch), the Householder one with. */
+void vo_gmres_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, const double *b,
+                double *x, vo_tag *tag, const vo_precond *P) {
+  if (!P || P->kind == VO_PRECOND_NONE)
+    vo_gmres_pipelined(n, rp, ci, v, b, x, tag);
+  else
+    vo_gmres_householder(n, rp, ci, v, b, x, tag, P);
+}
+
+/* ------------------------------------------------------------------------ */
+/* CSR triangular solves inplace_solve(A, vec, tag) and                      */
+/* inplace_solve(trans(A), vec, tag): host_based/sparse_matrix_operations.hpp */
+/* :537-641 (csr_inplace_solve) and :734-871 (csr_trans_inplace_solve).      */
+/* tag: 0 lower, 1 upper, 2 unit_lower, 3 unit_upper.  Entries outside the   */
+/* tag's strict triangle are ignored; the lower/upper forms divide by the     */
+/* row's diagonal entry (the last one in the row; the transposed forms the    */
+/* first one in the column's storage), 0 when absent, as the reference.      */
+/* ------------------------------------------------------------------------ */
+void vo_csr_inplace_solve_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                            double *vec, int tag, int trans) {
+  if (!trans) {
+    if (tag == 2) {  /* unit_lower: rows 1..n-1 */
+      for (vo_u32 row = 1; row < n; ++row) {
+        double e = vec[row];
+        for (vo_u32 k = rp[row]; k < rp[row + 1]; ++k)
+          if (ci[k] < row) e -= vec[ci[k]] * v[k];
+        vec[row] = e;
+      }
+    } else if (tag == 0) {  /* lower */
+      for (vo_u32 row = 0; row < n; ++row) {
+        double e = vec[row], d = 0;
+        for (vo_u32 k = rp[row]; k < rp[row + 1]; ++k) {
+          if (ci[k] < row) e -= vec[ci[k]] * v[k];
+          else if (ci[k] == row) d = v[k];
+        }
+        vec[row] = e / d;
+      }
+    } else if (tag == 3) {  /* unit_upper: rows n-2..0 */
+      for (vo_u32 r2 = 1; r2 < n; ++r2) {
+        vo_u32 row = n - r2 - 1;
+        double e = vec[row];
+        for (vo_u32 k = rp[row]; k < rp[row + 1]; ++k)
+          if (ci[k] > row) e -= vec[ci[k]] * v[k];
+        vec[row] = e;
+      }
+    } else {  /* upper */
+      for (vo_u32 r2 = 0; r2 < n; ++r2) {
+        vo_u32 row = n - r2 - 1;
+        double e = vec[row], d = 0;
+        for (vo_u32 k = rp[row]; k < rp[row + 1]; ++k) {
+          if (ci[k] > row) e -= vec[ci[k]] * v[k];
+          else if (ci[k] == row) d = v[k];
+        }
+        vec[row] = e / d;
+      }
+    }
+    return;
+  }
+  /* transposed: column-oriented updates on the rows of A */
+  if (tag == 2 || tag == 0) {
+    for (vo_u32 col = 0; col < n; ++col) {
+      double e;
+      if (tag == 0) {
+        double d = 0;
+        for (vo_u32 k = rp[col]; k < rp[col + 1]; ++k)
+          if (ci[k] == col) { d = v[k]; break; }
+        e = vec[col] / d;
+        vec[col] = e;
+      } else {
+        e = vec[col];
+      }
+      for (vo_u32 k = rp[col]; k < rp[col + 1]; ++k)
+        if (ci[k] > col) vec[ci[k]] -= e * v[k];
+    }
+  } else {
+    for (vo_u32 c2 = 0; c2 < n; ++c2) {
+      vo_u32 col = n - c2 - 1;
+      double e;
+      if (tag == 1) {
+        double d = 0;
+        for (vo_u32 k = rp[col]; k < rp[col + 1]; ++k)
+          if (ci[k] == col) { d = v[k]; break; }
+        e = vec[col] / d;
+        vec[col] = e;
+      } else {
+        e = vec[col];
+      }
+      for (vo_u32 k = rp[col]; k < rp[col + 1]; ++k)
+        if (ci[k] < col) vec[ci[k]] -= e * v[k];
+    }
+  }
 }
 
 /* ------------------------------------------------------------------------ */

@@ -119,8 +119,14 @@ void vo_cg_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, cons
              double *x, vo_tag *tag, const vo_precond *P);
 void vo_bicgstab_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, const double *b,
                    double *x, vo_tag *tag, const vo_precond *P);
+/* GMRES: kind NONE runs the pipelined variant, any other kind the Householder
+ * variant of gmres.hpp:449-631, as the reference dispatches. */
 void vo_gmres_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v, const double *b,
-                double *x, vo_tag *tag);
+                double *x, vo_tag *tag, const vo_precond *P);
+/* 1: the Householder GMRES ends a cycle at a clamp of xi without declaring
+ * convergence and lets the next restart's true residual decide (the engine's
+ * rule); 0 (default): the reference's rho = 0 verdict */
+void vo_set_gmres_clamp_restart(int on);
 /* pins the GMRES restatement to the host backend's stage-1 partition */
 void vo_set_gmres_host_quirk(int on);
 /* mixed_precision_cg (FP32 inner CG, FP64 restarts), inner_tol as in the tag */
@@ -131,6 +137,11 @@ void vo_ir_jacobi_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *
                     const double *b, double *x, double tol, vo_u32 max_outer, double inner_tol,
                     vo_u32 max_inner, vo_u32 *outer_out, vo_u32 *inner_total_out,
                     double *relres_out);
+
+/* ---- CSR triangular solves (inplace_solve) ------------------------------ */
+/* tag 0 lower, 1 upper, 2 unit_lower, 3 unit_upper; trans != 0 solves with A^T */
+void vo_csr_inplace_solve_d(vo_u32 n, const vo_u32 *rp, const vo_u32 *ci, const double *v,
+                            double *vec, int tag, int trans);
 
 /* ---- ILU0 --------------------------------------------------------------- */
 /* lu holds a copy of v on entry and the ILU0 factors on exit. */

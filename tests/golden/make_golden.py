@@ -6,7 +6,7 @@ tree nor a particular numpy random stream.
 
 Run from the repository root:  python tests/golden/make_golden.py
 (python tests/golden/make_golden.py coo | row_scaling | matrix_market | cuthill_mckee |
- chow_patel | block_ilu writes only
+ chow_patel | block_ilu | gmres_precond | trisolve writes only
 that fixture; matrix_market also writes the input files under tests/golden/mm/)
 GMRES fixtures are produced with OMP_NUM_THREADS=1 (the host stage-1 kernel's
 result depends on the thread count).
@@ -98,6 +98,8 @@ def main():
         % (os.path.join(ROOT, "oracle"), os.path.join(OUT, "bicgstab_convdiff.npz"),
            os.path.join(OUT, "gmres_convdiff_1thread.npz"))], env=env, check=True)
     print("wrote gmres_convdiff_1thread.npz", out.returncode)
+    gmres_precond_fixture()
+    trisolve_fixture()
 
     # mixed_precision_cg
     rp, ci, v = gen.laplace2d(36, 36)
@@ -369,8 +371,72 @@ def block_ilu_fixture():
          iters_bicgstab_bilu8=s["iters"], error_bicgstab_bilu8=s["error"], **res)
 
 
+def gmres_precond_fixture():
+    """Preconditioned GMRES (the reference's Householder variant, gmres.hpp:449-631)
+    with Jacobi, ILU0, row scaling and Chow-Patel ILU, Krylov dimensions 30 and 10,
+    on a convection-diffusion matrix; one host thread (bit-reproducible sums)."""
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    assert oracle.have_ref(), "reference driver not built (needs the ViennaCL tree)"
+    rp, ci, v = gen.convdiff2d(48, 44, peclet=25.0, shift=0.02)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 6)
+    np.savez(os.path.join(tempfile.gettempdir(), "gmres_precond_in.npz"), rp=rp, ci=ci, v=v, b=b)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.run([sys.executable, "-c", (
+        "import sys; sys.path.insert(0, %r); import oracle, numpy as np; "
+        "d = np.load(%r); res = {}\n"
+        "for pc in ('jacobi', 'ilu0', 'row1', 'cpilu'):\n"
+        "    for kd in (30, 10):\n"
+        "        r = oracle.run_ref('gmres', d['rp'], d['ci'], d['v'], args=(1e-10, 1000, pc, kd), b=d['b'])\n"
+        "        key = '%%s_%%d' %% (pc, kd)\n"
+        "        res['x_' + key] = r['x']; res['iters_' + key] = r['iters']; res['error_' + key] = r['error']\n"
+        "np.savez_compressed(%r, rp=d['rp'], ci=d['ci'], v=d['v'], b=d['b'], tol=1e-10, "
+        "max_iters=1000, **res)")
+        % (os.path.join(ROOT, "oracle"), os.path.join(tempfile.gettempdir(), "gmres_precond_in.npz"),
+           os.path.join(OUT, "gmres_precond_convdiff.npz"))], env=env, check=True)
+    print("wrote gmres_precond_convdiff.npz")
+
+
+def trisolve_matrices():
+    """The 5x5 literal matrix of the reference's resize test (tests/src/sparse.cpp:
+    221-225), a row-scaled convection-diffusion matrix (unit diagonal, so the
+    unit-triangular solves stay bounded) and a lognormal random matrix."""
+    lit = np.array([[10.0, 0.1, 0.2, 0.3, 0.4], [1.0, 1.1, 1.2, 1.3, 1.4],
+                    [2.0, 2.1, 2.2, 2.3, 2.4], [3.0, 3.1, 3.2, 3.3, 3.4],
+                    [4.0, 4.1, 4.2, 4.3, 4.4]])
+    out = {"literal5": (np.arange(0, 26, 5, dtype=np.uint32),
+                        np.tile(np.arange(5, dtype=np.uint32), 5), lit.ravel())}
+    rp, ci, v = gen.convdiff2d(30, 28, peclet=20.0, shift=0.05)
+    d = oracle.diag(rp, ci, v)
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp.astype(np.int64)))
+    out["convdiff_scaled"] = (rp, ci, v / d[rows])
+    out["lognormal"] = gen.lognormal_random(2000, mu=2.0, sigma=0.8, hi=60, seed=21)
+    return out
+
+
+def trisolve_fixture():
+    """inplace_solve(A, b, tag) and inplace_solve(trans(A), b, tag) for the four
+    tags (host_based/sparse_matrix_operations.hpp:537-1090), b = 1 + U[0, 1)
+    as the reference's test builds its right-hand side (sparse.cpp:346)."""
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    assert oracle.have_ref(), "reference driver not built (needs the ViennaCL tree)"
+    res = {}
+    for name, (rp, ci, v) in trisolve_matrices().items():
+        b = 1.0 + np.random.default_rng(22).uniform(0, 1, len(rp) - 1)
+        r = oracle.run_ref("trisolve", rp, ci, v, b=b)
+        res.update({name + "_rp": rp, name + "_ci": ci, name + "_v": v, name + "_b": b})
+        for k in r:
+            if k.startswith("tri_"):
+                res[name + "_" + k] = r[k]
+    save("trisolve.npz", **res)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["coo"]:
+    if sys.argv[1:] == ["trisolve"]:
+        trisolve_fixture()
+    elif sys.argv[1:] == ["gmres_precond"]:
+        gmres_precond_fixture()
+    elif sys.argv[1:] == ["coo"]:
         coo_fixture()
     elif sys.argv[1:] == ["row_scaling"]:
         row_scaling_fixture()

@@ -64,6 +64,39 @@ def test_gmres_against_oracle_and_reference(V, golden):
     assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 2e-10
 
 
+@pytest.mark.parametrize("pc", ["jacobi", "ilu0", "row1", "cpilu"])
+@pytest.mark.parametrize("kd", [30, 10])
+def test_gmres_precond_golden(V, golden, pc, kd):
+    # linalg::solve(A, b, gmres_tag, precond): the reference's Householder
+    # variant (gmres.hpp:449-631) -- iterations within 2 %, x within 1e-8
+    d = golden("gmres_precond_convdiff.npz")
+    key = "%s_%d" % (pc, kd)
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    P = {"jacobi": lambda: V.jacobi_precond(A), "ilu0": lambda: V.ilu0_precond(A),
+         "row1": lambda: V.row_scaling(A, V.row_scaling_tag(1)), "cpilu": lambda: V.chow_patel_ilu_precond(A)}[pc]()
+    tag = V.gmres_tag(float(d["tol"]), int(d["max_iters"]), kd)
+    x = _np(V.solve(A, d["b"], tag, P))
+    assert tag.status() == V.SUCCESS
+    assert iters_close(tag.iters(), int(d["iters_" + key])), (tag.iters(), d["iters_" + key])
+    assert rel_err(x, d["x_" + key]) < 1e-8
+    assert tag.error() < float(d["tol"])
+    assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 1e-8
+
+
+def test_gmres_precond_iteration_cap(V, golden):
+    # max_iters 25 with Krylov dimension 10: max_restarts = 1, two cycles of 10
+    # steps, status NOT_CONVERGED and the reference's estimate
+    d = golden("gmres_precond_convdiff.npz")
+    A = V.compressed_matrix(d["rp"], d["ci"], d["v"])
+    tag = V.gmres_tag(1e-10, 25, 10)
+    V.solve(A, d["b"], tag, V.jacobi_precond(A))
+    xo, it_o, err_o = oracle.solve("gmres", d["rp"], d["ci"], d["v"], d["b"], 1e-10, 25, "jacobi",
+                                   krylov_dim=10)
+    assert tag.status() == V.NOT_CONVERGED
+    assert tag.iters() == it_o == 30
+    assert abs(tag.error() - err_o) < 1e-6 * err_o
+
+
 def test_mixed_cg_golden(V, golden):
     d = golden("mixed_cg_laplace2d.npz")
     A = V.compressed_matrix(d["rp"], d["ci"], d["v"])

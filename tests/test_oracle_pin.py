@@ -267,6 +267,33 @@ def test_gmres_converges_without_host_defect(golden):
     assert it <= int(d["iters"])
 
 
+def test_gmres_precond_golden_single_thread(golden):
+    # the Householder GMRES restatement against the reference's own runs
+    # (Jacobi, row scaling, ILU0, Chow-Patel ILU; Krylov dimensions 30, 10), one
+    # OpenMP thread in both: iteration counts equal, x and the error estimate
+    # bit-identical except with ILU0, whose level-scheduled apply sums in its
+    # own order (x to 1e-15, the estimate near 1e-10 to 1e-4 relative)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    code = (
+        "import sys; sys.path.insert(0, %r); import oracle, numpy as np\n"
+        "d = dict(np.load(%r))\n"
+        "for pc in ('jacobi', 'ilu0', 'row1', 'cpilu'):\n"
+        "    for kd in (30, 10):\n"
+        "        key = '%%s_%%d' %% (pc, kd)\n"
+        "        x, it, err = oracle.solve('gmres', d['rp'], d['ci'], d['v'], d['b'], 1e-10, 1000,\n"
+        "                                  pc, krylov_dim=kd)\n"
+        "        assert it == int(d['iters_' + key]), (key, it, d['iters_' + key])\n"
+        "        xr = d['x_' + key]\n"
+        "        assert np.linalg.norm(x - xr) <= 1e-12 * np.linalg.norm(xr), key\n"
+        "        assert abs(err - float(d['error_' + key])) <= 1e-4 * float(d['error_' + key]), key\n"
+        "        if pc != 'ilu0':\n"
+        "            assert np.array_equal(x, xr), key\n"
+        "            assert err == float(d['error_' + key]), key\n") % (
+        os.path.dirname(oracle.__file__),
+        os.path.join(os.path.dirname(__file__), "golden", "gmres_precond_convdiff.npz"))
+    subprocess.run([sys.executable, "-c", code], env=env, check=True)
+
+
 def test_mixed_cg_golden(golden):
     d = golden("mixed_cg_laplace2d.npz")
     x, it, err = oracle.solve("mixed_cg", d["rp"], d["ci"], d["v"], d["b"], float(d["tol"]),
@@ -356,3 +383,33 @@ def test_chow_patel_properties():
     D = oracle.chow_patel_ilu(drp, dci, dv, 3)
     b = gen.rhs_uniform(n, 2)
     assert np.allclose(oracle.chow_patel_apply(D, b, 2), b / D["diag_l"] / D["diag_u"], rtol=1e-15)
+
+
+@pytest.mark.parametrize("trans", [0, 1])
+@pytest.mark.parametrize("tag", ["lower", "upper", "unit_lower", "unit_upper"])
+@pytest.mark.parametrize("name", ["literal5", "convdiff_scaled", "lognormal"])
+def test_inplace_solve_golden(golden, name, tag, trans):
+    # the eight host triangular solves (host_based/sparse_matrix_operations.hpp:537-1090)
+    # restated: bit-identical to the reference's outputs
+    d = golden("trisolve.npz")
+    z = oracle.inplace_solve(d[name + "_rp"], d[name + "_ci"], d[name + "_v"], d[name + "_b"],
+                             tag, trans)
+    assert np.array_equal(z, d["%s_tri_%s_%d" % (name, tag, trans)])
+
+
+def test_gmres_clamp_false_convergence_and_restart_rule():
+    # Jacobi GMRES(30) on the configured lognormal matrix (262,144 rows): the
+    # reference's clamp of xi (gmres.hpp:575-578) ends the solve with an
+    # estimate of 0 while the true residual is 2e-3; with the engine's rule (a
+    # clamp ends the cycle, the next restart's residual decides) it converges
+    rp, ci, v = gen.lognormal_random(262144, seed=1)
+    b = gen.rhs_uniform(262144, 1)
+    try:
+        oracle.lib().vo_set_gmres_clamp_restart(0)
+        x, it, err = oracle.solve("gmres", rp, ci, v, b, 1e-10, 3000, "jacobi", krylov_dim=30)
+        assert err < 1e-10 and oracle.rel_residual(rp, ci, v, x, b) > 1e-3
+        oracle.lib().vo_set_gmres_clamp_restart(1)
+        x, it, err = oracle.solve("gmres", rp, ci, v, b, 1e-10, 3000, "jacobi", krylov_dim=30)
+        assert err < 1e-10 and oracle.rel_residual(rp, ci, v, x, b) < 1e-8
+    finally:
+        oracle.lib().vo_set_gmres_clamp_restart(0)

@@ -18,7 +18,7 @@ void cg_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Preco
 template <typename T>
 void bicgstab_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Precond *);
 template <typename T>
-void gmres_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *);
+void gmres_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Precond *);
 
 __global__ void col_count_kernel(uint64_t nnz, const uint32_t *__restrict__ ci, uint32_t *cnt) {
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
@@ -169,10 +169,7 @@ void adjoint_solve(Backend &be, Matrix &A, int solver, const Precond *P, const T
   switch (solver) {
     case 0: cg_solve<T>(be, At, dLdx, dLdb, tag, P); break;
     case 1: bicgstab_solve<T>(be, At, dLdx, dLdb, tag, P); break;
-    case 2:
-      require(!P, VCLGB_UNSUPPORTED, "GMRES runs without a preconditioner");
-      gmres_solve<T>(be, At, dLdx, dLdb, tag);
-      break;
+    case 2: gmres_solve<T>(be, At, dLdx, dLdb, tag, P); break;
     default: throw Error(VCLGB_INVALID_ARGUMENT, "solver must be 0 (CG), 1 (BiCGStab), 2 (GMRES)");
   }
   if (dLdA) {

@@ -1,6 +1,8 @@
 // api.cu -- the extern "C" entry points declared in include/vclgb.h.
 #include <algorithm>
 
+#include <cstdlib>
+
 #include "formats.hpp"
 #include "vecpass.cuh"
 
@@ -10,7 +12,7 @@ void cg_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Preco
 template <typename T>
 void bicgstab_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Precond *);
 template <typename T>
-void gmres_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *);
+void gmres_solve(Backend &, Matrix &, const T *, T *, vclgbSolverTag *, const Precond *);
 void mixed_cg_solve(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, float);
 void refined_cg_solve(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, double,
                       uint32_t, uint32_t *);
@@ -71,6 +73,7 @@ VCLGB_API vclgbStatus vclgbBackendCreate(vclgbBackend *out, void *stream) {
     be->num_sms = prop.multiProcessorCount;
     be->max_threads_per_sm = prop.maxThreadsPerMultiProcessor;
     be->max_smem_per_block = prop.sharedMemPerBlockOptin;
+    if (const char *e = std::getenv("VCLGB_PDL")) be->pdl = std::strcmp(e, "0") != 0;
     if (stream) {
       be->stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -640,6 +643,13 @@ VCLGB_API vclgbStatus vclgbPrecondApply(vclgbBackend h, vclgbPrecond P, void *ve
   return guarded(be, [&]() { precond_apply(*be, *vclgb::P(P), vec, nullptr); });
 }
 
+VCLGB_API vclgbStatus vclgbCsrInplaceSolve(vclgbBackend h, vclgbMatrix A, int tag, int transposed,
+                                           void *vec) {
+  if (!h || !A || !vec) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { csr_inplace_solve(*be, *M(A), tag, transposed != 0, vec); });
+}
+
 VCLGB_API vclgbStatus vclgbPrecondDestroy(vclgbPrecond *p) {
   if (!p || !*p) return VCLGB_INVALID_ARGUMENT;
   cudaDeviceSynchronize();
@@ -720,12 +730,14 @@ VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend h, vclgbMatrix A, const vo
 }
 
 VCLGB_API vclgbStatus vclgbSolveGMRES(vclgbBackend h, vclgbMatrix A, const void *b, void *x,
-                                      vclgbSolverTag *tag) {
+                                      vclgbSolverTag *tag, vclgbPrecond P) {
   return solve_entry(h, A, b, x, tag, [&](Backend &be, Matrix &m) {
     if (m.prec == VCLGB_FLOAT64)
-      gmres_solve<double>(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag);
+      gmres_solve<double>(be, m, static_cast<const double *>(b), static_cast<double *>(x), tag,
+                          P ? vclgb::P(P) : nullptr);
     else
-      gmres_solve<float>(be, m, static_cast<const float *>(b), static_cast<float *>(x), tag);
+      gmres_solve<float>(be, m, static_cast<const float *>(b), static_cast<float *>(x), tag,
+                         P ? vclgb::P(P) : nullptr);
   });
 }
 

@@ -51,6 +51,9 @@ std::unique_ptr<Precond> block_ilu0_create(Backend &be, const Matrix &A, uint32_
 std::unique_ptr<Precond> chow_patel_create(Backend &be, const Matrix &A, bool icc,
                                            uint32_t sweeps, uint32_t jacobi_iters);
 void chow_patel_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);
+// inplace_solve(A or trans(A), vec, tag) for a square CSR matrix; tag 0 lower,
+// 1 upper, 2 unit_lower, 3 unit_upper (precond.cu)
+void csr_inplace_solve(Backend &be, Matrix &A, int tag, bool trans, void *d_vec);
 // z = M^-1 z in place; skipped on the device when *skip_flag != 0
 void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag);
 // diag(A) into a device buffer of the matrix precision; returns 1 in *zero_found

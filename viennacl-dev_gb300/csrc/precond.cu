@@ -620,6 +620,35 @@ static void upload(Backend &be, DevBuf &dst, const std::vector<X> &src) {
                                cudaMemcpyHostToDevice, be.stream));
 }
 
+// Device copy of one triangle's level structure (pattern only): level
+// pointers, level rows, per-level row pointers and columns, and for the runs
+// of small levels the ring codes of level_run_kernel.
+template <typename T>
+static void tri_structure(Backend &be, const LevelPlan &pl, uint32_t n, Precond::Tri &tri) {
+  tri.levels = (uint32_t)(pl.level_ptr.size() - 1);
+  tri.rows = pl.row_index.size();
+  tri.nnz = pl.cols.size();
+  tri.h_level_ptr = pl.level_ptr;
+  tri.runs = n < 0x80000000u;  // codes hold a row index in an int32
+  if (tri.runs) {
+    std::vector<int32_t> ecode, xcode;
+    plan_ring_codes(pl.level_ptr, pl.row_index, pl.row_ptr, pl.cols, n, ecode, xcode);
+    upload(be, tri.ecode, ecode);
+    upload(be, tri.xcode, xcode);
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // host codes freed after use
+    VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel, 1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(kRingSlots * sizeof(T))));
+    VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel / 2, 4>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(kRingSlots * sizeof(T))));
+  }
+  upload(be, tri.level_ptr, pl.level_ptr);
+  upload(be, tri.row_index, pl.row_index);
+  upload(be, tri.row_ptr, pl.row_ptr);
+  upload(be, tri.cols, pl.cols);
+}
+
 template <typename T>
 static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
   const uint32_t n = A.rows;
@@ -682,28 +711,7 @@ static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
     extract_diag(be, tmp, P.diag, false);
   }
   auto fill_tri = [&](LevelPlan &pl, Precond::Tri &tri, bool upper) {
-    tri.levels = (uint32_t)(pl.level_ptr.size() - 1);
-    tri.rows = pl.row_index.size();
-    tri.nnz = pl.cols.size();
-    tri.h_level_ptr = pl.level_ptr;
-    tri.runs = n < 0x80000000u;  // codes hold a row index in an int32
-    if (tri.runs) {
-      std::vector<int32_t> ecode, xcode;
-      plan_ring_codes(pl.level_ptr, pl.row_index, pl.row_ptr, pl.cols, n, ecode, xcode);
-      upload(be, tri.ecode, ecode);
-      upload(be, tri.xcode, xcode);
-      VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // host codes freed after use
-      VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel, 1>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(kRingSlots * sizeof(T))));
-      VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel / 2, 4>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(kRingSlots * sizeof(T))));
-    }
-    upload(be, tri.level_ptr, pl.level_ptr);
-    upload(be, tri.row_index, pl.row_index);
-    upload(be, tri.row_ptr, pl.row_ptr);
-    upload(be, tri.cols, pl.cols);
+    tri_structure<T>(be, pl, n, tri);
     DevBuf src, roe;
     upload(be, src, pl.src);
     upload(be, roe, pl.row_of_entry);
@@ -898,6 +906,97 @@ static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *s
     ++L;
   }
   VCLGB_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// CSR triangular solves: inplace_solve(A, vec, tag) and inplace_solve(trans(A),
+// vec, tag) (linalg/host_based/sparse_matrix_operations.hpp:537-1090; the CUDA
+// backend runs them as one block of 128 threads, linalg/cuda/
+// sparse_matrix_operations.hpp:780-1008).  The rows of the tag's strict
+// triangle are put in levels as the ILU0 substitution's are (a row's level is
+// one more than the deepest level among its columns), so each level is one
+// parallel step: runs of small levels in one block (level_run_kernel), wide
+// levels grid-wide.  The non-unit forms divide the right-hand side by the
+// diagonal first and substitute with the entries divided by their row's
+// diagonal (x_r = b_r/d_r - sum (a_rc/d_r) x_c, as the ILU0 U solve does);
+// the unit forms use the entries as they are.  trans(A) runs the same on the
+// pattern of A^T (transpose map of the adjoint), its entries read from A.
+// The level structure depends on the pattern only and is cached on the
+// matrix; the values are gathered again at every call.
+// ---------------------------------------------------------------------------
+struct TriSolvePlan {
+  Precond::Tri tri;
+  DevBuf src, roe;  // entry of A behind each level entry, and the entry's row
+  DevBuf diag;
+};
+
+template <typename T>
+static void csr_inplace_solve_t(Backend &be, Matrix &A, int tag, bool trans, T *vec) {
+  const bool upper = tag == 1 || tag == 3, unit = tag >= 2;
+  const uint32_t n = A.rows;
+  auto &slot = A.tri_plan[(upper ? 1 : 0) | (trans ? 2 : 0)];
+  if (!slot) {
+    auto plan = std::make_shared<TriSolvePlan>();
+    std::vector<uint32_t> rp(n + 1), ci(A.nnz), map;
+    if (trans) {
+      DevBuf trp, tci, m;
+      csr_transpose_pattern(be, A.rows, A.cols, A.nnz, A.row_ptr, A.col_idx, trp, tci, m);
+      map.resize(A.nnz);
+      VCLGB_CUDA(cudaMemcpyAsync(rp.data(), trp.ptr, rp.size() * 4, cudaMemcpyDeviceToHost,
+                                 be.stream));
+      if (A.nnz) {
+        VCLGB_CUDA(cudaMemcpyAsync(ci.data(), tci.ptr, ci.size() * 4, cudaMemcpyDeviceToHost,
+                                   be.stream));
+        VCLGB_CUDA(cudaMemcpyAsync(map.data(), m.ptr, map.size() * 4, cudaMemcpyDeviceToHost,
+                                   be.stream));
+      }
+      VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    } else {
+      VCLGB_CUDA(cudaMemcpyAsync(rp.data(), A.row_ptr, rp.size() * 4, cudaMemcpyDeviceToHost,
+                                 be.stream));
+      if (A.nnz)
+        VCLGB_CUDA(cudaMemcpyAsync(ci.data(), A.col_idx, ci.size() * 4, cudaMemcpyDeviceToHost,
+                                   be.stream));
+      VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    }
+    LevelPlan pl = plan_levels(n, rp, ci, upper, nullptr);
+    if (trans)
+      for (auto &k : pl.src) k = map[k];
+    tri_structure<T>(be, pl, n, plan->tri);
+    upload(be, plan->src, pl.src);
+    upload(be, plan->roe, pl.row_of_entry);
+    plan->tri.vals.alloc(std::max<uint64_t>(plan->tri.nnz, 1) * sizeof(T), be.stream);
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // host plan freed after the uploads
+    slot = std::move(plan);
+  }
+  TriSolvePlan &P = *slot;
+  if (!unit) extract_diag(be, A, P.diag, false);
+  if (P.tri.nnz) {
+    const int g = waves_grid(be, 256, 8, P.tri.nnz);
+    level_vals_kernel<T><<<g, 256, 0, be.stream>>>(
+        P.tri.nnz, P.src.as<uint32_t>(), P.roe.as<uint32_t>(), static_cast<const T *>(A.values),
+        unit ? nullptr : P.diag.as<T>(), P.tri.vals.as<T>());
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+  }
+  if (!unit && n) {
+    const int g = waves_grid(be, 256, 8, n);
+    div_kernel<T><<<g, 256, 0, be.stream>>>(n, vec, P.diag.as<T>(), nullptr);
+    be.launches++;
+    VCLGB_CHECK_LAUNCH();
+  }
+  tri_apply<T>(be, P.tri, vec, nullptr);
+}
+
+void csr_inplace_solve(Backend &be, Matrix &A, int tag, bool trans, void *d_vec) {
+  require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "inplace_solve takes a CSR matrix");
+  require(A.rows == A.cols, VCLGB_INVALID_ARGUMENT, "inplace_solve needs a square matrix");
+  require(tag >= 0 && tag <= 3, VCLGB_INVALID_ARGUMENT,
+          "tag must be 0 lower, 1 upper, 2 unit_lower or 3 unit_upper");
+  if (A.prec == VCLGB_FLOAT64)
+    csr_inplace_solve_t<double>(be, A, tag, trans, static_cast<double *>(d_vec));
+  else
+    csr_inplace_solve_t<float>(be, A, tag, trans, static_cast<float *>(d_vec));
 }
 
 void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_flag) {

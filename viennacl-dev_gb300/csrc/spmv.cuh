@@ -177,6 +177,8 @@ template <int LANES, int MPL, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads, (E::NDOT > 0 && E::NDOT <= 2) ? 8 : 0)
     csr_fixed_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc, E epi,
                      T *partials, unsigned *counter) {
+  pdl_trigger();
+  pdl_wait();
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   T dots[DotArr<E::NDOT>::n];
@@ -232,6 +234,8 @@ template <typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     csr_window_kernel(CsrView<T> A, const T *__restrict__ x, int64_t xs, int64_t xinc, E epi,
                       T *partials, unsigned *counter) {
+  pdl_trigger();
+  pdl_wait();
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   __shared__ uint32_t lists[kWinRows];
@@ -419,6 +423,8 @@ __global__ void __launch_bounds__(kSpmvThreads)
     ell_kernel(uint32_t rows, uint32_t width, const uint32_t *__restrict__ coords,
                const T *__restrict__ elems, const T *__restrict__ x, int64_t xs, int64_t xinc,
                E epi, T *partials, unsigned *counter) {
+  pdl_trigger();
+  pdl_wait();
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   T dots[DotArr<E::NDOT>::n];
@@ -450,6 +456,8 @@ template <int ND, typename T, class E>
 __global__ void __launch_bounds__(kSpmvThreads)
     dia_kernel(uint32_t rows, uint32_t cols, DiaOffsets offs, const T *__restrict__ vals,
                const T *__restrict__ x, E epi, T *partials, unsigned *counter) {
+  pdl_trigger();
+  pdl_wait();
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   T dots[DotArr<E::NDOT>::n];
@@ -516,6 +524,8 @@ __global__ void __launch_bounds__(kSpmvThreads)
                 const T *__restrict__ elems, const uint32_t *__restrict__ perm,
                 const uint32_t *__restrict__ wide, uint32_t nwide, const T *__restrict__ x,
                 int64_t xs, int64_t xinc, E epi, T *partials, unsigned *counter) {
+  pdl_trigger();
+  pdl_wait();
   if (epi.skip()) return;
   __shared__ T smem[3 * (kSpmvThreads / 32) + 8];
   T dots[DotArr<E::NDOT>::n];
@@ -765,9 +775,9 @@ template <typename T, class E>
 void ell_launch(Backend &be, int grid, const Matrix &m, const T *x, int64_t xs, int64_t xinc,
                 const E &epi, T *partials, unsigned *counter) {
 #define VCLGB_ELL(W)                                                                          \
-  ell_kernel<W, T, E><<<one_wave<ell_kernel<W, T, E>>(be, grid, kSpmvThreads), kSpmvThreads, 0, \
-                        be.stream>>>(m.rows, m.ell_width, m.ell_coords.as<uint32_t>(),          \
-                                     m.ell_elems.as<T>(), x, xs, xinc, epi, partials, counter)
+  launch_kernel(be, ell_kernel<W, T, E>, one_wave<ell_kernel<W, T, E>>(be, grid, kSpmvThreads), \
+                kSpmvThreads, 0, m.rows, m.ell_width, m.ell_coords.as<uint32_t>(),              \
+                m.ell_elems.as<T>(), x, xs, xinc, epi, partials, counter)
   switch (m.ell_width) {
     case 1: VCLGB_ELL(1); break;
     case 2: VCLGB_ELL(2); break;
@@ -794,11 +804,10 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
     case VCLGB_CSR: {
       CsrView<T> A{m.row_ptr, m.col_idx, static_cast<const T *>(m.values), m.rows};
       const bool single = m.num_bins == 1 && m.bins[0].identity;
-#define VCLGB_CSR_FIXED(L, R)                                                \
-  csr_fixed_kernel<L, R, T, E><<<one_wave<csr_fixed_kernel<L, R, T, E>>(    \
-                                     be, grid, kSpmvThreads),               \
-                                 kSpmvThreads, 0, be.stream>>>(             \
-      A, x, xs, xinc, epi, partials, red.counter)
+#define VCLGB_CSR_FIXED(L, R)                                                      \
+  launch_kernel(be, csr_fixed_kernel<L, R, T, E>,                                 \
+                one_wave<csr_fixed_kernel<L, R, T, E>>(be, grid, kSpmvThreads),   \
+                kSpmvThreads, 0, A, x, xs, xinc, epi, partials, red.counter)
       const uint32_t lanes = single ? m.bins[0].lanes : 0u;
       if (lanes == 1) {
         switch (m.max_row_len) {
@@ -817,8 +826,8 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
         const size_t nwin = (m.rows + kWinRows - 1) / kWinRows;
         const int wgrid = one_wave<csr_window_kernel<T, E>>(
             be, (int)(nwin < (size_t)grid ? (nwin ? nwin : 1) : grid), kSpmvThreads);
-        csr_window_kernel<T, E><<<wgrid, kSpmvThreads, 0, be.stream>>>(A, x, xs, xinc, epi,
-                                                                       partials, red.counter);
+        launch_kernel(be, csr_window_kernel<T, E>, wgrid, kSpmvThreads, 0, A, x, xs, xinc, epi,
+                      partials, red.counter);
       }
 #undef VCLGB_CSR_FIXED
       break;
@@ -834,9 +843,9 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
         o.n = (int)m.dia_ndiag;
         for (int d = 0; d < kMaxDiag; ++d) o.off[d] = m.dia_off[d];
 #define VCLGB_DIA(ND)                                                                        \
-  dia_kernel<ND, T, E><<<one_wave<dia_kernel<ND, T, E>>(be, grid, kSpmvThreads), kSpmvThreads, \
-                         0, be.stream>>>(m.rows, m.cols, o, m.dia_vals.as<T>(), x, epi,       \
-                                         partials, red.counter)
+  launch_kernel(be, dia_kernel<ND, T, E>, one_wave<dia_kernel<ND, T, E>>(be, grid, kSpmvThreads), \
+                kSpmvThreads, 0, m.rows, m.cols, o, m.dia_vals.as<T>(), x, epi, partials,     \
+                red.counter)
         switch (o.n) {
           case 3: VCLGB_DIA(3); break;
           case 5: VCLGB_DIA(5); break;
@@ -852,15 +861,15 @@ void spmv_launch(Backend &be, const Matrix &m, const T *x, int64_t xs, int64_t x
     }
     case VCLGB_SELL:
       if (m.C % 32 == 0)
-        sell_kernel<true, T, E><<<one_wave<sell_kernel<true, T, E>>(be, grid, kSpmvThreads),
-                                  kSpmvThreads, 0, be.stream>>>(
+        launch_kernel(be, sell_kernel<true, T, E>,
+                      one_wave<sell_kernel<true, T, E>>(be, grid, kSpmvThreads), kSpmvThreads, 0,
             m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
             m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
             m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, m.sell_wide.as<uint32_t>(),
             m.sell_nwide, x, xs, xinc, epi, partials, red.counter);
       else
-        sell_kernel<false, T, E><<<one_wave<sell_kernel<false, T, E>>(be, grid, kSpmvThreads),
-                                   kSpmvThreads, 0, be.stream>>>(
+        launch_kernel(be, sell_kernel<false, T, E>,
+                      one_wave<sell_kernel<false, T, E>>(be, grid, kSpmvThreads), kSpmvThreads, 0,
             m.rows, m.C, m.sell_cpb.as<uint32_t>(), m.sell_start.as<uint32_t>(),
             m.sell_cols.as<uint32_t>(), m.sell_elems.as<T>(),
             m.sigma > 1 ? m.sell_perm.as<uint32_t>() : nullptr, nullptr, 0u, x, xs, xinc, epi,

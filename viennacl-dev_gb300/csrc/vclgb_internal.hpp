@@ -114,7 +114,31 @@ struct Backend {
   std::vector<int> tev_kind;      // kind of pair k: 0 SpMV, 1 vector pass
   size_t tev_used = 0;            // events recorded since the last collection
   std::vector<float> times[2];
+  // programmatic dependent launch for the solver kernels (on unless the
+  // environment sets VCLGB_PDL=0): a kernel's blocks may start while the
+  // previous kernel on the stream finishes, and wait for it on the device
+  bool pdl = true;
 };
+
+// Launches kern<<<grid, block, smem, be.stream>>>(args...), with programmatic
+// dependent launch when the backend allows it.  Every kernel launched through
+// here calls pdl_wait() before it reads anything the previous kernel on the
+// stream may write (without the attribute that wait returns at once).
+template <typename... KArgs, typename... Args>
+inline void launch_kernel(Backend &be, void (*kern)(KArgs...), int grid, int block, size_t smem,
+                          Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = be.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = be.pdl ? 1 : 0;
+  VCLGB_CUDA(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+}
 
 // Starts a timed region of `kind` on the backend's stream; returns the pair
 // index, or -1 when timing is off.
@@ -225,6 +249,7 @@ constexpr int kMaxBins = 8;
 constexpr uint32_t kSellWide = 128;
 
 struct Transposed;  // adjoint.cu: A^T and its entry map
+struct TriSolvePlan;  // precond.cu: level structure of one triangle for inplace_solve
 
 // DIA: an internal format only (no ViennaCL counterpart), the refined
 // solver's FP32 inner copy of a matrix whose entries lie on a few diagonals
@@ -294,6 +319,8 @@ struct Matrix {
   DevBuf inv_sqrt_diag;
   // cached transpose for the adjoint solve
   std::shared_ptr<Transposed> transposed;
+  // level structures of the triangular solves, by (upper, transposed)
+  std::shared_ptr<TriSolvePlan> tri_plan[4];
   // diagonal (FP64 or FP32), built on demand for Jacobi
   DevBuf diag;
   bool diag_built = false;
@@ -333,6 +360,16 @@ struct Precond {
 // device helpers
 // ---------------------------------------------------------------------------
 #ifdef __CUDACC__
+// Programmatic dependent launch: pdl_trigger lets the next kernel on the
+// stream start its blocks (they occupy SM slots only as this kernel's blocks
+// leave); pdl_wait blocks until the previous kernel has finished and its
+// writes are visible (at once when this kernel was launched without the
+// attribute).
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

@@ -12,6 +12,8 @@ constexpr int kVecThreads = 256;
 template <typename T, class F>
 __global__ void __launch_bounds__(kVecThreads)
     vec_pass_kernel(size_t n, F f, T *partials, unsigned *counter) {
+  pdl_trigger();
+  pdl_wait();
   if (f.skip()) return;
   __shared__ T smem[DotArr<F::NDOT>::n * kVecThreads];
   T dots[DotArr<F::NDOT>::n];
@@ -37,9 +39,9 @@ inline int vec_grid(const Backend &be, size_t n) { return waves_grid(be, kVecThr
 template <typename T, class F>
 void vec_pass(Backend &be, size_t n, const F &f, const Reduction &red) {
   const int tp = timing_begin(be, 1);
-  vec_pass_kernel<T, F><<<one_wave<vec_pass_kernel<T, F>>(be, vec_grid(be, n), kVecThreads),
-                          kVecThreads, 0, be.stream>>>(
-      n, f, static_cast<T *>(red.partials), red.counter);
+  launch_kernel(be, vec_pass_kernel<T, F>,
+                one_wave<vec_pass_kernel<T, F>>(be, vec_grid(be, n), kVecThreads), kVecThreads, 0,
+                n, f, static_cast<T *>(red.partials), red.counter);
   be.launches++;
   VCLGB_CHECK_LAUNCH();
   timing_end(be, tp);

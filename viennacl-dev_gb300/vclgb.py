@@ -124,6 +124,7 @@ SIGNATURES = {
     "vclgbRowScalingCreate": (_I32, [_P, _P, _U32, ctypes.POINTER(_P)]),
     "vclgbIlu0Create": (_I32, [_P, _P, _I32, ctypes.POINTER(_P)]),
     "vclgbPrecondApply": (_I32, [_P, _P, _P]),
+    "vclgbCsrInplaceSolve": (_I32, [_P, _P, _I32, _I32, _P]),
     "vclgbPrecondDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbIlu0GetInfo": (_I32, [_P, ctypes.POINTER(Ilu0Info)]),
     "vclgbIlu0Export": (_I32, [_P, _P, _I32, _P]),
@@ -135,7 +136,7 @@ SIGNATURES = {
     "vclgbSolverTagInit": (None, [ctypes.POINTER(SolverTag), _I32]),
     "vclgbSolveCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
     "vclgbSolveBiCGStab": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
-    "vclgbSolveGMRES": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag)]),
+    "vclgbSolveGMRES": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _P]),
     "vclgbSolveMixedCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _F]),
     "vclgbSolveRefinedCG": (_I32, [_P, _P, _P, _P, ctypes.POINTER(SolverTag), _D, _U32,
                                    ctypes.POINTER(_U32)]),
@@ -516,6 +517,50 @@ def prod(A, x, alpha=1.0, y=None, beta=0.0, x_start=0, x_stride=1, y_start=0, y_
     return y
 
 
+# ---- triangular solves: linalg::inplace_solve(A | trans(A), vec, tag) --------
+class lower_tag:
+    """viennacl::linalg::lower_tag"""
+    code = 0
+
+
+class upper_tag:
+    """viennacl::linalg::upper_tag"""
+    code = 1
+
+
+class unit_lower_tag:
+    """viennacl::linalg::unit_lower_tag"""
+    code = 2
+
+
+class unit_upper_tag:
+    """viennacl::linalg::unit_upper_tag"""
+    code = 3
+
+
+class trans:
+    """viennacl::trans(A): the transposed operand of inplace_solve."""
+
+    def __init__(self, A):
+        self.A = A
+
+
+def inplace_solve(A, vec, tag):
+    """linalg::inplace_solve(A, vec, tag) / inplace_solve(trans(A), vec, tag) for a
+    compressed_matrix: vec (a contiguous CUDA tensor of the matrix precision) is
+    overwritten by the solution of the tag's triangle; returns vec."""
+    torch = _torch()
+    transposed = isinstance(A, trans)
+    M = A.A if transposed else A
+    if not (isinstance(vec, torch.Tensor) and vec.is_cuda and vec.dtype == M.dtype
+            and vec.is_contiguous()):
+        raise VclgbError(INVALID_ARGUMENT, "inplace_solve needs a contiguous CUDA vector "
+                         "of the matrix precision")
+    code = tag.code if hasattr(tag, "code") else int(tag)
+    M.be.check(M.be.lib.vclgbCsrInplaceSolve(M.be.h, M.h, code, int(transposed), _ptr(vec)))
+    return vec
+
+
 def inner_prod(x, y, be=None):
     """linalg::inner_prod -> device scalar (0-d tensor)."""
     torch = _torch()
@@ -778,9 +823,8 @@ def solve(A, b, tag, precond=None, x=None):
         be.check(lib.vclgbSolveBiCGStab(be.h, A.h, _ptr(b), _ptr(x), t,
                                         precond.h if precond else _P(0)), ok)
     elif isinstance(tag, gmres_tag):
-        if precond is not None:
-            raise VclgbError(UNSUPPORTED, "GMRES is provided without a preconditioner")
-        be.check(lib.vclgbSolveGMRES(be.h, A.h, _ptr(b), _ptr(x), t), ok)
+        be.check(lib.vclgbSolveGMRES(be.h, A.h, _ptr(b), _ptr(x), t,
+                                     precond.h if precond else _P(0)), ok)
     else:
         raise TypeError("unknown solver tag")
     return x
