@@ -381,20 +381,35 @@ def secondaries(V, torch, peak, args):
     fd = torch.tensor(f, device="cuda")
     P = V.jacobi_precond(A)
     res = {}
-    for name in ("plain_fp64_jacobi_pcg", "refined_fp32_inner"):
+
+    def c3_arm(name, make_tag, precond):
         ts = []
         for rep in range(2):
-            tag = V.cg_tag(1e-10, 20000) if name.startswith("plain") else V.refined_cg_tag(1e-10, 40000, 1e-4)
+            tag = make_tag()
             torch.cuda.synchronize()
             t0 = time.time()
-            xx = V.solve(A, fd, tag, P if name.startswith("plain") else None)
+            xx = V.solve(A, fd, tag, precond)
             torch.cuda.synchronize()
             ts.append(time.time() - t0)
         res[name] = {"s": min(ts), "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
+                     "tol": tag.tolerance(),
                      "true_rel_residual": true_rel_residual(rp, ci, v, xx.cpu().numpy(), f)}
-        if not name.startswith("plain"):
+        if hasattr(tag, "outer"):
             res[name]["outer"] = tag.outer
+        return res[name]
+
+    plain = c3_arm("plain_fp64_jacobi_pcg", lambda: V.cg_tag(1e-10, 20000), P)
+    c3_arm("refined_fp32_inner", lambda: V.refined_cg_tag(1e-10, 40000, 1e-4), None)
     res["speedup"] = res["plain_fp64_jacobi_pcg"]["s"] / res["refined_fp32_inner"]["s"]
+    # Jacobi-PCG stops on <r, D^-1 r> / <b, D^-1 b> (cg.hpp:306-310), whose ratio
+    # to the true ||b - Ax|| / ||b|| is steady late in the solve: the plain arm
+    # is run again with its tolerance scaled so that its true residual is below
+    # 1e-10 as well, and the speed-up is also reported at equal true residual
+    if plain["true_rel_residual"] > 1e-10:
+        tol2 = 1e-10 * 0.9 * 1e-10 / plain["true_rel_residual"]
+        c3_arm("plain_fp64_jacobi_pcg_true_1e-10", lambda: V.cg_tag(tol2, 40000), P)
+        res["speedup_at_true_1e-10"] = (res["plain_fp64_jacobi_pcg_true_1e-10"]["s"] /
+                                        res["refined_fp32_inner"]["s"])
     sec["diffusion3d_192_mixed_vs_plain"] = res
     del A, P
     sec["ilu0_convdiff2d_512"] = bench_ilu0(V, torch)
@@ -630,7 +645,8 @@ def bench_adjoint(V, torch):
             an = gA @ ((vp - vm) / (2 * eps))
         worst = max(worst, abs(fd - an) / abs(an))
     return {"rows": n, "forward_s": t_fwd, "forward_iters": tag.iters(), "adjoint_s": t_bwd,
-            "adjoint_iters": atag.iters(), "fd_directions": 8, "fd_worst_rel_err": worst}
+            "adjoint_iters": atag.iters(), "fd_directions": 8, "fd_worst_rel_err": worst,
+            "fd_64_directions": "tests/test_gpu_adjoint.py::test_finite_differences_spd_64_directions[512]"}
 
 
 def true_rel_residual(rp, ci, v, x, b):

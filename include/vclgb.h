@@ -249,6 +249,71 @@ VCLGB_API vclgbStatus vclgbNorm2(vclgbBackend be, vclgbPrecision prec, uint64_t 
                                  const void *d_x, int64_t x_start, int64_t x_stride,
                                  void *d_result);
 
+/* ---- vector updates and element-wise operations (a vector is a device pointer
+ *      of the given precision, element i at start + i*stride) ----------------- */
+/* A scalar operand of av/avbv/element_op: a host value, or a device scalar of
+ * the vectors' precision when d_value != NULL (viennacl::scalar<T>); negated
+ * first when flip_sign != 0; divided by instead of multiplied with when
+ * reciprocal != 0 (the len/reciprocal/flip_sign arguments of
+ * linalg/vector_operations.hpp:78-183). */
+typedef struct {
+  double value;
+  const void *d_value;
+  int32_t reciprocal;
+  int32_t flip_sign;
+} vclgbScalarArg;
+
+/* av / avbv / avbv_v (linalg/vector_operations.hpp:78-183; CUDA backend
+ * linalg/cuda/vector_operations.hpp:77-760):
+ *   d_z == NULL:  y = x op alpha           (av; accumulate != 0: y += x op alpha)
+ *   otherwise:    y = x op alpha + z op beta   (avbv; accumulate != 0: y += ..., avbv_v)
+ * with op * or / by the scalar's reciprocal flag.  Every product, quotient and
+ * sum is rounded on its own (no fused multiply-add), so the result equals a
+ * host evaluation of the same expression bit for bit.  y may alias x or z
+ * element for element (same start and stride). */
+VCLGB_API vclgbStatus vclgbAvbv(vclgbBackend be, vclgbPrecision prec, uint64_t n, void *d_y,
+                                int64_t y_start, int64_t y_stride, const void *d_x,
+                                int64_t x_start, int64_t x_stride, vclgbScalarArg alpha,
+                                const void *d_z, int64_t z_start, int64_t z_stride,
+                                vclgbScalarArg beta, int accumulate);
+
+/* element_op with op_element_binary (linalg/vector_operations.hpp:255-345,
+ * linalg/detail/op_applier.hpp): y = x OP z for OP element_prod (x*z),
+ * element_div (x/z) or element_pow (pow(x, z)).  Either operand may be a
+ * scalar instead: pass d_x == NULL (then x_scalar) or d_z == NULL (then
+ * z_scalar); reciprocal is ignored there.  prod and div are correctly rounded
+ * (bit-identical to the host); pow calls CUDA's pow. */
+typedef enum { VCLGB_OP_PROD = 0, VCLGB_OP_DIV = 1, VCLGB_OP_POW = 2 } vclgbBinaryOp;
+VCLGB_API vclgbStatus vclgbElementBinary(vclgbBackend be, vclgbPrecision prec, uint64_t n,
+                                         void *d_y, int64_t y_start, int64_t y_stride,
+                                         const void *d_x, int64_t x_start, int64_t x_stride,
+                                         vclgbScalarArg x_scalar, const void *d_z,
+                                         int64_t z_start, int64_t z_stride,
+                                         vclgbScalarArg z_scalar, int op);
+
+/* element_op with op_element_unary (linalg/detail/op_applier.hpp): y = f(x)
+ * for the reference's unary functions; exp10 is exp(x ln 10) and rsqrt is
+ * pow(x, -0.5), as the reference defines them.  The functions are CUDA's own
+ * (results within its documented error bounds of the host's). */
+typedef enum {
+  VCLGB_OP_ABS = 16, VCLGB_OP_ACOS, VCLGB_OP_ACOSH, VCLGB_OP_ASIN, VCLGB_OP_ASINH,
+  VCLGB_OP_ATAN, VCLGB_OP_ATANH, VCLGB_OP_CEIL, VCLGB_OP_COS, VCLGB_OP_COSH, VCLGB_OP_ERF,
+  VCLGB_OP_ERFC, VCLGB_OP_EXP, VCLGB_OP_EXP2, VCLGB_OP_EXP10, VCLGB_OP_FABS, VCLGB_OP_FLOOR,
+  VCLGB_OP_LOG, VCLGB_OP_LOG2, VCLGB_OP_LOG10, VCLGB_OP_ROUND, VCLGB_OP_SIN, VCLGB_OP_SINH,
+  VCLGB_OP_SQRT, VCLGB_OP_TAN, VCLGB_OP_TANH, VCLGB_OP_TRUNC, VCLGB_OP_RSQRT, VCLGB_OP_SIGN
+} vclgbUnaryOp;
+VCLGB_API vclgbStatus vclgbElementUnary(vclgbBackend be, vclgbPrecision prec, uint64_t n,
+                                        void *d_y, int64_t y_start, int64_t y_stride,
+                                        const void *d_x, int64_t x_start, int64_t x_stride, int op);
+
+/* vector_assign (linalg/vector_operations.hpp:187-216): y = alpha;
+ * vector_swap (:218-250): exchanges x and y. */
+VCLGB_API vclgbStatus vclgbVectorAssign(vclgbBackend be, vclgbPrecision prec, uint64_t n, void *d_y,
+                                        int64_t y_start, int64_t y_stride, double alpha);
+VCLGB_API vclgbStatus vclgbVectorSwap(vclgbBackend be, vclgbPrecision prec, uint64_t n, void *d_x,
+                                      int64_t x_start, int64_t x_stride, void *d_y,
+                                      int64_t y_start, int64_t y_stride);
+
 /* ---- preconditioners -------------------------------------------------------- */
 typedef struct vclgbPrecond_st *vclgbPrecond;
 
@@ -469,7 +534,11 @@ VCLGB_API vclgbStatus vclgbTransposeExport(vclgbBackend be, vclgbMatrix A, int w
  * on a device looks up that array's device address with the device current
  * (a one-time set-up); make the first call before any stream capture.  All
  * calls on a device share the array and it keeps the last call's contents:
- * calls that overlap on the GPU (different streams at the same time) race. */
+ * calls that overlap on the GPU (different streams at the same time) race.
+ * A CUDA error already pending on the calling thread when the call begins is
+ * left in place for its owner (not cleared): the call then launches nothing
+ * and returns VCLGB_CUDA_ERROR; an error of this call's own launches returns
+ * VCLGB_CUDA_ERROR too. */
 VCLGB_API vclgbStatus vclgbHybSpmvNoAlloc(void *cuda_stream, vclgbPrecision prec, uint32_t rows,
                                           uint32_t ell_width, const uint32_t *d_ell_coords,
                                           const void *d_ell_elems, const uint32_t *d_tail_row_ptr,

@@ -38,10 +38,18 @@ class Precond(ctypes.Structure):
                 ("jacobi_iters", ctypes.c_uint32)]
 
 
+def reference_tree():
+    """The ViennaCL source tree the recipe (Makefile) builds the reference driver
+    against, or None where it is absent; REF=<path> in the environment overrides."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    path = r.stdout.strip()
+    return path if r.returncode == 0 and path else None
+
+
 def build():
     """Compiles liboracle.so (and the reference driver where the reference exists)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if os.path.isdir("/root/reference/viennacl"):
+    if reference_tree():
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 

@@ -66,9 +66,11 @@ def _assemble_kappa(N, kx, ky):
     return rp, ci, v
 
 
-def test_finite_differences_spd_64_directions(V):
+@pytest.mark.parametrize("N", [48, 512])
+def test_finite_differences_spd_64_directions(V, N):
+    # N = 512: the configured 512^2 diffusion problem (262,144 unknowns,
+    # per-edge lognormal kappa with contrast 1e3, seed 4)
     import torch
-    N = 48
     rp, ci, v, (kx, ky) = gen.diffusion2d_edges(N, contrast=1e3, seed=4)
     n = len(rp) - 1
     rng = np.random.default_rng(77)

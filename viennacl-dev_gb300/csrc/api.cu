@@ -73,7 +73,7 @@ VCLGB_API vclgbStatus vclgbBackendCreate(vclgbBackend *out, void *stream) {
     be->num_sms = prop.multiProcessorCount;
     be->max_threads_per_sm = prop.maxThreadsPerMultiProcessor;
     be->max_smem_per_block = prop.sharedMemPerBlockOptin;
-    if (const char *e = std::getenv("VCLGB_PDL")) be->pdl = std::strcmp(e, "0") != 0;
+    if (const char *e = std::getenv("VCLGB_PDL")) be->pdl = std::strcmp(e, "1") == 0;
     if (stream) {
       be->stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -694,6 +694,60 @@ VCLGB_API vclgbStatus vclgbIlu0Export(vclgbBackend h, vclgbPrecond p, int which,
     if (bytes) VCLGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, be->stream));
     VCLGB_CUDA(cudaStreamSynchronize(be->stream));
   });
+}
+
+// ---------------------------------------------------------------------------
+static bool bad_vec(const void *p, int64_t start, int64_t stride, uint64_t n) {
+  return n && (!p || start < 0 || stride == 0);
+}
+
+VCLGB_API vclgbStatus vclgbAvbv(vclgbBackend h, vclgbPrecision prec, uint64_t n, void *y,
+                                int64_t ys, int64_t yinc, const void *x, int64_t xs, int64_t xinc,
+                                vclgbScalarArg alpha, const void *z, int64_t zs, int64_t zinc,
+                                vclgbScalarArg beta, int accumulate) {
+  if (!h || bad_vec(y, ys, yinc, n) || bad_vec(x, xs, xinc, n) || (z && bad_vec(z, zs, zinc, n)))
+    return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    const VecArg vy{y, ys, yinc}, vx{x, xs, xinc}, vz{z, zs, zinc};
+    avbv(*be, prec, n, vy, vx, alpha, z ? &vz : nullptr, z ? &beta : nullptr, accumulate != 0);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbElementBinary(vclgbBackend h, vclgbPrecision prec, uint64_t n, void *y,
+                                         int64_t ys, int64_t yinc, const void *x, int64_t xs,
+                                         int64_t xinc, vclgbScalarArg xsc, const void *z,
+                                         int64_t zs, int64_t zinc, vclgbScalarArg zsc, int op) {
+  if (!h || bad_vec(y, ys, yinc, n) || (x && bad_vec(x, xs, xinc, n)) ||
+      (z && bad_vec(z, zs, zinc, n)))
+    return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() {
+    const VecArg vy{y, ys, yinc}, vx{x, xs, xinc}, vz{z, zs, zinc};
+    element_binary(*be, prec, n, vy, x ? &vx : nullptr, xsc, z ? &vz : nullptr, zsc, op);
+  });
+}
+
+VCLGB_API vclgbStatus vclgbElementUnary(vclgbBackend h, vclgbPrecision prec, uint64_t n, void *y,
+                                        int64_t ys, int64_t yinc, const void *x, int64_t xs,
+                                        int64_t xinc, int op) {
+  if (!h || bad_vec(y, ys, yinc, n) || bad_vec(x, xs, xinc, n)) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { element_unary(*be, prec, n, {y, ys, yinc}, {x, xs, xinc}, op); });
+}
+
+VCLGB_API vclgbStatus vclgbVectorAssign(vclgbBackend h, vclgbPrecision prec, uint64_t n, void *y,
+                                        int64_t ys, int64_t yinc, double alpha) {
+  if (!h || bad_vec(y, ys, yinc, n)) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { vector_assign(*be, prec, n, {y, ys, yinc}, alpha); });
+}
+
+VCLGB_API vclgbStatus vclgbVectorSwap(vclgbBackend h, vclgbPrecision prec, uint64_t n, void *x,
+                                      int64_t xs, int64_t xinc, void *y, int64_t ys, int64_t yinc) {
+  if (!h || bad_vec(x, xs, xinc, n) || bad_vec(y, ys, yinc, n)) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { vector_swap(*be, prec, n, {x, xs, xinc}, {y, ys, yinc}); });
 }
 
 // ---------------------------------------------------------------------------

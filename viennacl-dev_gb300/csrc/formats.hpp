@@ -60,6 +60,22 @@ void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_f
 // if a diagonal entry is zero (host-synchronising)
 void extract_diag(Backend &be, const Matrix &A, DevBuf &out, bool check_zero);
 
+// a strided vector operand: element i at p[start + i * stride]
+struct VecArg {
+  const void *p;
+  int64_t start, stride;
+};
+// vector updates and element-wise operations (blas1.cu)
+void avbv(Backend &be, vclgbPrecision prec, uint64_t n, const VecArg &y, const VecArg &x,
+          const vclgbScalarArg &a, const VecArg *z, const vclgbScalarArg *b, bool accumulate);
+void element_binary(Backend &be, vclgbPrecision prec, uint64_t n, const VecArg &y,
+                    const VecArg *x, const vclgbScalarArg &xs, const VecArg *z,
+                    const vclgbScalarArg &zs, int op);
+void element_unary(Backend &be, vclgbPrecision prec, uint64_t n, const VecArg &y,
+                   const VecArg &x, int op);
+void vector_assign(Backend &be, vclgbPrecision prec, uint64_t n, const VecArg &y, double a);
+void vector_swap(Backend &be, vclgbPrecision prec, uint64_t n, const VecArg &x, const VecArg &y);
+
 // vector reductions (blas1.cu)
 void dot_launch(Backend &be, vclgbPrecision prec, uint64_t n, const void *x, int64_t xs,
                 int64_t xinc, const void *y, int64_t ys, int64_t yinc, void *d_result,

@@ -7,6 +7,7 @@
 // carries in a fixed file-scope device array, so a call performs no
 // allocation of any kind.  The tail entry's row is found by binary search in
 // the tail row_ptr instead of a COO row array.
+#include <atomic>
 #include <mutex>
 
 #include "spmv.cuh"
@@ -26,7 +27,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 struct NoAllocDevice {
   void *scratch = nullptr;  // device address of g_noalloc_scratch on this device
   int num_sms = 0;
-  bool ready = false;
+  // set (release) once scratch and num_sms are filled in; later calls read it
+  // (acquire) without taking the set-up lock
+  std::atomic<bool> ready{false};
 };
 static NoAllocDevice g_noalloc_dev[64];
 static std::mutex g_noalloc_mutex;
@@ -174,14 +177,17 @@ extern "C" VCLGB_API vclgbStatus vclgbHybSpmvNoAlloc(
   if (!d_x || !d_y || (ell_width && (!d_ell_coords || !d_ell_elems)) ||
       (tail_nnz && (!d_tail_row_ptr || !d_tail_cols || !d_tail_vals)))
     return VCLGB_INVALID_ARGUMENT;
+  // an error left pending by an earlier call of the caller's is theirs to
+  // read: it is neither cleared nor reported as this call's, and nothing runs
+  if (cudaPeekAtLastError() != cudaSuccess) return VCLGB_CUDA_ERROR;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return VCLGB_CUDA_ERROR;
   NoAllocDevice &d = g_noalloc_dev[dev];
-  {
+  if (!d.ready.load(std::memory_order_acquire)) {
     // one-time per-device set-up with this device current: the device address
     // of the scratch array (the host-side symbol is not a device address)
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!d.ready) {
+    if (!d.ready.load(std::memory_order_relaxed)) {
       void *ptr = nullptr;
       if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr)
         return VCLGB_CUDA_ERROR;
@@ -190,7 +196,7 @@ extern "C" VCLGB_API vclgbStatus vclgbHybSpmvNoAlloc(
         return VCLGB_CUDA_ERROR;
       d.scratch = ptr;
       d.num_sms = sms;
-      d.ready = true;
+      d.ready.store(true, std::memory_order_release);
     }
   }
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);

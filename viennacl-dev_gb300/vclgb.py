@@ -56,6 +56,11 @@ class SolverTag(ctypes.Structure):
                 ("error", ctypes.c_double)]
 
 
+class ScalarArg(ctypes.Structure):
+    _fields_ = [("value", ctypes.c_double), ("d_value", ctypes.c_void_p),
+                ("reciprocal", ctypes.c_int32), ("flip_sign", ctypes.c_int32)]
+
+
 class ChowPatelInfo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("sweeps", ctypes.c_uint32),
                 ("jacobi_iters", ctypes.c_uint32), ("nnz_L", ctypes.c_uint64),
@@ -125,6 +130,13 @@ SIGNATURES = {
     "vclgbIlu0Create": (_I32, [_P, _P, _I32, ctypes.POINTER(_P)]),
     "vclgbPrecondApply": (_I32, [_P, _P, _P]),
     "vclgbCsrInplaceSolve": (_I32, [_P, _P, _I32, _I32, _P]),
+    "vclgbAvbv": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, ScalarArg, _P, _I64,
+                         _I64, ScalarArg, _I32]),
+    "vclgbElementBinary": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, ScalarArg, _P,
+                                  _I64, _I64, ScalarArg, _I32]),
+    "vclgbElementUnary": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, _I32]),
+    "vclgbVectorAssign": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _D]),
+    "vclgbVectorSwap": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64]),
     "vclgbPrecondDestroy": (_I32, [ctypes.POINTER(_P)]),
     "vclgbIlu0GetInfo": (_I32, [_P, ctypes.POINTER(Ilu0Info)]),
     "vclgbIlu0Export": (_I32, [_P, _P, _I32, _P]),
@@ -559,6 +571,116 @@ def inplace_solve(A, vec, tag):
     code = tag.code if hasattr(tag, "code") else int(tag)
     M.be.check(M.be.lib.vclgbCsrInplaceSolve(M.be.h, M.h, code, int(transposed), _ptr(vec)))
     return vec
+
+
+# ---- vector updates and element-wise operations -----------------------------
+# Vectors are CUDA tensors of one precision; a strided view is given as
+# (tensor, start, stride) with the element count n.
+def _vec(v):
+    """tensor | (tensor, start, stride) -> (tensor, start, stride)"""
+    if isinstance(v, tuple):
+        return v[0], int(v[1]), int(v[2])
+    return v, 0, 1
+
+
+def _scalar(a, reciprocal=False, flip_sign=False):
+    """a host number or a 0-d CUDA tensor (viennacl::scalar) -> ScalarArg"""
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        return ScalarArg(0.0, a.data_ptr(), int(reciprocal), int(flip_sign)), a
+    return ScalarArg(float(a), None, int(reciprocal), int(flip_sign)), None
+
+
+def _count(t, start, stride, n):
+    return int(n) if n is not None else (t.numel() - start + abs(stride) - 1) // abs(stride)
+
+
+def avbv(y, x, alpha, z=None, beta=0.0, accumulate=False, n=None, reciprocal_alpha=False,
+         flip_sign_alpha=False, reciprocal_beta=False, flip_sign_beta=False, be=None):
+    """linalg av / avbv / avbv_v: y = x*alpha [+ z*beta], or y += ... (accumulate);
+    alpha/beta host numbers or device scalars, divided by when reciprocal_*."""
+    be = be or backend()
+    (ty, ys, yi), (tx, xs, xi) = _vec(y), _vec(x)
+    sa, keep_a = _scalar(alpha, reciprocal_alpha, flip_sign_alpha)
+    sb, keep_b = _scalar(beta, reciprocal_beta, flip_sign_beta)
+    tz, zs, zi = _vec(z) if z is not None else (None, 0, 1)
+    be.check(be.lib.vclgbAvbv(be.h, _dtype_prec(ty.dtype), _count(ty, ys, yi, n), _ptr(ty), ys, yi,
+                              _ptr(tx), xs, xi, sa, _ptr(tz), zs, zi, sb, int(bool(accumulate))))
+    return ty
+
+
+def av(y, x, alpha, **kw):
+    """linalg av: y = x*alpha (x/alpha with reciprocal_alpha=True)."""
+    return avbv(y, x, alpha, **kw)
+
+
+def _binary(op, x, z, out, n, be):
+    torch = _torch()
+    be = be or backend()
+    xv = _vec(x) if isinstance(x, (torch.Tensor, tuple)) else None
+    zv = _vec(z) if isinstance(z, (torch.Tensor, tuple)) else None
+    ref = (xv or zv)[0]
+    if out is None:
+        out = torch.empty(_count(*(xv or zv), n), dtype=ref.dtype, device="cuda")
+    ty, ys, yi = _vec(out)
+    sx, kx = _scalar(x) if xv is None else (ScalarArg(), None)
+    sz, kz = _scalar(z) if zv is None else (ScalarArg(), None)
+    xv = xv or (None, 0, 1)
+    zv = zv or (None, 0, 1)
+    be.check(be.lib.vclgbElementBinary(be.h, _dtype_prec(ty.dtype), _count(ty, ys, yi, n), _ptr(ty),
+                                       ys, yi, _ptr(xv[0]), xv[1], xv[2], sx, _ptr(zv[0]), zv[1],
+                                       zv[2], sz, op))
+    return ty
+
+
+def element_prod(x, z, out=None, n=None, be=None):
+    """element_prod(x, z) (either may be a scalar)."""
+    return _binary(0, x, z, out, n, be)
+
+
+def element_div(x, z, out=None, n=None, be=None):
+    """element_div(x, z) (either may be a scalar)."""
+    return _binary(1, x, z, out, n, be)
+
+
+def element_pow(x, z, out=None, n=None, be=None):
+    """element_pow(x, z) (either may be a scalar)."""
+    return _binary(2, x, z, out, n, be)
+
+
+UNARY_OPS = ["abs", "acos", "acosh", "asin", "asinh", "atan", "atanh", "ceil", "cos", "cosh",
+             "erf", "erfc", "exp", "exp2", "exp10", "fabs", "floor", "log", "log2", "log10",
+             "round", "sin", "sinh", "sqrt", "tan", "tanh", "trunc", "rsqrt", "sign"]
+
+
+def element_unary(name, x, out=None, n=None, be=None):
+    """element_<name>(x) for the reference's unary element functions."""
+    torch = _torch()
+    be = be or backend()
+    tx, xs, xi = _vec(x)
+    if out is None:
+        out = torch.empty(_count(tx, xs, xi, n), dtype=tx.dtype, device="cuda")
+    ty, ys, yi = _vec(out)
+    be.check(be.lib.vclgbElementUnary(be.h, _dtype_prec(ty.dtype), _count(ty, ys, yi, n), _ptr(ty),
+                                      ys, yi, _ptr(tx), xs, xi, 16 + UNARY_OPS.index(name)))
+    return ty
+
+
+def vector_assign(y, alpha, n=None, be=None):
+    """vector_assign: y = alpha."""
+    be = be or backend()
+    ty, ys, yi = _vec(y)
+    be.check(be.lib.vclgbVectorAssign(be.h, _dtype_prec(ty.dtype), _count(ty, ys, yi, n), _ptr(ty),
+                                      ys, yi, float(alpha)))
+    return ty
+
+
+def vector_swap(x, y, n=None, be=None):
+    """vector_swap: exchanges the elements of x and y."""
+    be = be or backend()
+    (tx, xs, xi), (ty, ys, yi) = _vec(x), _vec(y)
+    be.check(be.lib.vclgbVectorSwap(be.h, _dtype_prec(tx.dtype), _count(tx, xs, xi, n), _ptr(tx),
+                                    xs, xi, _ptr(ty), ys, yi))
 
 
 def inner_prod(x, y, be=None):
