@@ -364,7 +364,10 @@ def secondaries(V, torch, peak, args):
     PJ = V.jacobi_precond(A)
     for name, tag, P in (("bicgstab", V.bicgstab_tag(1e-10, 3000), None),
                          ("gmres30", V.gmres_tag(1e-10, 3000, 30), None),
-                         ("bicgstab_jacobi", V.bicgstab_tag(1e-10, 3000), PJ)):
+                         ("bicgstab_jacobi", V.bicgstab_tag(1e-10, 3000), PJ),
+                         ("gmres30_jacobi", V.gmres_tag(1e-10, 3000, 30), PJ),
+                         ("bicgstab_jacobi_1e-12", V.bicgstab_tag(1e-12, 3000), PJ),
+                         ("gmres30_jacobi_1e-12", V.gmres_tag(1e-12, 3000, 30), PJ)):
         torch.cuda.synchronize()
         t0 = time.time()
         xx = V.solve(A, bd, tag, P)
@@ -372,6 +375,14 @@ def secondaries(V, torch, peak, args):
         s[name] = {"s": time.time() - t0, "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
                    "error_estimate": tag.error(),
                    "true_rel_residual": true_rel_residual(rp, ci, v, xx.cpu().numpy(), b)}
+    # the oracle's runs of the same matrix and right-hand side
+    # (tests/golden/make_lognormal_solvers.py): the unpreconditioned stall, and the
+    # reference's Jacobi GMRES(30) ending falsely converged
+    ref_file = os.path.join(ROOT, "tests", "golden", "lognormal_4194304_solvers.json")
+    if os.path.exists(ref_file):
+        with open(ref_file) as fh:
+            s["oracle"] = {k: {kk: vv for kk, vv in r.items() if kk != "seconds"}
+                           for k, r in json.load(fh)["runs"].items()}
     sec["solvers_lognormal_4M"] = s
     del A
     # 192^3 variable-coefficient diffusion: refined (FP32 inner) vs plain FP64 Jacobi-PCG
@@ -586,12 +597,29 @@ def bench_batched(V, torch):
     torch.cuda.synchronize()
     t_loop = time.time() - t0
     del mats
+    # algorithmic bytes of the batch: per iteration of a system, its SpMV
+    # (12 B/nnz + 20 B/row: values, indices, row pointers, x and y) and the
+    # vector traffic of the pipelined recurrences (CG: 7 vectors; BiCGStab: two
+    # SpMVs and 13 vectors), each vector counted once per pass; a system's
+    # working set (at most 20,000 rows) stays in L2 during its solve, so this is
+    # mostly L2 traffic and the HBM fraction is a lower bound of the work rate
+    n_k = np.diff(sp.astype(np.int64))
+    nnz_k = rp.astype(np.int64)[sp[1:].astype(np.int64)] - rp.astype(np.int64)[sp[:-1].astype(np.int64)]
+    spmv_b = 12 * nnz_k + 20 * n_k
+    per_it = np.where(methods == 0, spmv_b + 56 * n_k, 2 * spmv_b + 104 * n_k)
+    alg_bytes = float(np.sum(per_it * iters.astype(np.int64)))
+    li = np.array(loop_iters, dtype=np.int64)
+    dev = np.abs(iters.astype(np.int64) - li) / np.maximum(li, 1)
     return {"systems": len(methods), "rows": int(sp[-1]), "nnz": int(rp[-1]), "generate_s": gen_s,
             "batched_s": t_batch, "loop_of_plain_solves_s": t_loop, "speedup": t_loop / t_batch,
             "tuned_block": block, "tuned_lanes": lanes, "tune_s": tune_s,
             "all_converged": bool((status == V.SUCCESS).all()),
             "iters_max": int(iters.max()), "iters_mean": float(iters.mean()),
-            "iters_equal_to_loop": int(np.sum(np.array(loop_iters) == iters))}
+            "iters_equal_to_loop": int(np.sum(li == iters)),
+            "iters_worst_rel_dev_vs_loop": {"cg": float(dev[methods == 0].max()),
+                                            "bicgstab": float(dev[methods == 1].max())},
+            "algorithmic_bytes": alg_bytes, "algorithmic_GBs": alg_bytes / t_batch / 1e9,
+            "bytes_note": "SpMV + recurrence vectors per iteration per system; mostly L2 traffic"}
 
 
 def bench_adjoint(V, torch):
@@ -772,6 +800,38 @@ def profile_kernels(args):
         torch.cuda.synchronize()
         print("profile workload done")
         return
+    if args.profile_case == "coverage":
+        # one or a few launches of every kernel family outside the headline:
+        # conversions and Jacobi-PCG (4 iterations) on the 128^3 Laplacian,
+        # pipelined BiCGStab (4 iterations) and GMRES(30) (one cycle) on 2D
+        # convection-diffusion 2048^2, a batch of 256 systems, and the adjoint's
+        # transpose and gradient on 512^2 diffusion
+        rp, ci, v = gen.laplace3d(128)
+        A = V.compressed_matrix(rp, ci, v)
+        fmts = [V.ell_matrix(A), V.sliced_ell_matrix(A, 32, 256), V.hyb_matrix(A),
+                V.coordinate_matrix(A)]
+        b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 1), device="cuda")
+        V.solve(A, b, V.cg_tag(1e-30, 4), V.jacobi_precond(A))
+        del fmts, A
+        rp, ci, v = gen.convdiff2d(2048, 2048, peclet=10.0, shift=0.01)
+        A = V.compressed_matrix(rp, ci, v)
+        b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 3), device="cuda")
+        V.solve(A, b, V.bicgstab_tag(1e-30, 4))
+        V.solve(A, b, V.gmres_tag(1e-30, 30, 30))
+        del A
+        rp, ci, v, sp, methods, bb = gen.batch_systems(256)
+        A = V.compressed_matrix(rp, ci, v)
+        bt = V.Batch(A, sp, methods)
+        bt.solve(torch.tensor(bb, device="cuda"), 1e-10, 20000)
+        del bt, A
+        rp, ci, v, _ = gen.diffusion2d_edges(512, contrast=1e3, seed=4)
+        A = V.compressed_matrix(rp, ci, v)
+        b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 4), device="cuda")
+        x = V.solve(A, b, V.cg_tag(1e-6, 300), V.jacobi_precond(A))
+        V.solve_adjoint(A, x, x - b, V.cg_tag(1e-6, 300), solver="cg")
+        torch.cuda.synchronize()
+        print("profile workload done")
+        return
     if args.profile_case == "lognormal":
         rp, ci, v = gen.lognormal_random(1 << 20, mu=2.5, sigma=1.0, hi=2000, seed=1)
         n = len(rp) - 1
@@ -806,7 +866,7 @@ def main():
     ap.add_argument("--profile-kernels", action="store_true",
                     help="run the small fixed workload used for ncu captures")
     ap.add_argument("--profile-case", default="laplace",
-                    choices=["laplace", "lognormal", "preconditioners"])
+                    choices=["laplace", "lognormal", "preconditioners", "coverage"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
