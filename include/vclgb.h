@@ -197,6 +197,29 @@ VCLGB_API vclgbStatus vclgbCsrBandwidth(vclgbBackend be, vclgbMatrix A, uint32_t
 VCLGB_API vclgbStatus vclgbMatrixToFloat32(vclgbBackend be, vclgbMatrix m, vclgbMatrix *out);
 VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m);
 
+/* Per-matrix SpMV autotuner (no reference counterpart; the reference's slice
+ * height is the caller's and its CSR kernel a fixed rule,
+ * linalg/cuda/sparse_matrix_operations.hpp:262-396).  Times the CSR kernel the
+ * row-length analysis picks (lanes per row by length class) against
+ * SELL-C-sigma for C in {32, 64} and sigma in {1, C, 256, 1024, 4096}, HYB
+ * (csr_threshold 0.8) and ELL where it pads to at most twice the nonzeros,
+ * each converted on the device and timed over ten products; forms padding
+ * beyond 8 x nnz are skipped.  The fastest is kept with the matrix: from then
+ * on vclgbSpmv and every solver's SpMV phase on `csr` run on it.  It is a
+ * converted copy: after changing the matrix's values call
+ * vclgbMatrixAutotuneClear (or tune again).  Host-synchronising. */
+typedef struct {
+  int32_t format;          /* chosen vclgbFormat (VCLGB_CSR: the CSR kernel won) */
+  uint32_t slice_height;   /* SELL: C */
+  uint32_t sigma;          /* SELL: sort window */
+  uint32_t candidates;     /* forms tried, CSR included */
+  double csr_threshold;    /* HYB: the threshold used */
+  double us_csr;           /* microseconds per product, CSR kernel */
+  double us_best;          /* microseconds per product, chosen form */
+} vclgbTuneInfo;
+VCLGB_API vclgbStatus vclgbMatrixAutotune(vclgbBackend be, vclgbMatrix csr, vclgbTuneInfo *info);
+VCLGB_API vclgbStatus vclgbMatrixAutotuneClear(vclgbMatrix csr);
+
 typedef struct {
   int32_t format;        /* vclgbFormat */
   int32_t precision;     /* vclgbPrecision */

@@ -643,6 +643,20 @@ VCLGB_API vclgbStatus vclgbPrecondApply(vclgbBackend h, vclgbPrecond P, void *ve
   return guarded(be, [&]() { precond_apply(*be, *vclgb::P(P), vec, nullptr); });
 }
 
+VCLGB_API vclgbStatus vclgbMatrixAutotune(vclgbBackend h, vclgbMatrix A, vclgbTuneInfo *info) {
+  if (!h || !A || !info) return VCLGB_INVALID_ARGUMENT;
+  Backend *be = B(h);
+  return guarded(be, [&]() { matrix_autotune(*be, *M(A), info); });
+}
+
+VCLGB_API vclgbStatus vclgbMatrixAutotuneClear(vclgbMatrix A) {
+  if (!A) return VCLGB_INVALID_ARGUMENT;
+  return guarded(nullptr, [&]() {
+    cudaDeviceSynchronize();  // no product may still read the tuned form
+    M(A)->tuned.reset();
+  });
+}
+
 VCLGB_API vclgbStatus vclgbCsrInplaceSolve(vclgbBackend h, vclgbMatrix A, int tag, int transposed,
                                            void *vec) {
   if (!h || !A || !vec) return VCLGB_INVALID_ARGUMENT;

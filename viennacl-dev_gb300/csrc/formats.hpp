@@ -60,6 +60,9 @@ void precond_apply(Backend &be, const Precond &P, void *d_vec, const int *skip_f
 // if a diagonal entry is zero (host-synchronising)
 void extract_diag(Backend &be, const Matrix &A, DevBuf &out, bool check_zero);
 
+// per-matrix SpMV autotuner (tune.cu): keeps the fastest form on A (A.tuned)
+void matrix_autotune(Backend &be, Matrix &A, vclgbTuneInfo *info);
+
 // a strided vector operand: element i at p[start + i * stride]
 struct VecArg {
   const void *p;

@@ -61,6 +61,31 @@ void extract_diag(Backend &be, const Matrix &A, DevBuf &out, bool check_zero) {
   }
 }
 
+template <typename T>
+__global__ void recip_kernel(size_t n, const T *__restrict__ d, T *inv) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    inv[i] = T(1) / d[i];
+}
+
+// 1 / diag of a diagonal preconditioner, formed once: the fused solver
+// kernels multiply by it (an FP64 division is a sequence of FP64-pipe
+// instructions on GB300; dividing every row in every iteration made the
+// Jacobi-PCG update kernel FP64-bound at a quarter of HBM speed).  The
+// products differ from the reference's element_div by at most an ulp;
+// vclgbPrecondApply keeps the division.
+static void make_inv_diag(Backend &be, Precond &P) {
+  P.inv_diag.alloc(std::max<size_t>(P.rows, 1) * (P.prec == VCLGB_FLOAT64 ? 8 : 4), be.stream);
+  if (!P.rows) return;
+  const int g = waves_grid(be, 256, 8, P.rows);
+  if (P.prec == VCLGB_FLOAT64)
+    recip_kernel<double><<<g, 256, 0, be.stream>>>(P.rows, P.diag.as<double>(), P.inv_diag.as<double>());
+  else
+    recip_kernel<float><<<g, 256, 0, be.stream>>>(P.rows, P.diag.as<float>(), P.inv_diag.as<float>());
+  be.launches++;
+  VCLGB_CHECK_LAUNCH();
+}
+
 std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A) {
   require(A.format == VCLGB_CSR, VCLGB_INVALID_ARGUMENT, "jacobi_precond is built from CSR");
   auto P = std::make_unique<Precond>();
@@ -68,6 +93,7 @@ std::unique_ptr<Precond> jacobi_create(Backend &be, const Matrix &A) {
   P->prec = A.prec;
   P->rows = A.rows;
   extract_diag(be, A, P->diag, true);
+  make_inv_diag(be, *P);
   return P;
 }
 
@@ -134,6 +160,7 @@ std::unique_ptr<Precond> row_scaling_create(Backend &be, const Matrix &A, uint32
     be.launches++;
     VCLGB_CHECK_LAUNCH();
   }
+  make_inv_diag(be, *P);
   return P;
 }
 

@@ -133,8 +133,8 @@ struct EpiCg {  // Ap = A p, <Ap,Ap>, <p,Ap>; convergence test; next alpha/beta
 // ===========================================================================
 // preconditioned CG (cg.hpp:257-322)
 // ===========================================================================
-// JAC: Jacobi fused (z = r / d); otherwise the preconditioner runs between
-// kernels.  A compile-time choice: a runtime flag let the compiler predicate
+// JAC: Jacobi fused (z = r * (1/d), the reciprocal formed once with the
+// preconditioner); otherwise the preconditioner runs between kernels.  A compile-time choice: a runtime flag let the compiler predicate
 // the FP64 division sequence into the non-Jacobi path.
 template <typename T, bool JAC>
 struct PcgInit {  // x = 0; r = b; z = b/d (or z = b); p = z; <r,z>
@@ -147,7 +147,7 @@ struct PcgInit {  // x = 0; r = b; z = b/d (or z = b); p = z; <r,z>
     T bi = b[i];
     x[i] = T(0); r[i] = bi;
     if (jacobi) {
-      T zi = bi / dg[i];
+      T zi = bi * dg[i];
       p[i] = zi;
       d[0] += bi * zi;
     } else {
@@ -217,10 +217,9 @@ __device__ __forceinline__ void pcg_check(St<T> *st, T new_ip) {
   else if (st->iters >= st->max_iters) st->done = kMaxIters;
 }
 
-// Jacobi: z = r / d is formed once per iteration here and stored; PcgP reads
-// it back.  An FP64 division is a software sequence of about ten FP64-pipe
-// instructions on GB300, so dividing again in PcgP cost more than the 8 bytes
-// per row of reading z (the write of z replaces PcgP's reads of r and d).
+// Jacobi: z = r / d is formed once per iteration here (as r times the
+// reciprocal diagonal) and stored; PcgP reads it back (the write of z replaces
+// PcgP's reads of r and d).
 template <typename T, bool JAC>
 struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (generic)
   static constexpr int NDOT = 1;
@@ -235,7 +234,7 @@ struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (ge
     T vr = r[i] - s.a * tmp[i];
     r[i] = vr;
     if (jacobi) {
-      const T zi = vr / dg[i];
+      const T zi = vr * dg[i];
       z[i] = zi;
       d[0] += vr * zi;
     } else {
@@ -308,6 +307,7 @@ struct EpiBicgAp {  // Ap = A p, <Ap, r0*>
   __device__ void finalize(const T (&s)[1]) const {
     st->iters += 1;
     st->Ap_r0 = s[0];
+    st->alpha = st->r_r0 / s[0];  // once here, not in every thread of BicgS
   }
 };
 
@@ -317,7 +317,7 @@ struct BicgS {  // alpha = <r,r0*>/<Ap,r0*>; s = r - alpha Ap; <s,s>
   T *s_; const T *r, *Ap; St<T> *st;
   struct S { T a; };
   __device__ bool skip() const { return st->done != kRunning; }
-  __device__ S load() const { return {st->r_r0 / st->Ap_r0}; }
+  __device__ S load() const { return {st->alpha}; }
   __device__ void apply(size_t i, S s, T (&d)[1]) const {
     T v = r[i] - s.a * Ap[i];
     d[0] += v * v;
@@ -426,7 +426,7 @@ struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0
   __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
     T v = pv.b - acc;
     if (jacobi) {
-      v = v / pv.d;
+      v = v * pv.d;
       p[i] = v;
       r0[i] = v;
       d[0] += v * v;
@@ -471,7 +471,7 @@ struct EpiGb1 {  // t0 = M^-1 A p (Jacobi fused); <t0, r0*> -> alpha
   __device__ bool skip() const { return st->done != kRunning; }
   __device__ Pre pre(uint32_t i) const { return {dg[i], r0[i]}; }
   __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
-    T v = acc / pv.d;
+    T v = acc * pv.d;
     t0[i] = v;
     d[0] += v * pv.r0;
   }
@@ -519,7 +519,7 @@ struct EpiGb2 {  // t1 = M^-1 A s (Jacobi fused); ||t1||^2, <t1,s> -> omega
   __device__ bool skip() const { return st->done != kRunning; }
   __device__ Pre pre(uint32_t i) const { return {dg[i], s_[i]}; }
   __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[2]) const {
-    T v = acc / pv.d;
+    T v = acc * pv.d;
     t1[i] = v;
     d[0] += v * v;
     d[1] += v * pv.s;
@@ -601,6 +601,7 @@ constexpr int kGmresMaxK = 64;
 template <typename T>
 struct Gm {  // GMRES device state
   T nrhs, rho0, rho, vnorm2;
+  T inv_rho0, inv_vnorm;  // 1/rho0, 1/||v_k||: formed once, the passes multiply
   T R[kGmresMaxK * kGmresMaxK];
   T xi[kGmresMaxK];
   T h[kGmresMaxK];
@@ -628,6 +629,7 @@ struct GmInit {
   __device__ void finalize(const T (&s)[1]) const {
     g->nrhs = sqrt(s[0]);
     g->rho0 = g->nrhs;
+    g->inv_rho0 = T(1) / g->rho0;
     g->rho = T(1);
     g->iters = 0;
     g->error = 0;
@@ -668,6 +670,7 @@ struct EpiGmResid {  // r = b - A x; rho0 = ||r||
   }
   __device__ void finalize(const T (&s)[1]) const {
     g->rho0 = sqrt(s[0]);
+    g->inv_rho0 = T(1) / g->rho0;
     gm_cycle_check(g);
   }
 };
@@ -678,8 +681,8 @@ struct GmScaleR {  // r /= rho0 (the reference scales before its convergence tes
   T *r; Gm<T> *g;
   struct S { T inv; };
   __device__ bool skip() const { return false; }
-  __device__ S load() const { return {g->rho0}; }
-  __device__ void apply(size_t i, S c, T (&)[1]) const { r[i] /= c.inv; }
+  __device__ S load() const { return {g->inv_rho0}; }
+  __device__ void apply(size_t i, S c, T (&)[1]) const { r[i] *= c.inv; }
   __device__ void finalize(const T (&)[1]) const {}
 };
 
@@ -693,7 +696,10 @@ struct EpiGmV {  // v_k = A src, ||v_k||^2 (used for k = 0)
     vk[i] = acc;
     d[0] += acc * acc;
   }
-  __device__ void finalize(const T (&s)[1]) const { g->vnorm2 = s[0]; }
+  __device__ void finalize(const T (&s)[1]) const {
+    g->vnorm2 = s[0];
+    g->inv_vnorm = T(1) / sqrt(s[0]);
+  }
 };
 
 // classical Gram-Schmidt stage 1: h_j = <v_j, v_k>, j < k, one pass over the
@@ -772,7 +778,10 @@ __global__ void __launch_bounds__(256)
     vk[i] = v;
   }
   T s[1];
-  if (grid_reduce<1, true>(d, partials, counter, smem, s)) g->vnorm2 = s[0];
+  if (grid_reduce<1, true>(d, partials, counter, smem, s)) {
+    g->vnorm2 = s[0];
+    g->inv_vnorm = T(1) / sqrt(s[0]);
+  }
 }
 
 template <typename T>
@@ -781,9 +790,9 @@ struct GmNormalize {  // R(k,k) = ||v_k||; v_k /= ||v_k||; xi_k = <r, v_k>
   T *vk; const T *r; Gm<T> *g; int k;
   struct S { T nv; };
   __device__ bool skip() const { return g->done != kRunning; }
-  __device__ S load() const { return {sqrt(g->vnorm2)}; }
+  __device__ S load() const { return {g->inv_vnorm}; }
   __device__ void apply(size_t i, S c, T (&d)[1]) const {
-    T v = vk[i] / c.nv;
+    T v = vk[i] * c.nv;  // times 1/||v_k||, formed once by the kernel before
     d[0] += r[i] * v;
     vk[i] = v;
   }
@@ -857,7 +866,7 @@ struct GmUpdateX {  // x += c0 r + sum_{j>=1} c_j v_{j-1}
 // ===========================================================================
 template <typename T>
 struct Gh {  // device state of the preconditioned GMRES
-  T nrhs, rho0, inv_rho0, rho, wnorm2, vnorm2;
+  T nrhs, rho0, inv_rho0, rho, wnorm2, vnorm2, inv_vnorm;
   T R[kGmresMaxK * kGmresMaxK];  // column k at R[k * K ...]: Q^T w, then ||w'|| at row k
   T proj[kGmresMaxK];
   T h[kGmresMaxK];
@@ -967,6 +976,7 @@ __device__ __forceinline__ void gh_w_done(Gh<T> *g, T ww) {
   g->iters += 1;  // one Krylov step (gmres.hpp:522)
   g->wnorm2 = ww;
   g->vnorm2 = ww;
+  g->inv_vnorm = T(1) / sqrt(ww);
 }
 
 template <typename T, bool JAC>
@@ -1077,6 +1087,7 @@ __global__ void __launch_bounds__(256)
   T s[1];
   if (grid_reduce<1, true>(d, partials, counter, smem, s)) {
     g->vnorm2 = s[0];
+    g->inv_vnorm = T(1) / sqrt(s[0]);
     if (!SECOND) g->reorth_skip = !(s[0] < T(0.5) * g->wnorm2);
     else g->reorth_skip = 1;
   }
@@ -1088,7 +1099,7 @@ struct GhNormalize {  // q_k = w / ||w||, xi_k = <r, q_k>; the step's stopping t
   T *q; const T *w, *r; Gh<T> *g; int k;
   struct S { T inv; };
   __device__ bool skip() const { return g->step_skip != 0; }
-  __device__ S load() const { return {T(1) / sqrt(g->vnorm2)}; }
+  __device__ S load() const { return {g->inv_vnorm}; }
   __device__ void apply(size_t i, S c, T (&d)[1]) const {
     const T v = w[i] * c.inv;
     d[0] += r[i] * v;
@@ -1274,7 +1285,7 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
     });
   } else {
     const bool jac = diag_needed(P);
-    const T *dg = jac ? P->diag.as<T>() : nullptr;
+    const T *dg = jac ? P->inv_diag.as<T>() : nullptr;  // 1 / diag
     if (jac) {
       vec_pass<T>(be, n, PcgInit<T, true>{b, dg, x, r, z, p, st}, red);
     } else {
@@ -1333,7 +1344,7 @@ void bicgstab_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *ta
     });
   } else {
     const bool jac = diag_needed(P);
-    const T *dg = jac ? P->diag.as<T>() : nullptr;
+    const T *dg = jac ? P->inv_diag.as<T>() : nullptr;  // 1 / diag
     // t0 -> Ap, t1 -> As
     vec_pass<T>(be, n, GbInit<T>{b, x, st}, red);
     const int *rskip = &st->restart_skip;
@@ -1446,16 +1457,6 @@ static void gmres_pipelined_solve(Backend &be, Matrix &A, const T *b, T *x, vclg
                                      : VCLGB_BREAKDOWN;
 }
 
-template <typename T>
-struct GhInvDiag {  // inv_d = 1 / diag (Jacobi and row scaling, formed once per solve)
-  static constexpr int NDOT = 0;
-  T *inv_d; const T *dg;
-  __device__ bool skip() const { return false; }
-  __device__ NoScal load() const { return {}; }
-  __device__ void apply(size_t i, NoScal, T (&)[1]) const { inv_d[i] = T(1) / dg[i]; }
-  __device__ void finalize(const T (&)[1]) const {}
-};
-
 // linalg::solve(A, b, gmres_tag, precond) with any preconditioner
 // (gmres.hpp:449-631); see Gh above.  Jacobi and row scaling are fused into
 // the SpMV epilogues as a multiplication by the reciprocal diagonal; any
@@ -1475,7 +1476,6 @@ static void gmres_precond_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbS
   size_t o_cnt = ws.add(64);
   const size_t ld = ((size_t)std::max<uint32_t>(n, 1) + 31) / 32 * 32;
   size_t o_r = ws.add(ld * sizeof(T)), o_w = ws.add(ld * sizeof(T));
-  size_t o_id = ws.add(jac ? ld * sizeof(T) : 0);
   size_t o_Q = ws.add(ld * K * sizeof(T));
   size_t o_hyb = ws.add(hyb_scratch_bytes(A));
   ws.commit(be);
@@ -1495,10 +1495,9 @@ static void gmres_precond_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbS
   }
   Reduction red{ws.at<void>(o_part), ws.at<unsigned>(o_cnt)};
   T *r = ws.at<T>(o_r), *w = ws.at<T>(o_w), *Q = ws.at<T>(o_Q);
-  T *inv_d = jac ? ws.at<T>(o_id) : nullptr;
+  const T *inv_d = jac ? P->inv_diag.as<T>() : nullptr;  // formed with the preconditioner
   void *hyb = ws.at<void>(o_hyb);
   const int *done = &g->done, *sskip = &g->step_skip;
-  if (jac) vec_pass<T>(be, n, GhInvDiag<T>{inv_d, P->diag.as<T>()}, red);
   vec_pass<T>(be, n, GhInit<T>{b, x, g}, red);
   T *part = static_cast<T *>(red.partials);
   const int grid = vec_grid(be, n);

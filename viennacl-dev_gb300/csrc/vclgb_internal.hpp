@@ -324,6 +324,9 @@ struct Matrix {
   std::shared_ptr<Transposed> transposed;
   // level structures of the triangular solves, by (upper, transposed)
   std::shared_ptr<TriSolvePlan> tri_plan[4];
+  // the SpMV form the autotuner picked (tune.cu); when set, every product on
+  // this matrix runs on it
+  std::unique_ptr<Matrix> tuned;
   // diagonal (FP64 or FP32), built on demand for Jacobi
   DevBuf diag;
   bool diag_built = false;
@@ -334,6 +337,7 @@ struct Precond {
   vclgbPrecision prec = VCLGB_FLOAT64;
   uint32_t rows = 0;
   DevBuf diag;   // jacobi: diag(A); ilu0: U diagonal
+  DevBuf inv_diag;  // jacobi / row scaling: 1 / diag, formed once (the solvers multiply)
   // ILU0
   bool level_scheduling = true;
   uint64_t nnz = 0;
@@ -547,6 +551,9 @@ vclgbStatus guarded(Backend *be, F &&f) {
 inline Backend *B(vclgbBackend h) { return reinterpret_cast<Backend *>(h); }
 inline Matrix *M(vclgbMatrix h) { return reinterpret_cast<Matrix *>(h); }
 inline Precond *P(vclgbPrecond h) { return reinterpret_cast<Precond *>(h); }
+
+// the form a product on m runs on: the autotuned one when there is one
+inline const Matrix &spmv_form(const Matrix &m) { return m.tuned ? *m.tuned : m; }
 
 // implemented in the .cu files
 void csr_analyse(Backend &be, Matrix &m);

@@ -29,6 +29,7 @@ STATUS_NAMES = ["SUCCESS", "GENERIC_FAILURE", "INVALID_ARGUMENT", "INVALID_MATRI
                 "ZERO_ON_DIAGONAL", "TIMEOUT", "UNSUPPORTED"]
 FLOAT32, FLOAT64 = 0, 1
 CSR, ELL, SELL, HYB, COO = 0, 1, 2, 3, 4
+FORMAT_NAMES = {CSR: "csr", ELL: "ell", SELL: "sell", HYB: "hyb", COO: "coo"}
 
 
 class VclgbError(RuntimeError):
@@ -59,6 +60,13 @@ class SolverTag(ctypes.Structure):
 class ScalarArg(ctypes.Structure):
     _fields_ = [("value", ctypes.c_double), ("d_value", ctypes.c_void_p),
                 ("reciprocal", ctypes.c_int32), ("flip_sign", ctypes.c_int32)]
+
+
+class TuneInfo(ctypes.Structure):
+    _fields_ = [("format", ctypes.c_int32), ("slice_height", ctypes.c_uint32),
+                ("sigma", ctypes.c_uint32), ("candidates", ctypes.c_uint32),
+                ("csr_threshold", ctypes.c_double), ("us_csr", ctypes.c_double),
+                ("us_best", ctypes.c_double)]
 
 
 class ChowPatelInfo(ctypes.Structure):
@@ -130,6 +138,8 @@ SIGNATURES = {
     "vclgbIlu0Create": (_I32, [_P, _P, _I32, ctypes.POINTER(_P)]),
     "vclgbPrecondApply": (_I32, [_P, _P, _P]),
     "vclgbCsrInplaceSolve": (_I32, [_P, _P, _I32, _I32, _P]),
+    "vclgbMatrixAutotune": (_I32, [_P, _P, ctypes.POINTER(TuneInfo)]),
+    "vclgbMatrixAutotuneClear": (_I32, [_P]),
     "vclgbAvbv": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, ScalarArg, _P, _I64,
                          _I64, ScalarArg, _I32]),
     "vclgbElementBinary": (_I32, [_P, _I32, _U64, _P, _I64, _I64, _P, _I64, _I64, ScalarArg, _P,
@@ -338,6 +348,19 @@ class compressed_matrix(_Matrix):
         self.be.check(self.be.lib.vclgbCsrCreate(self.be.h, _dtype_prec(dtype), n, m, int(va.numel()),
                                                  _ptr(rp), _ptr(ci), _ptr(va), ctypes.byref(h)))
         self.h = h
+
+    def autotune(self):
+        """Times the CSR kernel against SELL-C-sigma / HYB / ELL forms and keeps the
+        fastest for every later product on this matrix; returns a dict of the choice."""
+        info = TuneInfo()
+        self.be.check(self.be.lib.vclgbMatrixAutotune(self.be.h, self.h, ctypes.byref(info)))
+        return {"format": FORMAT_NAMES[info.format], "slice_height": info.slice_height,
+                "sigma": info.sigma, "csr_threshold": info.csr_threshold,
+                "candidates": info.candidates, "us_csr": info.us_csr, "us_best": info.us_best}
+
+    def autotune_clear(self):
+        """Drops the tuned form (products run on the CSR arrays again)."""
+        self.be.check(self.be.lib.vclgbMatrixAutotuneClear(self.h))
 
     def row_blocks(self):
         torch = _torch()
