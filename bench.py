@@ -336,6 +336,10 @@ def secondaries(V, torch, peak, args):
         t, g = spmv_gbs(V, M, n, nnz, 30, x, y)
         r[name] = {"us": t * 1e6, "GBs": g, "frac_of_peak": g / peak,
                    "GFLOPs": 2 * nnz / t / 1e9}
+    r["autotune"] = A.autotune()
+    t, g = spmv_gbs(V, A, n, nnz, 30, x, y)
+    r["autotuned"] = {"us": t * 1e6, "GBs": g, "frac_of_peak": g / peak}
+    A.autotune_clear()
     sec["spmv_laplace3d_128"] = r
     del A
     # 4M-row lognormal matrix
@@ -356,6 +360,11 @@ def secondaries(V, torch, peak, args):
         r[name] = {"us": t * 1e6, "GBs": g, "frac_of_peak": g / peak, "stored": int(M.info().stored)}
     r["ell"] = "skipped: max row length 2000 pads ELL to ~100 GB"
     del mats
+    # the per-matrix autotuner's choice, and the product on the chosen form
+    r["autotune"] = A.autotune()
+    t, g = spmv_gbs(V, A, n, nnz, 20, x, y)
+    r["autotuned"] = {"us": t * 1e6, "GBs": g, "frac_of_peak": g / peak}
+    A.autotune_clear()
     sec["spmv_lognormal_4M"] = r
     # BiCGStab / GMRES(30) on the lognormal matrix (no preconditioner, as configured)
     b = gen.rhs_uniform(n, 1)

@@ -32,25 +32,39 @@ struct Batch {
   const Matrix *A = nullptr;
 };
 
-template <int BS, typename T, int NV>
-__device__ __forceinline__ void cta_sum(T (&v)[NV], T *red) {
+// Block reduction of NV values whose sums thread 0 turns into the step's NS
+// scalars: a butterfly per warp, warp 0 adds the warp sums, thread 0 runs
+// step(sums, out) once and every thread reads out[] after the barrier.  Every
+// thread re-adding the warp sums and repeating the step's divisions and
+// square roots cost each iteration more FP64 work than the rows of a small
+// system (GB300's FP64 pipe is narrow).  Deterministic: fixed order.
+// red holds 4 * (BS / 32) + 8 values.
+template <int BS, int NV, int NS, typename T, class F>
+__device__ __forceinline__ void cta_step(T (&v)[NV], T *red, T (&out)[NS], F &&step) {
+  constexpr int NW = BS / 32, P = Pow2<NV>::v, SPAN = 32 / P;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NW = BS / 32;
+  const T w = warp_sum_multi<NV>(v, lane);
+  __syncthreads();  // the previous step's readers are done with red[]
+  if ((lane & (SPAN - 1)) == 0 && lane / SPAN < NV) red[(lane / SPAN) * NW + warp] = w;
+  __syncthreads();
+  if (warp == 0) {
+    T t[NV];
 #pragma unroll
-  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
-  __syncthreads();  // the previous reduction's readers are done with red[]
-  if (lane == 0) {
+    for (int i = 0; i < NV; ++i) t[i] = lane < NW ? red[i * NW + lane] : T(0);
+    const T sum = warp_sum_multi<NV>(t, lane);
+    T sums[NV];
 #pragma unroll
-    for (int i = 0; i < NV; ++i) red[i * NW + warp] = v[i];
+    for (int i = 0; i < NV; ++i) sums[i] = __shfl_sync(0xffffffffu, sum, i * SPAN);
+    if (lane == 0) {
+      T o[NS];
+      step(sums, o);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) red[4 * NW + j] = o[j];
+    }
   }
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    T s = 0;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) s += red[i * NW + w];
-    v[i] = s;  // every thread gets the same sums in the same order
-  }
+  for (int j = 0; j < NS; ++j) out[j] = red[4 * NW + j];
 }
 
 // y = A_k x on the rows [r0, r0+n) of system k; optional fused dots
@@ -96,9 +110,10 @@ struct BatchArgs {
 
 template <int BS, int LANES, typename T>
 __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
-  __shared__ T red[4 * (BS / 32)];
+  __shared__ T red[4 * (BS / 32) + 8];
   __shared__ uint32_t sys_sh;
   const double tol2 = a.tol * a.tol;
+  constexpr T kGo = T(0), kStop = T(1), kBreak = T(2);  // step verdicts
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) sys_sh = atomicAdd(a.queue, 1u);
@@ -112,7 +127,7 @@ __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
     const T *b = a.b;
     uint32_t it = 0;
     int st = kMaxIters;
-    double err = 0;
+    double err = 0;   // thread 0's
     if (method == 0) {
       // ---- pipelined CG (cg.hpp:128-187) ----
       T d[1] = {0};
@@ -121,24 +136,30 @@ __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
         x[r0 + i] = 0; r[r0 + i] = bi; p[r0 + i] = bi;
         d[0] += bi * bi;
       }
-      cta_sum<BS>(d, red);
-      T nrm = sqrt(d[0]);
-      const T nrhs2 = nrm * nrm;
-      T rr = nrhs2;
-      if (nrhs2 <= T(0)) { st = kConverged; goto done; }
+      T nrhs2 = 0, rr = 0;  // thread 0's
+      T o1[1];
+      cta_step<BS>(d, red, o1, [&](const T (&sm)[1], T (&o)[1]) {
+        const T nrm = sqrt(sm[0]);
+        nrhs2 = nrm * nrm;  // norm_2(residual)^2 as cg.hpp:149
+        rr = nrhs2;
+        o[0] = nrhs2 <= T(0) ? kStop : kGo;
+      });
+      if (o1[0] != kGo) { st = kConverged; goto done; }
       {
-        __syncthreads();
         T e2[2] = {0, 0};
         cta_spmv<BS, LANES>(a.rp, a.ci, a.v, r0, n, p, [&](uint32_t row, T acc) {
           Ap[row] = acc; e2[0] += acc * acc; e2[1] += p[row] * acc;
         });
-        cta_sum<BS>(e2, red);
-        T alpha = rr / e2[1];
-        T nap = sqrt(e2[0]);
-        T beta = (alpha * alpha * nap * nap - rr) / rr;
+        T ab[2];
+        cta_step<BS>(e2, red, ab, [&](const T (&sm)[2], T (&o)[2]) {
+          const T alpha = rr / sm[1];
+          const T nap = sqrt(sm[0]);
+          o[0] = alpha;
+          o[1] = (alpha * alpha * nap * nap - rr) / rr;
+        });
         for (it = 1; it <= a.max_iters; ++it) {
+          const T alpha = ab[0], beta = ab[1];
           T d1[1] = {0};
-          __syncthreads();
           for (uint32_t i = threadIdx.x; i < n; i += BS) {
             uint32_t g = r0 + i;
             T vp = p[g], vr = r[g];
@@ -148,18 +169,27 @@ __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
             d1[0] += vr * vr;
             p[g] = vp; r[g] = vr;
           }
-          cta_sum<BS>(d1, red);  // also orders the p writes before the SpMV reads
-          rr = d1[0];
+          T o0[1];
+          // also orders the p writes before the SpMV reads
+          cta_step<BS>(d1, red, o0, [&](const T (&sm)[1], T (&o)[1]) { rr = sm[0]; o[0] = 0; });
           T e[2] = {0, 0};
           cta_spmv<BS, LANES>(a.rp, a.ci, a.v, r0, n, p, [&](uint32_t row, T acc) {
             Ap[row] = acc; e[0] += acc * acc; e[1] += p[row] * acc;
           });
-          cta_sum<BS>(e, red);
-          err = sqrt(fabs((double)rr) / (double)nrhs2);
-          if (fabs((double)rr / (double)nrhs2) < tol2) { st = kConverged; break; }
-          alpha = rr / e[1];
-          beta = (alpha * alpha * e[0] - rr) / rr;
-          if (!isfinite(alpha) || !isfinite(beta)) { st = kBreakdown; break; }
+          T ov[3];
+          cta_step<BS>(e, red, ov, [&](const T (&sm)[2], T (&o)[3]) {
+            err = sqrt(fabs((double)rr) / (double)nrhs2);
+            if (fabs((double)rr / (double)nrhs2) < tol2) { o[2] = kStop; return; }
+            const T al = rr / sm[1];
+            const T be = (al * al * sm[0] - rr) / rr;
+            o[0] = al;
+            o[1] = be;
+            o[2] = (!isfinite(al) || !isfinite(be)) ? kBreak : kGo;
+          });
+          if (ov[2] == kStop) { st = kConverged; break; }
+          if (ov[2] == kBreak) { st = kBreakdown; break; }
+          ab[0] = ov[0];
+          ab[1] = ov[1];
         }
         if (it > a.max_iters) it = a.max_iters;
       }
@@ -173,19 +203,25 @@ __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
         x[g] = 0; r[g] = bi; p[g] = bi; rs[g] = bi;
         d[0] += bi * bi;
       }
-      cta_sum<BS>(d, red);
-      const T nrhs = sqrt(d[0]);
-      T r_r0 = nrhs * nrhs;
-      if (nrhs <= T(0)) { st = kConverged; goto done; }
+      T nrhs = 0, r_r0 = 0, Ap_r0 = 0, s_s = 0;  // thread 0's
+      T o1[1];
+      cta_step<BS>(d, red, o1, [&](const T (&sm)[1], T (&o)[1]) {
+        nrhs = sqrt(sm[0]);
+        r_r0 = nrhs * nrhs;
+        o[0] = nrhs <= T(0) ? kStop : kGo;
+      });
+      if (o1[0] != kGo) { st = kConverged; goto done; }
       for (it = 1; it <= a.max_iters; ++it) {
-        __syncthreads();
         T e1[1] = {0};
         cta_spmv<BS, LANES>(a.rp, a.ci, a.v, r0, n, p, [&](uint32_t row, T acc) {
           Ap[row] = acc; e1[0] += acc * rs[row];
         });
-        cta_sum<BS>(e1, red);
-        const T Ap_r0 = e1[0];
-        const T alpha = r_r0 / Ap_r0;
+        T oa[1];
+        cta_step<BS>(e1, red, oa, [&](const T (&sm)[1], T (&o)[1]) {
+          Ap_r0 = sm[0];
+          o[0] = r_r0 / Ap_r0;
+        });
+        const T alpha = oa[0];
         T e2[1] = {0};
         for (uint32_t i = threadIdx.x; i < n; i += BS) {
           uint32_t g = r0 + i;
@@ -193,19 +229,27 @@ __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
           s[g] = vs;
           e2[0] += vs * vs;
         }
-        cta_sum<BS>(e2, red);
-        const T s_s = e2[0];
+        T os[1];
+        cta_step<BS>(e2, red, os, [&](const T (&sm)[1], T (&o)[1]) { s_s = sm[0]; o[0] = 0; });
         T e3[3] = {0, 0, 0};
         cta_spmv<BS, LANES>(a.rp, a.ci, a.v, r0, n, s, [&](uint32_t row, T acc) {
           As[row] = acc; e3[0] += acc * acc; e3[1] += s[row] * acc; e3[2] += acc * rs[row];
         });
-        cta_sum<BS>(e3, red);
-        const T beta = -e3[2] / Ap_r0;
-        const T omega = e3[1] / e3[0];
-        const T rn = sqrt(s_s - T(2) * omega * e3[1] + omega * omega * e3[0]);
-        err = (double)rn / (double)nrhs;
-        if (err < a.tol) { st = kConverged; break; }
-        if (!isfinite(alpha) || !isfinite(omega) || !isfinite(beta)) { st = kBreakdown; break; }
+        T ow[3];
+        cta_step<BS>(e3, red, ow, [&](const T (&sm)[3], T (&o)[3]) {
+          const T be = -sm[2] / Ap_r0;
+          const T om = sm[1] / sm[0];
+          const T rn = sqrt(s_s - T(2) * om * sm[1] + om * om * sm[0]);
+          err = (double)rn / (double)nrhs;
+          o[0] = be;
+          o[1] = om;
+          if (err < a.tol) o[2] = kStop;
+          else if (!isfinite(o[1]) || !isfinite(be) || !isfinite(r_r0 / Ap_r0)) o[2] = kBreak;
+          else o[2] = kGo;
+        });
+        if (ow[2] == kStop) { st = kConverged; break; }
+        if (ow[2] == kBreak) { st = kBreakdown; break; }
+        const T beta = ow[0], omega = ow[1];
         T e4[1] = {0};
         for (uint32_t i = threadIdx.x; i < n; i += BS) {
           uint32_t g = r0 + i;
@@ -217,8 +261,8 @@ __global__ void __launch_bounds__(BS) batched_kernel(BatchArgs<T> a) {
           r[g] = vr;
           p[g] = vp;
         }
-        cta_sum<BS>(e4, red);
-        r_r0 = e4[0];
+        T orr[1];
+        cta_step<BS>(e4, red, orr, [&](const T (&sm)[1], T (&o)[1]) { r_r0 = sm[0]; o[0] = 0; });
       }
       if (it > a.max_iters) it = a.max_iters;
     }
