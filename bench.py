@@ -446,7 +446,22 @@ def secondaries(V, torch, peak, args):
         V.solve(A, bd, V.cg_tag(1e-8, 2000), P)
     tag = V.cg_tag(1e-8, 2000)
     t = time_events(lambda: V.solve(A, bd, tag, P), 10)
-    sec["laplace2d_256_jacobi_pcg"] = {"s": t, "iters": tag.iters()}
+    sec["laplace2d_256_jacobi_pcg"] = {"s": t, "iters": tag.iters(),
+                                       "us_per_iter": 1e6 * t / max(tag.iters(), 1)}
+    # small-system latency: 70^2 Laplacian (4,900 rows), Jacobi-PCG to 1e-10;
+    # the whole solve is launch- and latency-bound, so this is the cost of one
+    # iteration's kernel chain on the device-side loop
+    rp, ci, v = gen.laplace2d(70, 70)
+    b = gen.rhs_uniform(len(rp) - 1, 0)
+    A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A)
+    bd = torch.tensor(b, device="cuda")
+    for _ in range(3):
+        V.solve(A, bd, V.cg_tag(1e-10, 2000), P)
+    tag = V.cg_tag(1e-10, 2000)
+    t = time_events(lambda: V.solve(A, bd, tag, P), 20)
+    sec["laplace2d_70_jacobi_pcg_latency"] = {"s": t, "iters": tag.iters(),
+                                              "us_per_iter": 1e6 * t / max(tag.iters(), 1)}
     return sec
 
 
@@ -827,6 +842,7 @@ def profile_kernels(args):
         b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 3), device="cuda")
         V.solve(A, b, V.bicgstab_tag(1e-30, 4))
         V.solve(A, b, V.gmres_tag(1e-30, 30, 30))
+        V.solve(A, b, V.gmres_tag(1e-30, 30, 30), V.jacobi_precond(A))
         del A
         rp, ci, v, sp, methods, bb = gen.batch_systems(256)
         A = V.compressed_matrix(rp, ci, v)

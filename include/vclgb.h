@@ -52,8 +52,13 @@ typedef enum { VCLGB_FLOAT32 = 0, VCLGB_FLOAT64 = 1 } vclgbPrecision;
 /* ---- backend: ViennaCLBackend (libviennacl/include/viennacl.hpp:104-113) -- */
 typedef struct vclgbBackend_st *vclgbBackend;
 
-/* Creates a backend on the current CUDA device using the given stream
- * (NULL = the legacy default stream, as the reference's launches use). */
+/* Creates a backend on the current CUDA device using the given stream.
+ * NULL: a blocking stream of the backend's own, ordered with the legacy
+ * default stream as the reference's launches are, and destroyed with the
+ * backend.  vclgbBackendSetStream moves the backend (and its scratch
+ * buffers) to the caller's stream; a stream of the backend's own stays alive
+ * until the backend is destroyed.  Matrices, preconditioners and batches
+ * may be destroyed before or after their backend. */
 VCLGB_API vclgbStatus vclgbBackendCreate(vclgbBackend *backend, void *cuda_stream);
 VCLGB_API vclgbStatus vclgbBackendDestroy(vclgbBackend *backend);
 VCLGB_API vclgbStatus vclgbBackendSetStream(vclgbBackend backend, void *cuda_stream);

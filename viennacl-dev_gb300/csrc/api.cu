@@ -100,14 +100,14 @@ VCLGB_API vclgbStatus vclgbBackendDestroy(vclgbBackend *h) {
   if (!h || !*h) return VCLGB_INVALID_ARGUMENT;
   Backend *be = B(*h);
   cudaStreamSynchronize(be->stream);
-  be->red_partials.release();
-  be->red_counter.release();
+  be->release_buffers();
   cudaStreamSynchronize(be->stream);
   if (be->host_flags) cudaFreeHost(be->host_flags);
   for (cudaEvent_t e : be->tev) cudaEventDestroy(e);
   for (cudaEvent_t e : be->poll_ev)
     if (e) cudaEventDestroy(e);
   if (be->own_stream) cudaStreamDestroy(be->stream);
+  if (be->retired_stream) cudaStreamDestroy(be->retired_stream);
   delete be;
   *h = nullptr;
   return VCLGB_SUCCESS;
@@ -119,9 +119,14 @@ VCLGB_API vclgbStatus vclgbBackendSetStream(vclgbBackend h, void *stream) {
   return guarded(be, [&]() {
     require(stream != nullptr, VCLGB_INVALID_ARGUMENT, "stream must not be NULL");
     VCLGB_CUDA(cudaStreamSynchronize(be->stream));
-    if (be->own_stream) VCLGB_CUDA(cudaStreamDestroy(be->stream));
+    if (be->own_stream) {
+      // matrices and preconditioners made on it still free their scratch on it
+      if (be->retired_stream) VCLGB_CUDA(cudaStreamDestroy(be->retired_stream));
+      be->retired_stream = be->stream;
+    }
     be->own_stream = false;
     be->stream = static_cast<cudaStream_t>(stream);
+    be->adopt_stream(be->stream);
   });
 }
 
@@ -381,6 +386,7 @@ VCLGB_API vclgbStatus vclgbMatrixDestroy(vclgbMatrix *m) {
   if (!m || !*m) return VCLGB_INVALID_ARGUMENT;
   Matrix *mm = M(*m);
   cudaDeviceSynchronize();
+  FreesAfterDeviceSync legacy_frees;
   delete mm;
   *m = nullptr;
   return VCLGB_SUCCESS;
@@ -667,6 +673,7 @@ VCLGB_API vclgbStatus vclgbCsrInplaceSolve(vclgbBackend h, vclgbMatrix A, int ta
 VCLGB_API vclgbStatus vclgbPrecondDestroy(vclgbPrecond *p) {
   if (!p || !*p) return VCLGB_INVALID_ARGUMENT;
   cudaDeviceSynchronize();
+  FreesAfterDeviceSync legacy_frees;
   delete vclgb::P(*p);
   *p = nullptr;
   return VCLGB_SUCCESS;
@@ -871,6 +878,7 @@ VCLGB_API vclgbStatus vclgbBatchSolve(vclgbBackend h, vclgbBatch bt, const void 
 VCLGB_API vclgbStatus vclgbBatchDestroy(vclgbBatch *bt) {
   if (!bt || !*bt) return VCLGB_INVALID_ARGUMENT;
   cudaDeviceSynchronize();
+  FreesAfterDeviceSync legacy_frees;
   batch_destroy(reinterpret_cast<Batch *>(*bt));
   *bt = nullptr;
   return VCLGB_SUCCESS;

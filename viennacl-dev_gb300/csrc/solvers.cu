@@ -702,87 +702,182 @@ struct EpiGmV {  // v_k = A src, ||v_k||^2 (used for k = 0)
   }
 };
 
-// classical Gram-Schmidt stage 1: h_j = <v_j, v_k>, j < k, one pass over the
-// rows reading each basis vector once (a tall-skinny GEMV)
-template <typename T, int KB>
-__global__ void __launch_bounds__(256)
-    gmres_multidot_kernel(size_t n, int k, const T *__restrict__ V, size_t ld, Gm<T> *g,
-                          T *partials, unsigned *counter) {
-  if (g->done != kRunning) return;
-  __shared__ T red[KB * 8];
-  __shared__ bool am_last;
-  const T *vk = V + (size_t)k * ld;
-  T acc[KB];
+// ---------------------------------------------------------------------------
+// Classical Gram-Schmidt over the first k columns of a basis Q (leading
+// dimension ld), shared by both GMRES forms: the multi-dot h_j = <Q_j, w>,
+// j < k (one pass over the basis, a tall-skinny GEMV) and the update
+// w -= sum_j h_j Q_j with ||w||^2.  On GB300 these passes are bound by the
+// FP64 pipe (2 FMAs per clock per SM; k FMAs per row against (k+1)*8 bytes),
+// so only the FMAs the algorithm needs are issued: the column loops are
+// unrolled to the exact count (a guard j < k inside a loop unrolled to a
+// larger bound still issued the guarded FMAs -- measured 77 us against 31 us
+// at k = 2 on 4M rows), and each row's column loads are issued before its
+// FMAs.  The multi-dot runs one group of up to kCgsCols columns per
+// blockIdx.y; the update walks the columns in chunks of kCgsCols, subtracting
+// in column order as a single loop would.
+// ---------------------------------------------------------------------------
+constexpr int kCgsCols = 8;
+
+template <typename T, int C>
+__device__ __forceinline__ void cgs_dot_rows(size_t n, const T *__restrict__ Q, size_t ld,
+                                             const T *__restrict__ w, T *red) {
+  T acc[C];
 #pragma unroll
-  for (int j = 0; j < KB; ++j) acc[j] = T(0);
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    T v = vk[i];
+  for (int j = 0; j < C; ++j) acc[j] = T(0);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const T v = w[i];
+    T q[C];
 #pragma unroll
-    for (int j = 0; j < KB; ++j)
-      if (j < k) acc[j] += V[(size_t)j * ld + i] * v;
+    for (int j = 0; j < C; ++j) q[j] = Q[(size_t)j * ld + i];
+#pragma unroll
+    for (int j = 0; j < C; ++j) acc[j] += q[j] * v;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int j = 0; j < KB; ++j) {
-    if (j < k) {
-      T t = warp_sum(acc[j]);
-      if (lane == 0) red[j * 8 + warp] = t;
-    }
+  for (int j = 0; j < C; ++j) {
+    const T t = warp_sum(acc[j]);
+    if (lane == 0) red[j * 8 + warp] = t;
+  }
+}
+
+// Out: skip(), store(j, h_j).  Grid (blocks per group, column groups), 256
+// threads; partials[j * gridDim.x + block] holds each block's share of h_j.
+template <typename T, class Out>
+__global__ void __launch_bounds__(256)
+    cgs_multidot_kernel(size_t n, int k, const T *__restrict__ Q, size_t ld,
+                        const T *__restrict__ w, Out out, T *partials, unsigned *counter) {
+  if (out.skip()) return;
+  __shared__ T red[kCgsCols * 8];
+  __shared__ bool am_last;
+  const int j0 = kCgsCols * (int)blockIdx.y;
+  const int c = min(kCgsCols, k - j0);
+  const T *Qg = Q + (size_t)j0 * ld;
+  switch (c) {
+    case 1: cgs_dot_rows<T, 1>(n, Qg, ld, w, red); break;
+    case 2: cgs_dot_rows<T, 2>(n, Qg, ld, w, red); break;
+    case 3: cgs_dot_rows<T, 3>(n, Qg, ld, w, red); break;
+    case 4: cgs_dot_rows<T, 4>(n, Qg, ld, w, red); break;
+    case 5: cgs_dot_rows<T, 5>(n, Qg, ld, w, red); break;
+    case 6: cgs_dot_rows<T, 6>(n, Qg, ld, w, red); break;
+    case 7: cgs_dot_rows<T, 7>(n, Qg, ld, w, red); break;
+    default: cgs_dot_rows<T, 8>(n, Qg, ld, w, red); break;
   }
   __syncthreads();
-  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+  const unsigned nb = gridDim.x;
+  for (int j = threadIdx.x; j < c; j += blockDim.x) {
     T t = 0;
-    for (int w = 0; w < 8; ++w) t += red[j * 8 + w];
-    partials[(size_t)j * gridDim.x + blockIdx.x] = t;
+    for (int q = 0; q < 8; ++q) t += red[j * 8 + q];
+    partials[(size_t)(j0 + j) * nb + blockIdx.x] = t;
   }
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1;
   __syncthreads();
   if (!am_last) return;
   __threadfence();
-  // last block: one warp per dot, fixed order
+  // last block: one warp per projection, partials read at L2 in a fixed order
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int j = warp; j < k; j += 8) {
     T t = 0;
-    for (unsigned b = lane; b < gridDim.x; b += 32)
-      t += ((volatile T *)partials)[(size_t)j * gridDim.x + b];
+    for (unsigned b = lane; b < nb; b += 32) t += __ldcg(partials + (size_t)j * nb + b);
     t = warp_sum(t);
-    if (lane == 0) {
-      g->h[j] = t;
-      g->R[j + (size_t)k * g->K] = t;
-    }
+    if (lane == 0) out.store(j, t);
   }
   if (threadIdx.x == 0) *counter = 0;
 }
 
-// stage 2 for k basis vectors: v_k -= sum_j h_j v_j; ||v_k||^2
-template <typename T, int KB>
-__global__ void __launch_bounds__(256)
-    gmres_orth_kernel(size_t n, int k, T *__restrict__ V, size_t ld, Gm<T> *g, T *partials,
-                      unsigned *counter) {
-  if (g->done != kRunning) return;
-  __shared__ T hs[KB];
-  __shared__ T smem[256];  // block_sum_wide over 256 threads
-  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = g->h[j];
-  __syncthreads();
-  T *vk = V + (size_t)k * ld;
-  T d[1] = {T(0)};
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    T v = vk[i];
+template <typename T, int C>
+__device__ __forceinline__ T cgs_sub_cols(T v, const T *__restrict__ Q, size_t ld, size_t i,
+                                          const T *hs) {
+  T q[C];
 #pragma unroll
-    for (int j = 0; j < KB; ++j)
-      if (j < k) v -= hs[j] * V[(size_t)j * ld + i];
-    d[0] += v * v;
-    vk[i] = v;
+  for (int j = 0; j < C; ++j) q[j] = Q[(size_t)j * ld + i];
+#pragma unroll
+  for (int j = 0; j < C; ++j) v -= hs[j] * q[j];
+  return v;
+}
+
+template <typename T, int TAIL>
+__device__ __forceinline__ T cgs_orth_rows(size_t n, int full, const T *__restrict__ Q, size_t ld,
+                                           T *__restrict__ w, const T *hs) {
+  T d = T(0);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    T v = w[i];
+    for (int c = 0; c < full; ++c)
+      v = cgs_sub_cols<T, kCgsCols>(v, Q + (size_t)c * kCgsCols * ld, ld, i, hs + c * kCgsCols);
+    if constexpr (TAIL > 0)
+      v = cgs_sub_cols<T, TAIL>(v, Q + (size_t)full * kCgsCols * ld, ld, i, hs + full * kCgsCols);
+    d += v * v;
+    w[i] = v;
+  }
+  return d;
+}
+
+// Fin: skip(), h(j) (the projections), finalize(||w||^2)
+template <typename T, class Fin>
+__global__ void __launch_bounds__(256)
+    cgs_orth_kernel(size_t n, int k, const T *__restrict__ Q, size_t ld, T *__restrict__ w, Fin fin,
+                    T *partials, unsigned *counter) {
+  if (fin.skip()) return;
+  __shared__ T hs[kGmresMaxK];
+  __shared__ T smem[256];  // block_sum_wide over 256 threads
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = fin.h(j);
+  __syncthreads();
+  const int full = k / kCgsCols;
+  T d[1];
+  switch (k % kCgsCols) {
+    case 0: d[0] = cgs_orth_rows<T, 0>(n, full, Q, ld, w, hs); break;
+    case 1: d[0] = cgs_orth_rows<T, 1>(n, full, Q, ld, w, hs); break;
+    case 2: d[0] = cgs_orth_rows<T, 2>(n, full, Q, ld, w, hs); break;
+    case 3: d[0] = cgs_orth_rows<T, 3>(n, full, Q, ld, w, hs); break;
+    case 4: d[0] = cgs_orth_rows<T, 4>(n, full, Q, ld, w, hs); break;
+    case 5: d[0] = cgs_orth_rows<T, 5>(n, full, Q, ld, w, hs); break;
+    case 6: d[0] = cgs_orth_rows<T, 6>(n, full, Q, ld, w, hs); break;
+    default: d[0] = cgs_orth_rows<T, 7>(n, full, Q, ld, w, hs); break;
   }
   T s[1];
-  if (grid_reduce<1, true>(d, partials, counter, smem, s)) {
-    g->vnorm2 = s[0];
-    g->inv_vnorm = T(1) / sqrt(s[0]);
-  }
+  if (grid_reduce<1, true>(d, partials, counter, smem, s)) fin.finalize(s[0]);
 }
+
+// One Gram-Schmidt pass (multi-dot, then update) of w against Q's first k
+// columns; both grids are capped at one wave of their kernel.
+template <typename T, class Out, class Fin>
+static void cgs_pass(Backend &be, size_t n, int k, const T *Q, size_t ld, T *w, const Out &out,
+                     const Fin &fin, T *partials, unsigned *counter) {
+  const int groups = (k + kCgsCols - 1) / kCgsCols;
+  const int want = vec_grid(be, n);
+  const int md_wave = one_wave<cgs_multidot_kernel<T, Out>>(be, 1 << 30, 256);
+  const int gx = std::max(1, std::min(want, md_wave / groups));
+  cgs_multidot_kernel<T, Out><<<dim3(gx, groups), 256, 0, be.stream>>>(n, k, Q, ld, w, out,
+                                                                       partials, counter);
+  const int go = one_wave<cgs_orth_kernel<T, Fin>>(be, want, 256);
+  cgs_orth_kernel<T, Fin><<<go, 256, 0, be.stream>>>(n, k, Q, ld, w, fin, partials, counter);
+  be.launches += 2;
+  VCLGB_CHECK_LAUNCH();
+}
+
+// unpreconditioned GMRES: h_j = <v_j, v_k> into h and R(:,k); ||v_k||^2
+template <typename T>
+struct GmDots {
+  Gm<T> *g; int k;
+  __device__ bool skip() const { return g->done != kRunning; }
+  __device__ void store(int j, T t) const {
+    g->h[j] = t;
+    g->R[j + (size_t)k * g->K] = t;
+  }
+};
+template <typename T>
+struct GmOrthEnd {
+  Gm<T> *g;
+  __device__ bool skip() const { return g->done != kRunning; }
+  __device__ T h(int j) const { return g->h[j]; }
+  __device__ void finalize(T s) const {
+    g->vnorm2 = s;
+    g->inv_vnorm = T(1) / sqrt(s);
+  }
+};
 
 template <typename T>
 struct GmNormalize {  // R(k,k) = ||v_k||; v_k /= ||v_k||; xi_k = <r, v_k>
@@ -1009,89 +1104,32 @@ struct GhWNorm {  // generic preconditioner: ||w||^2 after w = M^-1 A q
   __device__ void finalize(const T (&s)[1]) const { gh_w_done(g, s[0]); }
 };
 
-// Gram-Schmidt projections h_j = <q_j, w>, j < k, in one pass over the basis.
-// SECOND: the re-orthogonalisation pass (skipped unless the DGKS test asked
-// for it); its projections are added to R(:,k).
-template <typename T, int KB, bool SECOND>
-__global__ void __launch_bounds__(256)
-    gh_multidot_kernel(size_t n, int k, const T *__restrict__ Q, size_t ld, const T *__restrict__ w,
-                       Gh<T> *g, T *partials, unsigned *counter) {
-  if (SECOND ? g->reorth_skip : g->step_skip) return;
-  __shared__ T red[KB * 8];
-  __shared__ bool am_last;
-  T acc[KB];
-#pragma unroll
-  for (int j = 0; j < KB; ++j) acc[j] = T(0);
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const T v = w[i];
-#pragma unroll
-    for (int j = 0; j < KB; ++j)
-      if (j < k) acc[j] += Q[(size_t)j * ld + i] * v;
+// Gram-Schmidt for the preconditioned form.  SECOND: the re-orthogonalisation
+// pass (skipped unless the DGKS test asked for it); its projections are added
+// to R(:,k).  The first pass's update compares ||w'||^2 with ||w||^2 and
+// requests the second pass when more than half of it cancelled.
+template <typename T, bool SECOND>
+struct GhDots {
+  Gh<T> *g; int k;
+  __device__ bool skip() const { return SECOND ? g->reorth_skip : g->step_skip; }
+  __device__ void store(int j, T t) const {
+    g->h[j] = t;
+    if (SECOND) g->R[(size_t)k * g->K + j] += t;
+    else g->R[(size_t)k * g->K + j] = t;
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < KB; ++j) {
-    if (j < k) {
-      const T t = warp_sum(acc[j]);
-      if (lane == 0) red[j * 8 + warp] = t;
-    }
-  }
-  __syncthreads();
-  for (int j = threadIdx.x; j < k; j += blockDim.x) {
-    T t = 0;
-    for (int q = 0; q < 8; ++q) t += red[j * 8 + q];
-    partials[(size_t)j * gridDim.x + blockIdx.x] = t;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!am_last) return;
-  __threadfence();
-  // last block: one warp per projection, partials read at L2 in a fixed order
-  for (int j = warp; j < k; j += 8) {
-    T t = 0;
-    for (unsigned b = lane; b < gridDim.x; b += 32) t += __ldcg(partials + (size_t)j * gridDim.x + b);
-    t = warp_sum(t);
-    if (lane == 0) {
-      g->h[j] = t;
-      if (SECOND) g->R[(size_t)k * g->K + j] += t;
-      else g->R[(size_t)k * g->K + j] = t;
-    }
-  }
-  if (threadIdx.x == 0) *counter = 0;
-}
-
-// w -= sum_j h_j q_j; ||w||^2.  The first pass compares ||w'||^2 with ||w||^2
-// and requests the second pass when more than half of it cancelled.
-template <typename T, int KB, bool SECOND>
-__global__ void __launch_bounds__(256)
-    gh_orth_kernel(size_t n, int k, const T *__restrict__ Q, size_t ld, T *__restrict__ w,
-                   Gh<T> *g, T *partials, unsigned *counter) {
-  if (SECOND ? g->reorth_skip : g->step_skip) return;
-  __shared__ T hs[KB];
-  __shared__ T smem[256];  // block_sum_wide over 256 threads
-  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = g->h[j];
-  __syncthreads();
-  T d[1] = {T(0)};
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    T v = w[i];
-#pragma unroll
-    for (int j = 0; j < KB; ++j)
-      if (j < k) v -= hs[j] * Q[(size_t)j * ld + i];
-    d[0] += v * v;
-    w[i] = v;
-  }
-  T s[1];
-  if (grid_reduce<1, true>(d, partials, counter, smem, s)) {
-    g->vnorm2 = s[0];
-    g->inv_vnorm = T(1) / sqrt(s[0]);
-    if (!SECOND) g->reorth_skip = !(s[0] < T(0.5) * g->wnorm2);
+};
+template <typename T, bool SECOND>
+struct GhOrthEnd {
+  Gh<T> *g;
+  __device__ bool skip() const { return SECOND ? g->reorth_skip : g->step_skip; }
+  __device__ T h(int j) const { return g->h[j]; }
+  __device__ void finalize(T s) const {
+    g->vnorm2 = s;
+    g->inv_vnorm = T(1) / sqrt(s);
+    if (!SECOND) g->reorth_skip = !(s < T(0.5) * g->wnorm2);
     else g->reorth_skip = 1;
   }
-}
+};
 
 template <typename T>
 struct GhNormalize {  // q_k = w / ||w||, xi_k = <r, q_k>; the step's stopping test
@@ -1423,20 +1461,9 @@ static void gmres_pipelined_solve(Backend &be, Matrix &A, const T *b, T *x, vclg
       T *vk = V + (size_t)k * ld;
       const T *src = k == 0 ? r : V + (size_t)(k - 1) * ld;
       spmv_launch<T>(be, A, src, 0, 1, EpiGmV<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done, hyb);
-      if (k > 0) {
-        int grid = vec_grid(be, n);
-        T *part = static_cast<T *>(red.partials);
-#define VCLGB_GM_CASE(KB)                                                                          \
-  gmres_multidot_kernel<T, KB><<<grid, 256, 0, be.stream>>>(n, (int)k, V, ld, g, part, red.counter); \
-  gmres_orth_kernel<T, KB><<<grid, 256, 0, be.stream>>>(n, (int)k, V, ld, g, part, red.counter)
-        if (k <= 8) { VCLGB_GM_CASE(8); }
-        else if (k <= 16) { VCLGB_GM_CASE(16); }
-        else if (k <= 32) { VCLGB_GM_CASE(32); }
-        else { VCLGB_GM_CASE(64); }
-#undef VCLGB_GM_CASE
-        be.launches += 2;
-        VCLGB_CHECK_LAUNCH();
-      }
+      if (k > 0)
+        cgs_pass<T>(be, n, (int)k, V, ld, vk, GmDots<T>{g, (int)k}, GmOrthEnd<T>{g},
+                    static_cast<T *>(red.partials), red.counter);
       vec_pass<T>(be, n, GmNormalize<T>{vk, r, g, (int)k}, red);
     }
     scalar_step(be, GmCycleEnd<T>{g});
@@ -1500,7 +1527,6 @@ static void gmres_precond_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbS
   const int *done = &g->done, *sskip = &g->step_skip;
   vec_pass<T>(be, n, GhInit<T>{b, x, g}, red);
   T *part = static_cast<T *>(red.partials);
-  const int grid = vec_grid(be, n);
   auto cycle = [&]() {
     // r = M^-1 (b - A x), rho_0, the restart test, r /= rho_0
     if (jac) {
@@ -1525,22 +1551,10 @@ static void gmres_precond_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbS
         vec_pass<T>(be, n, GhWNorm<T>{w, g}, red);
       }
       if (k > 0) {
-#define VCLGB_GH_CASE(KB)                                                                      \
-  gh_multidot_kernel<T, KB, false><<<grid, 256, 0, be.stream>>>(n, (int)k, Q, ld, w, g, part,  \
-                                                                red.counter);                  \
-  gh_orth_kernel<T, KB, false><<<grid, 256, 0, be.stream>>>(n, (int)k, Q, ld, w, g, part,      \
-                                                            red.counter);                      \
-  gh_multidot_kernel<T, KB, true><<<grid, 256, 0, be.stream>>>(n, (int)k, Q, ld, w, g, part,   \
-                                                               red.counter);                   \
-  gh_orth_kernel<T, KB, true><<<grid, 256, 0, be.stream>>>(n, (int)k, Q, ld, w, g, part,       \
-                                                           red.counter)
-        if (k <= 8) { VCLGB_GH_CASE(8); }
-        else if (k <= 16) { VCLGB_GH_CASE(16); }
-        else if (k <= 32) { VCLGB_GH_CASE(32); }
-        else { VCLGB_GH_CASE(64); }
-#undef VCLGB_GH_CASE
-        be.launches += 4;
-        VCLGB_CHECK_LAUNCH();
+        cgs_pass<T>(be, n, (int)k, Q, ld, w, GhDots<T, false>{g, (int)k}, GhOrthEnd<T, false>{g},
+                    part, red.counter);
+        cgs_pass<T>(be, n, (int)k, Q, ld, w, GhDots<T, true>{g, (int)k}, GhOrthEnd<T, true>{g},
+                    part, red.counter);
       }
       vec_pass<T>(be, n, GhNormalize<T>{Q + (size_t)k * ld, w, r, g, (int)k}, red);
     }

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <atomic>
+#include <initializer_list>
 #include <stdint.h>
 
 #include <cstdio>
@@ -45,6 +46,16 @@ inline void require(bool ok, vclgbStatus s, const char *msg) {
 // ---------------------------------------------------------------------------
 // device memory owned by the engine (stream-ordered pool allocations)
 // ---------------------------------------------------------------------------
+// Set (by FreesAfterDeviceSync) while a long-lived object is destroyed after
+// cudaDeviceSynchronize: its buffers are then freed on the legacy default
+// stream, which always exists, instead of the stream they were allocated on
+// (which the caller may have destroyed since).
+inline thread_local bool g_frees_after_device_sync = false;
+struct FreesAfterDeviceSync {
+  FreesAfterDeviceSync() { g_frees_after_device_sync = true; }
+  ~FreesAfterDeviceSync() { g_frees_after_device_sync = false; }
+};
+
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
@@ -79,7 +90,7 @@ struct DevBuf {
     owned = false;
   }
   void release() noexcept {
-    if (ptr && owned) cudaFreeAsync(ptr, stream);
+    if (ptr && owned) cudaFreeAsync(ptr, g_frees_after_device_sync ? cudaStreamLegacy : stream);
     ptr = nullptr;
     bytes = 0;
     owned = true;
@@ -97,6 +108,9 @@ struct Backend {
   size_t max_smem_per_block = 48 * 1024;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // a stream of the backend's own that vclgbBackendSetStream replaced: kept
+  // until the backend is destroyed, because buffers allocated on it free on it
+  cudaStream_t retired_stream = nullptr;
   std::string last_error;
   uint64_t launches = 0;
   // pinned host words the solvers poll (convergence / status), two chunks
@@ -106,6 +120,16 @@ struct Backend {
   // persistent reduction scratch for the vector reductions
   DevBuf red_partials;
   DevBuf red_counter;
+  // trip counter of the solvers' device-side loops
+  DevBuf loop_trips;
+  // the buffers above follow the backend to a new stream, and are released
+  // before the backend's own stream is destroyed
+  void adopt_stream(cudaStream_t s) {
+    for (DevBuf *b : {&red_partials, &red_counter, &loop_trips}) b->stream = s;
+  }
+  void release_buffers() {
+    for (DevBuf *b : {&red_partials, &red_counter, &loop_trips}) b->release();
+  }
   // kernel timing (off by default): every SpMV phase and fused vector pass is
   // bracketed by a pair of CUDA events, recorded as event nodes when the
   // launches are captured into a graph; durations (ms) by kind

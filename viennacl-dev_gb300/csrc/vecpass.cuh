@@ -62,15 +62,90 @@ void scalar_step(Backend &be, const F &f) {
 // solver status words (device)
 enum : int { kRunning = 0, kConverged = 1, kMaxIters = 2, kBreakdown = 3 };
 
+// The condition of the solvers' device-side loop: another trip while the
+// solve runs and fewer than `limit` trips were made (the count bounds the
+// loop whatever the status word says).
+static __global__ void loop_condition_kernel(cudaGraphConditionalHandle h, const int *done,
+                                      unsigned *trips, unsigned limit) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const unsigned t = *trips + 1;
+    *trips = t;
+    cudaGraphSetConditional(h, (*done == kRunning && t < limit) ? 1u : 0u);
+  }
+}
+
 // Launches `one_iteration` (which enqueues the kernels of one solver
 // iteration and returns how many it launched) in chunks of check_every
 // iterations, captured once into a CUDA graph and replayed; after every
 // chunk the host reads the device status word.  Kernels of a finished solve
 // return at their first instruction, so overshooting is harmless.
+//
+// Without kernel timing the chunk is the body of a device-side WHILE node
+// (CUDA graph conditional node): the graph is launched once, the GPU repeats
+// the chunk until the status word leaves kRunning (or the trip bound is
+// reached), and the host waits once -- no status copy and no host round trip
+// per chunk.  Launches with programmatic dependent launch (the optional PDL
+// mode) keep the host-polled chunks.
 template <class F>
 void run_iterations(Backend &be, const int *d_done, uint32_t max_chunks_hint, uint32_t check_every,
                     bool use_graph, F &&one_iteration) {
   if (check_every == 0) check_every = 16;
+  if (use_graph && !be.timing && !be.pdl) {
+    const unsigned limit = max_chunks_hint + 4;
+    if (!be.loop_trips.ptr) be.loop_trips.alloc(256, be.stream);
+    unsigned *trips = be.loop_trips.as<unsigned>();
+    cudaGraph_t graph = nullptr;
+    VCLGB_CUDA(cudaGraphCreate(&graph, 0));
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&]() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+    };
+    try {
+      cudaGraphConditionalHandle handle;
+      VCLGB_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node;
+      VCLGB_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      VCLGB_CUDA(cudaStreamBeginCaptureToGraph(be.stream, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+      const uint64_t before = be.launches;
+      try {
+        for (uint32_t i = 0; i < check_every; ++i) one_iteration();
+        loop_condition_kernel<<<1, 32, 0, be.stream>>>(handle, d_done, trips, limit);
+        VCLGB_CHECK_LAUNCH();
+      } catch (...) {
+        cudaGraph_t g2 = nullptr;
+        cudaStreamEndCapture(be.stream, &g2);
+        throw;
+      }
+      const uint64_t per_trip = be.launches - before + 1;
+      be.launches = before;
+      VCLGB_CUDA(cudaStreamEndCapture(be.stream, &body));
+      VCLGB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+      VCLGB_CUDA(cudaMemsetAsync(trips, 0, sizeof(unsigned), be.stream));
+      VCLGB_CUDA(cudaGraphLaunch(exec, be.stream));
+      VCLGB_CUDA(cudaMemcpyAsync(be.host_flags, d_done, sizeof(int), cudaMemcpyDeviceToHost,
+                                 be.stream));
+      VCLGB_CUDA(cudaMemcpyAsync(be.host_flags + 2, trips, sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, be.stream));
+      VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+      be.launches += per_trip * (uint64_t)be.host_flags[2];
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+    if (be.host_flags[0] == kRunning)
+      throw Error(VCLGB_TIMEOUT, "solver did not report completion within its iteration bound");
+    be.tev_used = 0;
+    return;
+  }
   cudaGraphExec_t exec = nullptr;
   uint64_t per_chunk = 0;
   timing_collect(be, false);  // launches before the loop (timing on only)
