@@ -467,10 +467,11 @@ def secondaries(V, torch, peak, args):
 
 def bench_ilu0(V, torch):
     """ILU0 on a 512^2 upwind convection-diffusion matrix: the device
-    factorisation, the level-scheduled apply (runs of levels of up to 1024 rows
+    factorisation, the level-scheduled apply (runs of levels of up to 512 rows
     in one single-block launch), the same for block ILU0 with the reference's
     default 8 blocks, and BiCGStab with each against BiCGStab with Jacobi, to
-    1e-10."""
+    1e-10; ILU0 on the 128^3 Laplacian (levels of up to 12,288 rows, one
+    cluster launch a triangle) with ILU0-CG to 1e-10."""
     rp, ci, v = gen.convdiff2d(512, 512, peclet=10.0, shift=0.01)
     n = len(rp) - 1
     b = gen.rhs_uniform(n, 5)
@@ -503,6 +504,31 @@ def bench_ilu0(V, torch):
         torch.cuda.synchronize()
         out[name] = {"s": time.time() - t0, "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
                      "true_rel_residual": true_rel_residual(rp, ci, v, x.cpu().numpy(), b)}
+    del A, P, PB
+    # 3D: the 128^3 Laplacian's 381 levels a triangle hold up to 12,288 rows;
+    # runs of them go to a thread-block cluster (up to 16 CTAs of 1,024 threads)
+    rp, ci, v = gen.laplace3d(128)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 5)
+    A = V.compressed_matrix(rp, ci, v)
+    bd = torch.tensor(b, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.time()
+    P = V.ilu0_precond(A)
+    torch.cuda.synchronize()
+    r3 = {"rows": n, "nnz": int(rp[-1]), "setup_s": time.time() - t0,
+          "levels_L": int(P.info().num_levels_L)}
+    z = bd.clone()
+    r3["apply_us"] = time_events(lambda: P.apply(z), 10) * 1e6
+    tag = V.cg_tag(1e-10, 5000)
+    V.solve(A, bd, V.cg_tag(1e-10, 5000), P)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    x = V.solve(A, bd, tag, P)
+    torch.cuda.synchronize()
+    r3["cg_ilu0"] = {"s": time.time() - t0, "iters": tag.iters(), "status": V.STATUS_NAMES[tag.status()],
+                     "true_rel_residual": true_rel_residual(rp, ci, v, x.cpu().numpy(), b)}
+    out["laplace3d_128"] = r3
     return out
 
 
@@ -802,12 +828,18 @@ def profile_kernels(args):
     """Small fixed workloads for ncu captures.  laplace: a few SpMVs per format
     on the 128^3 Laplacian (about 300 MB on the device), one short CG solve and
     a short refined solve on 96^3 diffusion; lognormal: a few SpMVs per format on a 1M-row lognormal random
-    matrix (about 21M nnz, 250 MB of CSR arrays)."""
+    matrix (about 21M nnz, 250 MB of CSR arrays).
+
+    The backend's kernel timing is on for these workloads: the solvers then
+    run their iterations as host-polled graph chunks, whose kernels ncu
+    profiles; it does not profile the kernels of a graph's device-side WHILE
+    body, the solvers' loop otherwise."""
     import torch
     import vclgb as V
+    V.backend().set_kernel_timing(True)
     if args.profile_case == "preconditioners":
         # three applies each of ILU0, block ILU0 (8 blocks) and Chow-Patel ILU on
-        # the 512^2 convection-diffusion matrix, of Chow-Patel IC0 on 128^3
+        # the 512^2 convection-diffusion matrix, of Chow-Patel IC0 and ILU0 on 128^3
         rp, ci, v = gen.convdiff2d(512, 512, peclet=10.0, shift=0.01)
         A = V.compressed_matrix(rp, ci, v)
         z = torch.tensor(gen.rhs_uniform(len(rp) - 1, 5), device="cuda")
@@ -819,6 +851,10 @@ def profile_kernels(args):
         A = V.compressed_matrix(rp, ci, v)
         z = torch.tensor(gen.rhs_uniform(len(rp) - 1, 1), device="cuda")
         P = V.chow_patel_icc_precond(A)
+        for _ in range(3):
+            P.apply(z)
+        del P
+        P = V.ilu0_precond(A)  # 3D levels: cluster runs
         for _ in range(3):
             P.apply(z)
         torch.cuda.synchronize()

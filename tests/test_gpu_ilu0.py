@@ -73,17 +73,21 @@ def _random_dominant(n, per_row, seed):
     return M.indptr.astype(np.uint32), M.indices.astype(np.uint32), M.data.astype(np.float64)
 
 
-@pytest.mark.parametrize("case", ["lap3d", "lap3d_40", "diffusion2d", "scrambled2d",
+@pytest.mark.parametrize("case", ["lap3d", "lap3d_40", "lap3d_96", "diffusion2d", "scrambled2d",
                                   "scrambled3d", "random"])
 def test_factors_match_oracle(V, case):
-    # lap3d_40 has levels above and below the single-block run size, so the
-    # apply mixes both kernels; the scrambled and random patterns have rows
+    # lap3d (levels of at most 400 rows) runs one block; lap3d_40 (up to ~1,200
+    # rows a level) a cluster of 128-thread CTAs, or one block and grid-wide
+    # levels where clusters cannot be launched; lap3d_96 (up to ~6,900 rows) a
+    # cluster of 512-thread CTAs; the scrambled and random patterns have rows
     # spread over several levels
     import torch
     if case == "lap3d":
         rp, ci, v = gen.laplace3d(20)
     elif case == "lap3d_40":
         rp, ci, v = gen.laplace3d(40)
+    elif case == "lap3d_96":
+        rp, ci, v = gen.laplace3d(96)
     elif case == "scrambled2d":
         rp, ci, v = _scrambled(*gen.convdiff2d(40, 40, peclet=10.0, shift=0.01), seed=5)
     elif case == "scrambled3d":

@@ -16,10 +16,16 @@
 // semantics): a run of small levels is one block (level_run_kernel), a large
 // level one grid-wide launch (level_substitute_kernel).
 #include <algorithm>
+#include <exception>
 #include <map>
+#include <thread>
+
+#include <cooperative_groups.h>
 
 #include "formats.hpp"
 #include "vecpass.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace vclgb {
 
@@ -304,17 +310,21 @@ __global__ void __launch_bounds__(kFactorRun, 1)
   }
 }
 
-// gather of the level-set values from the factors (U scaled by its diagonal)
+// gather of the level-set values from the factors (U scaled by its diagonal),
+// one thread per level row
 template <typename T>
-__global__ void level_vals_kernel(size_t nnz, const uint32_t *__restrict__ src,
-                                  const uint32_t *__restrict__ row_of_entry,
-                                  const T *__restrict__ lu, const T *__restrict__ udiag,
-                                  T *vals) {
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
-       k += (size_t)gridDim.x * blockDim.x) {
-    T v = lu[src[k]];
-    if (udiag) v = v / udiag[row_of_entry[k]];
-    vals[k] = v;
+__global__ void level_vals_kernel(size_t level_rows, const uint32_t *__restrict__ row_index,
+                                  const uint32_t *__restrict__ row_ptr,
+                                  const uint32_t *__restrict__ src, const T *__restrict__ lu,
+                                  const T *__restrict__ udiag, T *vals) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < level_rows;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const T d = udiag ? udiag[row_index[t]] : T(1);
+    for (uint32_t k = row_ptr[t]; k < row_ptr[t + 1]; ++k) {
+      T v = lu[src[k]];
+      if (udiag) v = v / d;
+      vals[k] = v;
+    }
   }
 }
 
@@ -345,7 +355,10 @@ __global__ void div_kernel(size_t n, T *vec, const T *__restrict__ d, const int 
 
 // level structure of one triangle (host, from the pattern)
 struct LevelPlan {
-  std::vector<uint32_t> level_ptr, row_index, row_ptr, cols, src, row_of_entry;
+  std::vector<uint32_t> level_ptr, row_index, row_ptr, cols, src;
+  // ring codes of the runs of small levels (plan_codes), run_width 0: none
+  std::vector<int32_t> ecode, xcode;
+  uint32_t run_width = 0;
 };
 
 static LevelPlan plan_levels(uint32_t n, const std::vector<uint32_t> &rp,
@@ -379,10 +392,8 @@ static LevelPlan plan_levels(uint32_t n, const std::vector<uint32_t> &rp,
   std::vector<uint64_t> row_off(maxlev + 2, 0), nnz_off(maxlev + 2, 0);
   uint64_t ro = 0, no = 0;
   p.level_ptr.push_back(0);
-  std::vector<int64_t> level_slot(maxlev + 2, -1);
   for (uint32_t e = 1; e <= maxlev; ++e) {
     if (cnt_rows[e] == 0) continue;
-    level_slot[e] = (int64_t)p.level_ptr.size() - 1;
     row_off[e] = ro;
     nnz_off[e] = no;
     ro += cnt_rows[e];
@@ -393,62 +404,52 @@ static LevelPlan plan_levels(uint32_t n, const std::vector<uint32_t> &rp,
   p.row_ptr.assign(ro + 1, 0);
   p.cols.assign(no, 0);
   p.src.assign(no, 0);
-  p.row_of_entry.assign(no, 0);
-  // rows are visited in ascending order, so each level's list stays sorted
+  // rows are visited in ascending order, so each level's list stays sorted,
+  // and a row's entries of one level are appended together: its row pointer
+  // is the level's entry cursor when the row first reaches the level
   std::vector<uint64_t> rcur(row_off), ncur(nnz_off);
   std::fill(seen.begin(), seen.end(), 0);
   for (uint32_t row = 0; row < n; ++row) {
     for (uint32_t k = rp[row]; k < rp[row + 1]; ++k) {
-      uint32_t c = ci[k];
+      const uint32_t c = ci[k];
       if (!((!upper && c < row) || (upper && c > row))) continue;
-      uint32_t e = lev[c];
+      const uint32_t e = lev[c];
       if (seen[e] != row + 1) {
         seen[e] = row + 1;
         p.row_index[rcur[e]] = row;
+        p.row_ptr[rcur[e]] = (uint32_t)ncur[e];
         rcur[e] += 1;
       }
       p.cols[ncur[e]] = c;
       p.src[ncur[e]] = k;
-      p.row_of_entry[ncur[e]] = row;
       ncur[e] += 1;
     }
-    (void)level_slot;
   }
-  // global row_ptr: entries of a level's row are contiguous and in row order
-  {
-    uint64_t pos = 0;
-    for (uint32_t e = 1; e <= maxlev; ++e) {
-      if (cnt_rows[e] == 0) continue;
-      uint64_t r0 = row_off[e], r1 = r0 + cnt_rows[e];
-      uint64_t k = nnz_off[e];
-      for (uint64_t t = r0; t < r1; ++t) {
-        p.row_ptr[t] = (uint32_t)k;
-        uint32_t row = p.row_index[t];
-        while (k < nnz_off[e] + cnt_nnz[e] && p.row_of_entry[k] == row) ++k;
-      }
-      pos = k;
-    }
-    p.row_ptr[ro] = (uint32_t)no;
-    (void)pos;
-  }
+  p.row_ptr[ro] = (uint32_t)no;
   if (row_level_out) *row_level_out = std::move(lev);
   return p;
 }
 
-// Runs of small levels (level_run_kernel): consecutive levels of at most
-// kRunLevel rows each are substituted by one block; the values written in the
-// last kRing levels of a run stay in a shared-memory ring of kRing x kRunLevel
-// slots (level e's row at position p in slot (e mod kRing) * kRunLevel + p).
+// Runs of small levels: consecutive levels of at most run_width rows each are
+// substituted by one launch -- one block (level_run_kernel, levels of at most
+// kRunLevel rows) or one thread-block cluster (level_cluster_kernel, up to
+// kCodeWidth rows) -- with a barrier between levels; the values written in the
+// last kRing levels of a run stay in shared memory.  A read's ring code names
+// level e's position p as (e mod kRing) * kCodeWidth + p; the block keeps its
+// ring as kRing x kRunLevel slots, a cluster spreads it over its CTAs.
 constexpr uint32_t kRunLevel = 1024;
+constexpr uint32_t kCodeWidth = 16384;  // the widest cluster: 16 CTAs x 1024 threads
+constexpr uint32_t kCodeShift = 14;
+static_assert((1u << kCodeShift) == kCodeWidth, "code width");
 constexpr uint32_t kRing = 16;
 constexpr uint32_t kRingSlots = kRing * kRunLevel;
 static_assert((kRingSlots & (kRingSlots - 1)) == 0, "ring slots index by mask");
 
-// first level at or after L with more than kRunLevel rows (L itself if L has)
-static uint32_t run_end(const std::vector<uint32_t> &level_ptr, uint32_t L, bool runs) {
+// first level at or after L with more than `width` rows (L itself if L has)
+static uint32_t run_end(const std::vector<uint32_t> &level_ptr, uint32_t L, uint32_t width) {
   const uint32_t levels = (uint32_t)level_ptr.size() - 1;
-  if (!runs) return L;
-  while (L < levels && level_ptr[L + 1] - level_ptr[L] <= kRunLevel) ++L;
+  if (width == 0) return L;
+  while (L < levels && level_ptr[L + 1] - level_ptr[L] <= width) ++L;
   return L;
 }
 
@@ -468,21 +469,28 @@ static uint32_t widest_level(const std::vector<uint32_t> &level_ptr, uint32_t L,
 static void plan_ring_codes(const std::vector<uint32_t> &level_ptr,
                             const std::vector<uint32_t> &row_index,
                             const std::vector<uint32_t> &row_ptr, const std::vector<uint32_t> &cols,
-                            uint32_t n, std::vector<int32_t> &ecode, std::vector<int32_t> &xcode) {
+                            uint32_t n, uint32_t run_width, std::vector<int32_t> &ecode,
+                            std::vector<int32_t> &xcode) {
   const uint32_t levels = (uint32_t)level_ptr.size() - 1;
   ecode.resize(cols.size());
   xcode.resize(row_index.size());
-  std::vector<uint32_t> wlev(n, 0), wpos(n, 0), wrun(n, 0);  // run 0: none
+  // per row: level, position and run of its last write (run 0: none), in one
+  // record so a lookup touches one cache line
+  struct Written {
+    uint32_t lev, pos, run;
+  };
+  std::vector<Written> w(n, Written{0, 0, 0});
   uint32_t run = 0;
   for (uint32_t L = 0; L < levels;) {
-    uint32_t L1 = run_end(level_ptr, L, true);
+    uint32_t L1 = run_end(level_ptr, L, run_width);
     const bool small = L1 > L;
     if (!small) L1 = L + 1;
     ++run;
     for (uint32_t e = L; e < L1; ++e) {
       auto code = [&](uint32_t r) -> int32_t {
-        if (small && wrun[r] == run && e - wlev[r] < kRing)
-          return ~(int32_t)((wlev[r] % kRing) * kRunLevel + wpos[r]);
+        const Written &x = w[r];
+        if (small && x.run == run && e - x.lev < kRing)
+          return ~(int32_t)((x.lev % kRing) * kCodeWidth + x.pos);
         return (int32_t)r;
       };
       for (uint32_t t = level_ptr[e]; t < level_ptr[e + 1]; ++t) {
@@ -490,14 +498,20 @@ static void plan_ring_codes(const std::vector<uint32_t> &level_ptr,
         for (uint32_t j = row_ptr[t]; j < row_ptr[t + 1]; ++j) ecode[j] = code(cols[j]);
       }
       for (uint32_t t = level_ptr[e]; t < level_ptr[e + 1]; ++t) {
-        const uint32_t r = row_index[t];
-        wlev[r] = e;
-        wpos[r] = t - level_ptr[e];
-        wrun[r] = small ? run : 0;
+        w[row_index[t]] = Written{e, t - level_ptr[e], small ? run : 0};
       }
     }
     L = L1;
   }
+}
+
+// the ring codes of a plan's runs of levels of at most run_width rows (host
+// only, so that it can run beside the device work of another triangle)
+static void plan_codes(LevelPlan &pl, uint32_t n, uint32_t run_width) {
+  pl.run_width = n >= 0x80000000u ? 0 : run_width;  // codes hold a row index in an int32
+  if (pl.run_width)
+    plan_ring_codes(pl.level_ptr, pl.row_index, pl.row_ptr, pl.cols, n, pl.run_width, pl.ecode,
+                    pl.xcode);
 }
 
 // level_run_kernel: a run of consecutive small levels, one block; a level is
@@ -539,10 +553,11 @@ __device__ __forceinline__ RunRow run_fetch_row(uint32_t lev, uint32_t lev1,
                                                 const uint32_t *__restrict__ level_ptr,
                                                 const uint32_t *__restrict__ row_index,
                                                 const int32_t *__restrict__ xcode,
-                                                const uint32_t *__restrict__ row_ptr) {
+                                                const uint32_t *__restrict__ row_ptr,
+                                                uint32_t pos) {
   RunRow r{kNoRow, 0, 0, 0};
   if (lev < lev1) {
-    const uint32_t t = __ldg(level_ptr + lev) + threadIdx.x;
+    const uint32_t t = __ldg(level_ptr + lev) + pos;
     if (t < __ldg(level_ptr + lev + 1)) {
       r.row = __ldg(row_index + t);
       r.jb = __ldg(row_ptr + t);
@@ -553,7 +568,7 @@ __device__ __forceinline__ RunRow run_fetch_row(uint32_t lev, uint32_t lev1,
   return r;
 }
 
-template <typename T>
+template <typename T, bool L2 = false>
 __device__ __forceinline__ RunEntries<T> run_fetch_entries(RunRow r,
                                                            const int32_t *__restrict__ ecode,
                                                            const T *__restrict__ vals,
@@ -566,13 +581,18 @@ __device__ __forceinline__ RunEntries<T> run_fetch_entries(RunRow r,
     e.c[k] = on ? __ldg(ecode + r.jb + k) : 0;
     e.v[k] = on ? __ldg(vals + r.jb + k) : T(0);
   }
-  e.xg = (r.row != kNoRow && r.xc >= 0) ? vec[r.xc] : T(0);
+  e.xg = (r.row != kNoRow && r.xc >= 0) ? (L2 ? __ldcg(vec + r.xc) : vec[r.xc]) : T(0);
   return e;
+}
+
+// ring slot of code g in a block's ring (positions below kRunLevel)
+__device__ __forceinline__ uint32_t block_slot(uint32_t g) {
+  return ((g >> kCodeShift) & (kRing - 1)) * kRunLevel + (g & (kRunLevel - 1));
 }
 
 template <typename T>
 __device__ __forceinline__ T run_read(int32_t code, const T *ring, const T *vec) {
-  return code < 0 ? ring[(uint32_t)~code & (kRingSlots - 1)] : vec[code];
+  return code < 0 ? ring[block_slot((uint32_t)~code)] : vec[code];
 }
 
 // one level of a run: consume the entries of level lev from `ent`, refill it
@@ -590,7 +610,7 @@ __device__ __forceinline__ void run_level(uint32_t lev, uint32_t lev1, RunEntrie
                                           const T *__restrict__ vals, T *vec, T *ring) {
   const RunRow r = ent.r;
   T x = T(0), y[kRunPre];
-  if (r.row != kNoRow) x = r.xc >= 0 ? ent.xg : ring[(uint32_t)~r.xc & (kRingSlots - 1)];
+  if (r.row != kNoRow) x = r.xc >= 0 ? ent.xg : ring[block_slot((uint32_t)~r.xc)];
 #pragma unroll
   for (int k = 0; k < kRunPre; ++k) y[k] = r.jb + k < r.je ? run_read(ent.c[k], ring, vec) : T(0);
   T s = x;
@@ -603,7 +623,7 @@ __device__ __forceinline__ void run_level(uint32_t lev, uint32_t lev1, RunEntrie
     ring[(lev & (kRing - 1)) * kRunLevel + threadIdx.x] = s;
   }
   ent = run_fetch_entries<T>(row, ecode, vals, vec);
-  row = run_fetch_row(lev + 2 * DE, lev1, level_ptr, row_index, xcode, row_ptr);
+  row = run_fetch_row(lev + 2 * DE, lev1, level_ptr, row_index, xcode, row_ptr, threadIdx.x);
   __syncthreads();
   // the global copy is read only kRing levels later (or after the kernel),
   // so it is stored after the barrier, off the level's critical path
@@ -625,10 +645,12 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
   for (int k = 0; k < DE; ++k)
     ents[k] = run_fetch_entries<T>(
-        run_fetch_row(lev0 + k, lev1, level_ptr, row_index, xcode, row_ptr), ecode, vals, vec);
+        run_fetch_row(lev0 + k, lev1, level_ptr, row_index, xcode, row_ptr, threadIdx.x), ecode,
+        vals, vec);
 #pragma unroll
   for (int k = 0; k < DE; ++k)
-    rows[k] = run_fetch_row(lev0 + DE + k, lev1, level_ptr, row_index, xcode, row_ptr);
+    rows[k] = run_fetch_row(lev0 + DE + k, lev1, level_ptr, row_index, xcode, row_ptr,
+                            threadIdx.x);
   for (uint32_t lev = lev0; lev < lev1; lev += DE) {
 #pragma unroll
     for (int k = 0; k < DE; ++k) {
@@ -639,6 +661,183 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// Cluster runs (level_cluster_kernel): the same runs of small levels and the
+// same ring codes as level_run_kernel, spread over a thread-block cluster of
+// CC CTAs of 2^shift threads each (CC * 2^shift at least the run's widest
+// level).  Position p of a level belongs to CTA p >> shift, whose ring holds
+// the values its positions wrote in the last kRing levels (slot
+// (level mod kRing) << shift | p mod 2^shift); a value another CTA wrote is
+// read from that CTA's ring through distributed shared memory, and the
+// cluster barrier replaces __syncthreads.  GB300 executes 2 FP64 FMAs per
+// clock per SM, so a level of 512 rows with two or three entries each keeps
+// one SM's FP64 pipe busy for ~500-800 cycles; eight SMs take an eighth of
+// that.  Global values are read at L2 (ld.global.cg): they may have been
+// written by another CTA, whose stores the cluster barrier's release/acquire
+// orders but whose lines this SM's L1 could hold stale.  The arrive/wait pair
+// is split around the next level's pattern fetch and the global store.  The
+// per-row subtraction order is level_run_kernel's, so the results are equal.
+template <typename T>
+struct ClRing {
+  T *local;             // this CTA's ring, kRing << shift values
+  uint32_t rank, shift;
+};
+
+template <typename T>
+__device__ __forceinline__ T cl_ring_read(uint32_t g, const ClRing<T> &rg) {
+  const uint32_t p = g & (kCodeWidth - 1), e = (g >> kCodeShift) & (kRing - 1);
+  const uint32_t owner = p >> rg.shift, slot = (e << rg.shift) | (p & ((1u << rg.shift) - 1));
+  if (owner == rg.rank) return rg.local[slot];
+  return cg::this_cluster().map_shared_rank(rg.local, owner)[slot];
+}
+
+template <typename T>
+__device__ __forceinline__ T cl_read(int32_t code, const ClRing<T> &rg, const T *vec) {
+  return code < 0 ? cl_ring_read<T>((uint32_t)~code, rg) : __ldcg(vec + code);
+}
+
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+template <typename T, int DE>
+__device__ __forceinline__ void cl_level(uint32_t lev, uint32_t lev1, uint32_t pos,
+                                         RunEntries<T> &ent, RunRow &row,
+                                         const uint32_t *__restrict__ level_ptr,
+                                         const uint32_t *__restrict__ row_index,
+                                         const int32_t *__restrict__ xcode,
+                                         const uint32_t *__restrict__ row_ptr,
+                                         const int32_t *__restrict__ ecode,
+                                         const T *__restrict__ vals, T *vec,
+                                         const ClRing<T> &rg) {
+  const RunRow r = ent.r;
+  T x = T(0), y[kRunPre];
+  if (r.row != kNoRow) x = r.xc >= 0 ? ent.xg : cl_ring_read<T>((uint32_t)~r.xc, rg);
+#pragma unroll
+  for (int k = 0; k < kRunPre; ++k) y[k] = r.jb + k < r.je ? cl_read<T>(ent.c[k], rg, vec) : T(0);
+  T s = x;
+  if (r.row != kNoRow) {
+#pragma unroll
+    for (int k = 0; k < kRunPre; ++k)
+      if (r.jb + k < r.je) s -= y[k] * ent.v[k];
+    for (uint32_t j = r.jb + kRunPre; j < r.je; ++j)
+      s -= cl_read<T>(__ldg(ecode + j), rg, vec) * __ldg(vals + j);
+    rg.local[((lev & (kRing - 1)) << rg.shift) | threadIdx.x] = s;
+  }
+  cluster_arrive_release();
+  ent = run_fetch_entries<T, true>(row, ecode, vals, vec);
+  row = run_fetch_row(lev + 2 * DE, lev1, level_ptr, row_index, xcode, row_ptr, pos);
+  // read kRing levels later at the earliest, after at least one more barrier
+  if (r.row != kNoRow) vec[r.row] = s;
+  cluster_wait_acquire();
+}
+
+template <typename T, int DE, uint32_t NTMAX>
+__global__ void __launch_bounds__(NTMAX)
+    level_cluster_kernel(uint32_t lev0, uint32_t lev1, const uint32_t *__restrict__ level_ptr,
+                         const uint32_t *__restrict__ row_index, const int32_t *__restrict__ xcode,
+                         const uint32_t *__restrict__ row_ptr, const int32_t *__restrict__ ecode,
+                         const T *__restrict__ vals, T *vec, const int *skip, uint32_t shift) {
+  static_assert(DE >= 1 && DE < (int)kRing, "pipeline depth");
+  extern __shared__ __align__(16) unsigned char ring_bytes[];
+  if (skip && *skip) return;  // the same word for every CTA: the cluster leaves together
+  const ClRing<T> rg{reinterpret_cast<T *>(ring_bytes), cg::this_cluster().block_rank(), shift};
+  const uint32_t pos = (rg.rank << shift) | threadIdx.x;
+  RunEntries<T> ents[DE];
+  RunRow rows[DE];
+#pragma unroll
+  for (int k = 0; k < DE; ++k)
+    ents[k] = run_fetch_entries<T, true>(
+        run_fetch_row(lev0 + k, lev1, level_ptr, row_index, xcode, row_ptr, pos), ecode, vals,
+        vec);
+#pragma unroll
+  for (int k = 0; k < DE; ++k)
+    rows[k] = run_fetch_row(lev0 + DE + k, lev1, level_ptr, row_index, xcode, row_ptr, pos);
+  for (uint32_t lev = lev0; lev < lev1; lev += DE) {
+#pragma unroll
+    for (int k = 0; k < DE; ++k) {
+      if (lev + k >= lev1) break;  // uniform over the cluster
+      cl_level<T, DE>(lev + k, lev1, pos, ents[k], rows[k], level_ptr, row_index, xcode, row_ptr,
+                      ecode, vals, vec, rg);
+    }
+  }
+  // every read of another CTA's ring came before the last barrier, so each
+  // CTA may leave now
+}
+
+// Cluster size for runs of small levels: the largest of 16, 8 and 4 CTAs of
+// 1024 threads (128 KB of ring each) that the device can co-schedule
+// (occupancy query, once per precision), 0 if none.
+template <typename T>
+static int cluster_ctas() {
+  static std::atomic<int> cached{-1};
+  int v = cached.load(std::memory_order_relaxed);
+  if (v >= 0) return v;
+  v = 0;
+  auto wide = level_cluster_kernel<T, 1, 1024>;
+  auto deep = level_cluster_kernel<T, 4, 256>;
+  const size_t wide_smem = (size_t)kRing * 1024 * sizeof(T);
+  bool ok = cudaFuncSetAttribute(wide, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(deep, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)wide_smem) == cudaSuccess;
+  for (int cc : {16, 8, 4}) {
+    if (!ok) break;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cc);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = wide_smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cc;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, wide, &cfg) == cudaSuccess && clusters > 0) {
+      v = cc;
+      break;
+    }
+  }
+  (void)cudaGetLastError();
+  cached.store(v, std::memory_order_relaxed);
+  return v;
+}
+
+// One run of small levels [L, L1) on a cluster: position p of a level on CTA
+// p >> shift, 2^shift threads a CTA (at least a warp), as few CTAs as cover
+// the widest level.  CTAs of up to 256 threads fetch the pattern four levels
+// ahead; wider ones one level ahead (registers).
+template <typename T>
+static void cluster_run(Backend &be, const Precond::Tri &tri, uint32_t L, uint32_t L1,
+                        uint32_t widest, int cc, T *vec, const int *skip) {
+  uint32_t shift = 5;
+  while (((uint32_t)cc << shift) < widest) ++shift;
+  const uint32_t ctas = std::max<uint32_t>(1, (widest + (1u << shift) - 1) >> shift);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(1u << shift);
+  cfg.dynamicSmemBytes = ((size_t)kRing << shift) * sizeof(T);
+  cfg.stream = be.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  auto kern = shift <= 8 ? level_cluster_kernel<T, 4, 256> : level_cluster_kernel<T, 1, 1024>;
+  VCLGB_CUDA(cudaLaunchKernelEx(&cfg, kern, L, L1, tri.level_ptr.as<uint32_t>(),
+                                tri.row_index.as<uint32_t>(), tri.xcode.as<int32_t>(),
+                                tri.row_ptr.as<uint32_t>(), tri.ecode.as<int32_t>(),
+                                tri.vals.as<T>(), vec, skip, shift));
+}
+
 template <typename X>
 static void upload(Backend &be, DevBuf &dst, const std::vector<X> &src) {
   dst.alloc(std::max<size_t>(src.size(), 1) * sizeof(X), be.stream);
@@ -647,22 +846,28 @@ static void upload(Backend &be, DevBuf &dst, const std::vector<X> &src) {
                                cudaMemcpyHostToDevice, be.stream));
 }
 
-// Device copy of one triangle's level structure (pattern only): level
-// pointers, level rows, per-level row pointers and columns, and for the runs
-// of small levels the ring codes of level_run_kernel.
+// The widest level a run may hold: a cluster's width where clusters can be
+// launched, else a block's.
 template <typename T>
-static void tri_structure(Backend &be, const LevelPlan &pl, uint32_t n, Precond::Tri &tri) {
+static uint32_t run_width_for() {
+  const int cc = cluster_ctas<T>();
+  return cc > 0 ? (uint32_t)cc * 1024 : kRunLevel;
+}
+
+// Device copy of one triangle's level structure (pattern only): level
+// pointers, level rows, per-level row pointers and columns, and the ring
+// codes of its runs (plan_codes).
+template <typename T>
+static void tri_structure(Backend &be, const LevelPlan &pl, Precond::Tri &tri) {
   tri.levels = (uint32_t)(pl.level_ptr.size() - 1);
   tri.rows = pl.row_index.size();
   tri.nnz = pl.cols.size();
   tri.h_level_ptr = pl.level_ptr;
-  tri.runs = n < 0x80000000u;  // codes hold a row index in an int32
-  if (tri.runs) {
-    std::vector<int32_t> ecode, xcode;
-    plan_ring_codes(pl.level_ptr, pl.row_index, pl.row_ptr, pl.cols, n, ecode, xcode);
-    upload(be, tri.ecode, ecode);
-    upload(be, tri.xcode, xcode);
-    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // host codes freed after use
+  tri.run_width = pl.run_width;
+  tri.clusters = cluster_ctas<T>();
+  if (tri.run_width) {
+    upload(be, tri.ecode, pl.ecode);
+    upload(be, tri.xcode, pl.xcode);
     VCLGB_CUDA(cudaFuncSetAttribute(level_run_kernel<T, kRunLevel, 1>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(kRingSlots * sizeof(T))));
@@ -684,9 +889,27 @@ static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
   if (A.nnz)
     VCLGB_CUDA(cudaMemcpyAsync(ci.data(), A.col_idx, ci.size() * 4, cudaMemcpyDeviceToHost, be.stream));
   VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+  // U's levels and codes are planned on a second host thread while this one
+  // plans L, launches the factorisation and uploads L's structure
+  const uint32_t rw = run_width_for<T>();
+  LevelPlan U;
+  std::exception_ptr u_error;
+  std::thread u_planner([&]() {
+    try {
+      U = plan_levels(n, rp, ci, true, nullptr);
+      plan_codes(U, n, rw);
+    } catch (...) {
+      u_error = std::current_exception();
+    }
+  });
+  struct Join {
+    std::thread &t;
+    ~Join() {
+      if (t.joinable()) t.join();
+    }
+  } join_u{u_planner};
   std::vector<uint32_t> levL;
   LevelPlan L = plan_levels(n, rp, ci, false, &levL);
-  LevelPlan U = plan_levels(n, rp, ci, true, nullptr);
 
   // factorisation order: rows grouped by their L level (ascending rows in a level)
   uint32_t maxlev = 0;
@@ -738,23 +961,24 @@ static void ilu0_build(Backend &be, const Matrix &A, Precond &P) {
     extract_diag(be, tmp, P.diag, false);
   }
   auto fill_tri = [&](LevelPlan &pl, Precond::Tri &tri, bool upper) {
-    tri_structure<T>(be, pl, n, tri);
-    DevBuf src, roe;
+    tri_structure<T>(be, pl, tri);
+    DevBuf src;
     upload(be, src, pl.src);
-    upload(be, roe, pl.row_of_entry);
     tri.vals.alloc(std::max<uint64_t>(tri.nnz, 1) * sizeof(T), be.stream);
     if (tri.nnz) {
-      int g = waves_grid(be, 256, 8, tri.nnz);
-      level_vals_kernel<T><<<g, 256, 0, be.stream>>>(tri.nnz, src.as<uint32_t>(),
-                                                     roe.as<uint32_t>(), P.lu.as<T>(),
-                                                     upper ? P.diag.as<T>() : nullptr,
-                                                     tri.vals.as<T>());
+      int g = waves_grid(be, 256, 8, tri.rows);
+      level_vals_kernel<T><<<g, 256, 0, be.stream>>>(
+          tri.rows, tri.row_index.as<uint32_t>(), tri.row_ptr.as<uint32_t>(), src.as<uint32_t>(),
+          P.lu.as<T>(), upper ? P.diag.as<T>() : nullptr, tri.vals.as<T>());
       be.launches++;
       VCLGB_CHECK_LAUNCH();
     }
-    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // src/roe freed after use
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // src freed after use
   };
+  plan_codes(L, n, rw);
   fill_tri(L, P.L, false);
+  u_planner.join();
+  if (u_error) std::rethrow_exception(u_error);
   fill_tri(U, P.U, true);
 }
 
@@ -904,14 +1128,20 @@ std::unique_ptr<Precond> block_ilu0_create(Backend &be, const Matrix &A, uint32_
   return P;
 }
 
+// Runs whose levels hold at most kRunLevel / 2 rows take one block (a level
+// costs less there than the cluster barrier, ~0.42 us on GB300); wider runs a
+// cluster where one can be launched, else one block of kRunLevel threads.
 template <typename T>
 static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *skip) {
   for (uint32_t L = 0; L < tri.levels;) {
     const uint32_t r0 = tri.h_level_ptr[L], r1 = tri.h_level_ptr[L + 1];
-    const uint32_t L1 = run_end(tri.h_level_ptr, L, tri.runs);
+    const uint32_t L1 = run_end(tri.h_level_ptr, L, tri.run_width);
     if (L1 > L) {
       const size_t smem = kRingSlots * sizeof(T);
-      if (widest_level(tri.h_level_ptr, L, L1) <= kRunLevel / 2)
+      const uint32_t widest = widest_level(tri.h_level_ptr, L, L1);
+      if (widest > kRunLevel / 2 && tri.clusters > 0)
+        cluster_run<T>(be, tri, L, L1, widest, tri.clusters, vec, skip);
+      else if (widest <= kRunLevel / 2)
         level_run_kernel<T, kRunLevel / 2, 4><<<1, kRunLevel / 2, smem, be.stream>>>(
             L, L1, tri.level_ptr.as<uint32_t>(), tri.row_index.as<uint32_t>(),
             tri.xcode.as<int32_t>(), tri.row_ptr.as<uint32_t>(), tri.ecode.as<int32_t>(),
@@ -953,7 +1183,7 @@ static void tri_apply(Backend &be, const Precond::Tri &tri, T *vec, const int *s
 // ---------------------------------------------------------------------------
 struct TriSolvePlan {
   Precond::Tri tri;
-  DevBuf src, roe;  // entry of A behind each level entry, and the entry's row
+  DevBuf src;  // entry of A behind each level entry
   DevBuf diag;
 };
 
@@ -987,11 +1217,11 @@ static void csr_inplace_solve_t(Backend &be, Matrix &A, int tag, bool trans, T *
       VCLGB_CUDA(cudaStreamSynchronize(be.stream));
     }
     LevelPlan pl = plan_levels(n, rp, ci, upper, nullptr);
+    plan_codes(pl, n, run_width_for<T>());
     if (trans)
       for (auto &k : pl.src) k = map[k];
-    tri_structure<T>(be, pl, n, plan->tri);
+    tri_structure<T>(be, pl, plan->tri);
     upload(be, plan->src, pl.src);
-    upload(be, plan->roe, pl.row_of_entry);
     plan->tri.vals.alloc(std::max<uint64_t>(plan->tri.nnz, 1) * sizeof(T), be.stream);
     VCLGB_CUDA(cudaStreamSynchronize(be.stream));  // host plan freed after the uploads
     slot = std::move(plan);
@@ -999,10 +1229,11 @@ static void csr_inplace_solve_t(Backend &be, Matrix &A, int tag, bool trans, T *
   TriSolvePlan &P = *slot;
   if (!unit) extract_diag(be, A, P.diag, false);
   if (P.tri.nnz) {
-    const int g = waves_grid(be, 256, 8, P.tri.nnz);
+    const int g = waves_grid(be, 256, 8, P.tri.rows);
     level_vals_kernel<T><<<g, 256, 0, be.stream>>>(
-        P.tri.nnz, P.src.as<uint32_t>(), P.roe.as<uint32_t>(), static_cast<const T *>(A.values),
-        unit ? nullptr : P.diag.as<T>(), P.tri.vals.as<T>());
+        P.tri.rows, P.tri.row_index.as<uint32_t>(), P.tri.row_ptr.as<uint32_t>(),
+        P.src.as<uint32_t>(), static_cast<const T *>(A.values), unit ? nullptr : P.diag.as<T>(),
+        P.tri.vals.as<T>());
     be.launches++;
     VCLGB_CHECK_LAUNCH();
   }

@@ -374,7 +374,8 @@ struct Precond {
     DevBuf level_ptr, row_index, row_ptr, cols, vals;
     // where a run of small levels finds each value (precond.cu, level_run_kernel)
     DevBuf ecode, xcode;
-    bool runs = false;
+    uint32_t run_width = 0;  // widest level a run may hold (0: no runs)
+    int clusters = 0;        // CTAs of the cluster that runs wide runs (0: none)
   } L, U;
   // Chow-Patel: I - D_L^-1 L and I - D_U^-1 U (ICC: U = L^T) without their
   // diagonal entries, which the reference stores as zeros; diag = D_L,
