@@ -271,8 +271,11 @@ def test_row_scaling_rejects_unknown_norm(V):
 
 def test_kernel_timing_inside_captured_solves(V):
     # event pairs around each SpMV phase and vector pass, also inside the
-    # solver's CUDA graphs; the solve's result does not change
-    rp, ci, v = gen.laplace2d(64, 64)
+    # solver's CUDA graphs; the solve's result does not change.  The grid is
+    # above the small-system limit: below it a solve runs in one cluster
+    # launch, and kernel timing (which times the per-phase kernels) keeps the
+    # per-phase path
+    rp, ci, v = gen.laplace2d(224, 224)
     b = gen.rhs_uniform(len(rp) - 1, 2)
     A = V.compressed_matrix(rp, ci, v)
     t0 = V.cg_tag(1e-10, 2000)

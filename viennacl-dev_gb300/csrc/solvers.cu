@@ -8,8 +8,12 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "formats.hpp"
 #include "vecpass.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace vclgb {
 
@@ -1291,6 +1295,316 @@ static St<T> make_state(const vclgbSolverTag *tag) {
 
 static bool diag_needed(const Precond *P) { return P && P->kind == 1; }
 
+// ===========================================================================
+// Small systems in one thread-block cluster.  Below a few tens of thousands of
+// rows a solver iteration is a chain of short kernels whose launch gaps and
+// last-block reduction tails cost ~6 us each; here one cluster of up to 16
+// CTAs runs every iteration.  Each CTA owns a contiguous chunk of rows (a row
+// stays with one thread in every phase); a reduction is a block sum into a
+// double-buffered shared slot, one cluster barrier (release/acquire), and a
+// read of every CTA's slot through distributed shared memory in rank order,
+// after which every CTA holds the same sums and runs the same scalar step
+// (the expressions of CgInit/EpiCgFirst/CgUpdate/EpiCg and of the Jacobi PCG
+// functors above, in the same types).  Values another CTA wrote (the search
+// direction the products gather) are read at L2.  Nothing waits but the
+// hardware cluster barrier; the loop ends at the solver's own iteration bound.
+// ===========================================================================
+constexpr uint32_t kClusterSolveThreads = 512;
+constexpr uint32_t kClusterSolveMaxRows = 24000;
+
+// the scalar state of a cluster solve, kept by thread 0 of every CTA (each
+// runs the same steps on the same sums) and read by the block after a barrier
+template <typename T>
+struct ClState {
+  T part[2][2];    // this CTA's partial sums, double buffered by phase
+  T warp[2 * 16];  // block_sum scratch (2 values x 16 warps)
+  T rr, nrhs2, alpha, beta, ip;
+  double error;
+  unsigned iters;
+  int done;
+  int buf;
+};
+
+__device__ __forceinline__ void cl_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// The cluster sum of NV values per thread, then step(sums) on thread 0 of
+// each CTA (it updates the shared state); the block sees the new state on
+// return.  The scalar step runs once per CTA: FP64 divisions and square
+// roots in every thread would cost more than the rows of a small system.
+template <int NV, typename T, class F>
+__device__ __forceinline__ void cl_step(T (&v)[NV], ClState<T> &cs, F &&step) {
+  block_sum<NV>(v, cs.warp);
+  const int b = cs.buf;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) cs.part[b][i] = v[i];
+  }
+  cl_barrier();
+  if (threadIdx.x < 32) {
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned lane = threadIdx.x, nct = cl.num_blocks();
+    T t[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) t[i] = lane < nct ? *cl.map_shared_rank(&cs.part[b][i], lane) : T(0);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t[i] += __shfl_xor_sync(0xffffffffu, t[i], o);
+    }
+    if (lane == 0) {
+      cs.buf = b ^ 1;
+      step(t);
+    }
+  }
+  __syncthreads();
+}
+
+// row i of A times p (p read at L2: other CTAs wrote it)
+template <typename T>
+__device__ __forceinline__ T cl_row(const CsrView<T> &A, uint32_t i, const T *p) {
+  T acc = T(0);
+  const uint32_t e = __ldg(A.rp + i + 1);
+  for (uint32_t k = __ldg(A.rp + i); k < e; ++k) acc += __ldg(A.v + k) * __ldcg(p + __ldg(A.ci + k));
+  return acc;
+}
+
+// JAC false: pipelined CG (no preconditioner); true: PCG with the reciprocal
+// diagonal dg (Jacobi, row scaling)
+template <typename T, bool JAC>
+__global__ void __launch_bounds__(kClusterSolveThreads, 1)
+    cluster_cg_kernel(CsrView<T> A, const T *b, T *x, T *r, T *p, T *q, T *z, const T *dg,
+                      St<T> *st, uint32_t chunk) {
+  __shared__ ClState<T> cs;
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t n = A.rows;
+  const uint32_t r0 = min(cl.block_rank() * chunk, n), r1 = min(r0 + chunk, n);
+  const double tol = st->tol, abs_tol = st->abs_tol;
+  const unsigned max_iters = st->max_iters;
+  if (threadIdx.x == 0) {
+    cs.buf = 0;
+    cs.iters = 0;
+    cs.error = 0;
+    cs.alpha = cs.beta = cs.rr = cs.ip = cs.nrhs2 = T(0);
+  }
+  __syncthreads();
+  if (!JAC) {
+    T d[1] = {T(0)};
+    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+      const T bi = b[i];
+      x[i] = T(0); r[i] = bi; p[i] = bi;
+      d[0] += bi * bi;
+    }
+    cl_step<1>(d, cs, [&](const T (&s)[1]) {  // CgInit
+      const T nrm = sqrt(s[0]);
+      cs.nrhs2 = nrm * nrm;
+      cs.rr = cs.nrhs2;
+      cs.done = (cs.nrhs2 <= T(abs_tol * abs_tol)) ? kConverged : kRunning;
+    });
+    if (cs.done == kRunning) {
+      T e[2] = {T(0), T(0)};
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T acc = cl_row(A, i, p);
+        q[i] = acc;
+        e[0] += acc * acc;
+        e[1] += p[i] * acc;
+      }
+      cl_step<2>(e, cs, [&](const T (&s)[2]) {  // EpiCgFirst
+        const T rr = cs.rr;
+        const T alpha = rr / s[1];
+        const T nap = sqrt(s[0]);
+        cs.alpha = alpha;
+        cs.beta = (alpha * alpha * nap * nap - rr) / rr;
+        if (max_iters == 0) {
+          cs.done = kMaxIters;
+          cs.error = sqrt(fabs((double)rr) / (double)cs.nrhs2);
+        }
+      });
+    }
+    while (cs.done == kRunning) {
+      const T alpha = cs.alpha, beta = cs.beta;
+      T d1[1] = {T(0)};  // CgUpdate
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        T vp = p[i], vr = r[i];
+        x[i] += alpha * vp;
+        vr -= alpha * q[i];
+        vp = vr + beta * vp;
+        d1[0] += vr * vr;
+        p[i] = vp;
+        r[i] = vr;
+      }
+      cl_step<1>(d1, cs, [&](const T (&s)[1]) { cs.rr = s[0]; });
+      T e[2] = {T(0), T(0)};  // EpiCg
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T acc = cl_row(A, i, p);
+        q[i] = acc;
+        e[0] += acc * acc;
+        e[1] += p[i] * acc;
+      }
+      cl_step<2>(e, cs, [&](const T (&s)[2]) {
+        cs.iters += 1;
+        const T rr = cs.rr;
+        const double ratio = fabs((double)rr / (double)cs.nrhs2);
+        if (ratio < tol * tol || fabs((double)rr) < abs_tol * abs_tol) {
+          cs.done = kConverged;
+          cs.error = sqrt(fabs((double)rr) / (double)cs.nrhs2);
+          return;
+        }
+        const T a = rr / s[1];
+        const T bb = (a * a * s[0] - rr) / rr;
+        cs.alpha = a;
+        cs.beta = bb;
+        cs.error = sqrt(fabs((double)rr) / (double)cs.nrhs2);
+        if (!finite_(a) || !finite_(bb)) cs.done = kBreakdown;
+        else if (cs.iters >= max_iters) cs.done = kMaxIters;
+      });
+    }
+  } else {
+    T d[1] = {T(0)};  // PcgInit
+    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+      const T bi = b[i];
+      x[i] = T(0); r[i] = bi;
+      const T zi = bi * dg[i];
+      p[i] = zi;
+      d[0] += bi * zi;
+    }
+    cl_step<1>(d, cs, [&](const T (&s)[1]) {
+      cs.ip = s[0];
+      cs.nrhs2 = s[0];
+      cs.done = (fabs((double)s[0]) <= abs_tol * abs_tol) ? kConverged : kRunning;
+      if (cs.done == kRunning && max_iters == 0) cs.done = kMaxIters;
+    });
+    while (cs.done == kRunning) {
+      T e[1] = {T(0)};  // EpiPcg
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T acc = cl_row(A, i, p);
+        q[i] = acc;
+        e[0] += acc * p[i];
+      }
+      cl_step<1>(e, cs, [&](const T (&s)[1]) {
+        cs.iters += 1;
+        cs.alpha = cs.ip / s[0];
+        if (!finite_(cs.alpha)) cs.done = kBreakdown;
+      });
+      if (cs.done != kRunning) break;
+      const T alpha = cs.alpha;
+      T d1[1] = {T(0)};  // PcgUpdate (Jacobi)
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T vp = p[i];
+        x[i] += alpha * vp;
+        const T vr = r[i] - alpha * q[i];
+        r[i] = vr;
+        const T zi = vr * dg[i];
+        z[i] = zi;
+        d1[0] += vr * zi;
+      }
+      cl_step<1>(d1, cs, [&](const T (&s)[1]) {  // pcg_check
+        const T new_ip = s[0];
+        const double ratio = (double)new_ip / (double)cs.nrhs2;
+        cs.error = sqrt(fabs(ratio));
+        if (fabs(ratio) < tol * tol || fabs((double)new_ip) < abs_tol * abs_tol) {
+          cs.done = kConverged;
+          return;
+        }
+        cs.beta = new_ip / cs.ip;
+        cs.ip = new_ip;
+        if (!finite_(cs.beta)) cs.done = kBreakdown;
+        else if (cs.iters >= max_iters) cs.done = kMaxIters;
+      });
+      if (cs.done != kRunning) break;
+      const T beta = cs.beta;
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x)  // PcgP
+        p[i] = z[i] + beta * p[i];
+      cl_barrier();  // p complete in every CTA before the next product
+    }
+  }
+  if (cl.block_rank() == 0 && threadIdx.x == 0) {
+    st->iters = cs.iters;
+    st->error = cs.error;
+    st->done = cs.done;
+    st->rr = cs.rr;
+  }
+  // no CTA leaves while another may still read its shared slots
+  cl_barrier();
+}
+
+// CTAs of the small-system cluster the device can co-schedule (16, 8 or 4;
+// 0: none), once per precision
+template <typename T>
+static int cluster_solve_ctas() {
+  static std::atomic<int> cached{-1};
+  int v = cached.load(std::memory_order_relaxed);
+  if (v >= 0) return v;
+  v = 0;
+  auto k0 = cluster_cg_kernel<T, false>;
+  auto k1 = cluster_cg_kernel<T, true>;
+  bool ok = cudaFuncSetAttribute(k0, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess;
+  for (int cc : {16, 8, 4}) {
+    if (!ok) break;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cc);
+    cfg.blockDim = dim3(kClusterSolveThreads);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cc;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int c0 = 0, c1 = 0;
+    if (cudaOccupancyMaxActiveClusters(&c0, k0, &cfg) == cudaSuccess && c0 > 0 &&
+        cudaOccupancyMaxActiveClusters(&c1, k1, &cfg) == cudaSuccess && c1 > 0) {
+      v = cc;
+      break;
+    }
+  }
+  (void)cudaGetLastError();
+  cached.store(v, std::memory_order_relaxed);
+  return v;
+}
+
+// Runs the small-system CG if it applies (CSR rows below the limit, no
+// preconditioner or a diagonal one, no kernel timing); false otherwise.
+template <typename T>
+static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st, T *r, T *p,
+                       T *q, T *z, const Precond *P) {
+  const uint32_t n = A.rows;
+  if (n == 0 || n > kClusterSolveMaxRows || A.format != VCLGB_CSR || be.timing) return false;
+  if (P && !diag_needed(P)) return false;
+  const int cc = cluster_solve_ctas<T>();
+  if (cc == 0) return false;
+  const uint32_t chunk = (n + cc - 1) / cc;
+  // threads a CTA: the chunk's rows rounded up to 128, 256 or 512 (a cluster
+  // barrier over fewer warps is quicker; measured best per size)
+  const uint32_t threads = chunk <= 128 ? 128 : chunk <= 256 ? 256 : kClusterSolveThreads;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cc);
+  cfg.blockDim = dim3(threads);
+  cfg.stream = be.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cc;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), n};
+  const T *dg = P ? P->inv_diag.as<T>() : nullptr;
+  if (P)
+    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, true>, view, b, x, r, p, q, z, dg,
+                                  st, chunk));
+  else
+    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, false>, view, b, x, r, p, q, z, dg,
+                                  st, chunk));
+  be.launches++;
+  return true;
+}
+
 template <typename T>
 void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, const Precond *P) {
   const uint32_t n = A.rows;
@@ -1313,6 +1627,10 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
   uint32_t every = auto_check_every(tag, n);
   uint32_t chunks = tag->max_iters / every + 2;
 
+  if (cluster_cg<T>(be, A, b, x, st, r, p, q, z, P)) {
+    set_tag_outputs(be, st, tag);
+    return;
+  }
   if (!P) {
     // pipelined CG
     vec_pass<T>(be, n, CgInit<T>{b, x, r, p, st}, red);
