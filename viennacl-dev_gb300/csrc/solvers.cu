@@ -1311,12 +1311,13 @@ static bool diag_needed(const Precond *P) { return P && P->kind == 1; }
 // ===========================================================================
 constexpr uint32_t kClusterSolveThreads = 512;
 constexpr uint32_t kClusterSolveMaxRows = 24000;
+constexpr size_t kClusterSolveSmem = 192 * 1024;  // dynamic shared memory a CTA, at most
 
 // the scalar state of a cluster solve, kept by thread 0 of every CTA (each
 // runs the same steps on the same sums) and read by the block after a barrier
 template <typename T>
 struct ClState {
-  T part[2][2];    // this CTA's partial sums, double buffered by phase
+  T part[2][16][2];  // every CTA's partial sums (by rank), double buffered by phase
   T warp[2 * 16];  // block_sum scratch (2 values x 16 warps)
   T rr, nrhs2, alpha, beta, ip;
   double error;
@@ -1332,23 +1333,33 @@ __device__ __forceinline__ void cl_barrier() {
 
 // The cluster sum of NV values per thread, then step(sums) on thread 0 of
 // each CTA (it updates the shared state); the block sees the new state on
-// return.  The scalar step runs once per CTA: FP64 divisions and square
-// roots in every thread would cost more than the rows of a small system.
+// return.  Each CTA pushes its block sums into every CTA's slot for its rank
+// (distributed shared memory stores) before the barrier, so after it the
+// sums are read locally, in rank order.  The scalar step runs once per CTA:
+// FP64 divisions and square roots in every thread would cost more than the
+// rows of a small system.
 template <int NV, typename T, class F>
 __device__ __forceinline__ void cl_step(T (&v)[NV], ClState<T> &cs, F &&step) {
   block_sum<NV>(v, cs.warp);
   const int b = cs.buf;
-  if (threadIdx.x == 0) {
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned nct = cl.num_blocks(), me = cl.block_rank();
+  if (threadIdx.x < 32) {
+    T mine[NV];
 #pragma unroll
-    for (int i = 0; i < NV; ++i) cs.part[b][i] = v[i];
+    for (int i = 0; i < NV; ++i) mine[i] = __shfl_sync(0xffffffffu, v[i], 0);
+    if (threadIdx.x < nct) {
+      T *dst = cl.map_shared_rank(&cs.part[b][me][0], threadIdx.x);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) dst[i] = mine[i];
+    }
   }
   cl_barrier();
   if (threadIdx.x < 32) {
-    cg::cluster_group cl = cg::this_cluster();
-    const unsigned lane = threadIdx.x, nct = cl.num_blocks();
+    const unsigned lane = threadIdx.x;
     T t[NV];
 #pragma unroll
-    for (int i = 0; i < NV; ++i) t[i] = lane < nct ? *cl.map_shared_rank(&cs.part[b][i], lane) : T(0);
+    for (int i = 0; i < NV; ++i) t[i] = lane < nct ? cs.part[b][lane][i] : T(0);
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
 #pragma unroll
@@ -1362,12 +1373,23 @@ __device__ __forceinline__ void cl_step(T (&v)[NV], ClState<T> &cs, F &&step) {
   __syncthreads();
 }
 
-// row i of A times p (p read at L2: other CTAs wrote it)
+// The vectors live in shared memory: CTA k holds rows [k << shift, (k+1) <<
+// shift) of x, r, p, q (and z and the reciprocal diagonal for PCG); a
+// product gathers p through distributed shared memory from the CTA that owns
+// the column.  The loop touches no global memory but the matrix, so the
+// cluster barrier's release orders only shared-memory writes.
 template <typename T>
-__device__ __forceinline__ T cl_row(const CsrView<T> &A, uint32_t i, const T *p) {
+__device__ __forceinline__ T cl_row(const CsrView<T> &A, uint32_t i, const T *sp, uint32_t rank,
+                                    uint32_t shift) {
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t mask = (1u << shift) - 1;
   T acc = T(0);
   const uint32_t e = __ldg(A.rp + i + 1);
-  for (uint32_t k = __ldg(A.rp + i); k < e; ++k) acc += __ldg(A.v + k) * __ldcg(p + __ldg(A.ci + k));
+  for (uint32_t k = __ldg(A.rp + i); k < e; ++k) {
+    const uint32_t c = __ldg(A.ci + k), owner = c >> shift;
+    const T pc = owner == rank ? sp[c & mask] : *cl.map_shared_rank(sp + (c & mask), owner);
+    acc += __ldg(A.v + k) * pc;
+  }
   return acc;
 }
 
@@ -1375,12 +1397,15 @@ __device__ __forceinline__ T cl_row(const CsrView<T> &A, uint32_t i, const T *p)
 // diagonal dg (Jacobi, row scaling)
 template <typename T, bool JAC>
 __global__ void __launch_bounds__(kClusterSolveThreads, 1)
-    cluster_cg_kernel(CsrView<T> A, const T *b, T *x, T *r, T *p, T *q, T *z, const T *dg,
-                      St<T> *st, uint32_t chunk) {
+    cluster_cg_kernel(CsrView<T> A, const T *b, T *x, const T *dg, St<T> *st, uint32_t shift) {
   __shared__ ClState<T> cs;
+  extern __shared__ __align__(16) unsigned char cl_vec_bytes[];
   cg::cluster_group cl = cg::this_cluster();
+  const uint32_t rank = cl.block_rank(), len = 1u << shift;
+  T *sx = reinterpret_cast<T *>(cl_vec_bytes), *sr = sx + len, *sp = sr + len, *sq = sp + len;
+  T *sz = sq + len, *sd = sz + len;  // PCG only
   const uint32_t n = A.rows;
-  const uint32_t r0 = min(cl.block_rank() * chunk, n), r1 = min(r0 + chunk, n);
+  const uint32_t r0 = min(rank << shift, n), r1 = min(r0 + len, n), m = r1 - r0;
   const double tol = st->tol, abs_tol = st->abs_tol;
   const unsigned max_iters = st->max_iters;
   if (threadIdx.x == 0) {
@@ -1389,14 +1414,14 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
     cs.error = 0;
     cs.alpha = cs.beta = cs.rr = cs.ip = cs.nrhs2 = T(0);
   }
-  __syncthreads();
   if (!JAC) {
     T d[1] = {T(0)};
-    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-      const T bi = b[i];
-      x[i] = T(0); r[i] = bi; p[i] = bi;
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T bi = b[r0 + i];
+      sx[i] = T(0); sr[i] = bi; sp[i] = bi;
       d[0] += bi * bi;
     }
+    __syncthreads();
     cl_step<1>(d, cs, [&](const T (&s)[1]) {  // CgInit
       const T nrm = sqrt(s[0]);
       cs.nrhs2 = nrm * nrm;
@@ -1405,11 +1430,11 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
     });
     if (cs.done == kRunning) {
       T e[2] = {T(0), T(0)};
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const T acc = cl_row(A, i, p);
-        q[i] = acc;
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T acc = cl_row(A, r0 + i, sp, rank, shift);
+        sq[i] = acc;
         e[0] += acc * acc;
-        e[1] += p[i] * acc;
+        e[1] += sp[i] * acc;
       }
       cl_step<2>(e, cs, [&](const T (&s)[2]) {  // EpiCgFirst
         const T rr = cs.rr;
@@ -1426,22 +1451,22 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
     while (cs.done == kRunning) {
       const T alpha = cs.alpha, beta = cs.beta;
       T d1[1] = {T(0)};  // CgUpdate
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        T vp = p[i], vr = r[i];
-        x[i] += alpha * vp;
-        vr -= alpha * q[i];
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        T vp = sp[i], vr = sr[i];
+        sx[i] += alpha * vp;
+        vr -= alpha * sq[i];
         vp = vr + beta * vp;
         d1[0] += vr * vr;
-        p[i] = vp;
-        r[i] = vr;
+        sp[i] = vp;
+        sr[i] = vr;
       }
       cl_step<1>(d1, cs, [&](const T (&s)[1]) { cs.rr = s[0]; });
       T e[2] = {T(0), T(0)};  // EpiCg
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const T acc = cl_row(A, i, p);
-        q[i] = acc;
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T acc = cl_row(A, r0 + i, sp, rank, shift);
+        sq[i] = acc;
         e[0] += acc * acc;
-        e[1] += p[i] * acc;
+        e[1] += sp[i] * acc;
       }
       cl_step<2>(e, cs, [&](const T (&s)[2]) {
         cs.iters += 1;
@@ -1463,13 +1488,15 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
     }
   } else {
     T d[1] = {T(0)};  // PcgInit
-    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-      const T bi = b[i];
-      x[i] = T(0); r[i] = bi;
-      const T zi = bi * dg[i];
-      p[i] = zi;
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T bi = b[r0 + i], di = dg[r0 + i];
+      sd[i] = di;
+      sx[i] = T(0); sr[i] = bi;
+      const T zi = bi * di;
+      sp[i] = zi;
       d[0] += bi * zi;
     }
+    __syncthreads();
     cl_step<1>(d, cs, [&](const T (&s)[1]) {
       cs.ip = s[0];
       cs.nrhs2 = s[0];
@@ -1478,10 +1505,10 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
     });
     while (cs.done == kRunning) {
       T e[1] = {T(0)};  // EpiPcg
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const T acc = cl_row(A, i, p);
-        q[i] = acc;
-        e[0] += acc * p[i];
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T acc = cl_row(A, r0 + i, sp, rank, shift);
+        sq[i] = acc;
+        e[0] += acc * sp[i];
       }
       cl_step<1>(e, cs, [&](const T (&s)[1]) {
         cs.iters += 1;
@@ -1491,13 +1518,13 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
       if (cs.done != kRunning) break;
       const T alpha = cs.alpha;
       T d1[1] = {T(0)};  // PcgUpdate (Jacobi)
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const T vp = p[i];
-        x[i] += alpha * vp;
-        const T vr = r[i] - alpha * q[i];
-        r[i] = vr;
-        const T zi = vr * dg[i];
-        z[i] = zi;
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T vp = sp[i];
+        sx[i] += alpha * vp;
+        const T vr = sr[i] - alpha * sq[i];
+        sr[i] = vr;
+        const T zi = vr * sd[i];
+        sz[i] = zi;
         d1[0] += vr * zi;
       }
       cl_step<1>(d1, cs, [&](const T (&s)[1]) {  // pcg_check
@@ -1515,18 +1542,19 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
       });
       if (cs.done != kRunning) break;
       const T beta = cs.beta;
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x)  // PcgP
-        p[i] = z[i] + beta * p[i];
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x)  // PcgP
+        sp[i] = sz[i] + beta * sp[i];
       cl_barrier();  // p complete in every CTA before the next product
     }
   }
-  if (cl.block_rank() == 0 && threadIdx.x == 0) {
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) x[r0 + i] = sx[i];
+  if (rank == 0 && threadIdx.x == 0) {
     st->iters = cs.iters;
     st->error = cs.error;
     st->done = cs.done;
     st->rr = cs.rr;
   }
-  // no CTA leaves while another may still read its shared slots
+  // no CTA leaves while another may still read its shared memory
   cl_barrier();
 }
 
@@ -1543,12 +1571,17 @@ static int cluster_solve_ctas() {
   bool ok = cudaFuncSetAttribute(k0, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                 cudaSuccess &&
             cudaFuncSetAttribute(k1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-                cudaSuccess;
+                cudaSuccess &&
+            cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kClusterSolveSmem) == cudaSuccess &&
+            cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kClusterSolveSmem) == cudaSuccess;
   for (int cc : {16, 8, 4}) {
     if (!ok) break;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cc);
     cfg.blockDim = dim3(kClusterSolveThreads);
+    cfg.dynamicSmemBytes = kClusterSolveSmem;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = cc;
@@ -1569,22 +1602,29 @@ static int cluster_solve_ctas() {
 }
 
 // Runs the small-system CG if it applies (CSR rows below the limit, no
-// preconditioner or a diagonal one, no kernel timing); false otherwise.
+// preconditioner or a diagonal one, the vectors fit the CTAs' shared memory,
+// no kernel timing); false otherwise.
 template <typename T>
-static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st, T *r, T *p,
-                       T *q, T *z, const Precond *P) {
+static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st,
+                       const Precond *P) {
   const uint32_t n = A.rows;
   if (n == 0 || n > kClusterSolveMaxRows || A.format != VCLGB_CSR || be.timing) return false;
   if (P && !diag_needed(P)) return false;
   const int cc = cluster_solve_ctas<T>();
   if (cc == 0) return false;
-  const uint32_t chunk = (n + cc - 1) / cc;
-  // threads a CTA: the chunk's rows rounded up to 128, 256 or 512 (a cluster
-  // barrier over fewer warps is quicker; measured best per size)
-  const uint32_t threads = chunk <= 128 ? 128 : chunk <= 256 ? 256 : kClusterSolveThreads;
+  // rows a CTA: a power of two covering n / cc, so a column's owner is a shift
+  uint32_t shift = 5;
+  while (((uint64_t)cc << shift) < n) ++shift;
+  const uint32_t len = 1u << shift;
+  // threads a CTA: 128, 256 or 512 (a cluster barrier over fewer warps is
+  // quicker; measured best per size)
+  const uint32_t threads = len <= 128 ? 128 : len <= 256 ? 256 : kClusterSolveThreads;
+  const size_t smem = (size_t)(P ? 6 : 4) * len * sizeof(T);
+  if (smem > kClusterSolveSmem) return false;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cc);
   cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = be.stream;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1596,11 +1636,9 @@ static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st
   const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), n};
   const T *dg = P ? P->inv_diag.as<T>() : nullptr;
   if (P)
-    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, true>, view, b, x, r, p, q, z, dg,
-                                  st, chunk));
+    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, true>, view, b, x, dg, st, shift));
   else
-    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, false>, view, b, x, r, p, q, z, dg,
-                                  st, chunk));
+    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, false>, view, b, x, dg, st, shift));
   be.launches++;
   return true;
 }
@@ -1627,7 +1665,7 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
   uint32_t every = auto_check_every(tag, n);
   uint32_t chunks = tag->max_iters / every + 2;
 
-  if (cluster_cg<T>(be, A, b, x, st, r, p, q, z, P)) {
+  if (cluster_cg<T>(be, A, b, x, st, P)) {
     set_tag_outputs(be, st, tag);
     return;
   }
