@@ -1,0 +1,87 @@
+"""CG and diagonal-preconditioned CG on small systems run in one thread-block
+cluster launch (up to 24,000 rows); larger systems, and every solve with
+kernel timing on, keep the per-phase kernels.  Checked against the oracle
+(the reference's algorithms on the host): iteration counts within the solver
+tolerance band and the true residual at the requested tolerance, in FP64 and
+FP32, on both sides of the size limit, plus the launch count that tells the
+two paths apart."""
+import numpy as np
+import pytest
+
+import oracle
+import vclgb_gen as gen
+from conftest import iters_close
+
+pytestmark = pytest.mark.gpu
+
+LIMIT = 24000
+
+
+@pytest.fixture(scope="module")
+def V():
+    import torch
+    import vclgb
+    torch.cuda.set_device(0)
+    return vclgb
+
+
+@pytest.mark.parametrize("N", [20, 70, 150, 160])
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_small_cg_matches_oracle(V, N, pc):
+    import torch
+    rp, ci, v = gen.laplace2d(N, N)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 11)
+    A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.cg_tag(1e-10, 3000)
+    l0 = A.be.launches()
+    x = V.solve(A, torch.tensor(b, device="cuda"), tag, P) if P else \
+        V.solve(A, torch.tensor(b, device="cuda"), tag)
+    launches = A.be.launches() - l0
+    xs = x.cpu().numpy()
+    _, it_ref, _ = oracle.solve("cg", rp, ci, v, b, 1e-10, 3000, pc)
+    assert tag.status() == V.SUCCESS
+    assert iters_close(tag.iters(), it_ref), (tag.iters(), it_ref)
+    assert oracle.rel_residual(rp, ci, v, xs, b) < 1e-9
+    if n <= LIMIT:
+        assert launches <= 4, launches  # one cluster launch (plus the state set-up)
+    else:
+        assert launches > tag.iters(), launches
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_small_cg_fp32(V, pc):
+    import torch
+    rp, ci, v = gen.laplace2d(60, 60)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 12)
+    A = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.cg_tag(1e-5, 3000)
+    bd = torch.tensor(b.astype(np.float32), device="cuda")
+    x = V.solve(A, bd, tag, P) if P else V.solve(A, bd, tag)
+    _, it_ref, _ = oracle.solve("cg", rp, ci, v, b, 1e-5, 3000, pc)
+    assert tag.status() == V.SUCCESS
+    assert abs(tag.iters() - it_ref) <= max(3, it_ref // 5), (tag.iters(), it_ref)
+    assert oracle.rel_residual(rp, ci, v, x.cpu().numpy().astype(np.float64), b) < 1e-4
+
+
+def test_cluster_and_per_phase_paths_agree(V):
+    # the same solve through the cluster path and, with kernel timing on,
+    # through the per-phase kernels: equal iteration counts, solutions within
+    # the solver tolerance
+    import torch
+    rp, ci, v = gen.laplace2d(90, 90)
+    b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 13), device="cuda")
+    A = V.compressed_matrix(rp, ci, v)
+    t0 = V.cg_tag(1e-12, 3000)
+    x0 = V.solve(A, b, t0).cpu().numpy()
+    A.be.set_kernel_timing(True)
+    try:
+        t1 = V.cg_tag(1e-12, 3000)
+        x1 = V.solve(A, b, t1).cpu().numpy()
+    finally:
+        A.be.set_kernel_timing(False)
+    assert iters_close(t0.iters(), t1.iters())
+    assert np.linalg.norm(x0 - x1) / np.linalg.norm(x1) < 1e-9
