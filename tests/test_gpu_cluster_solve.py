@@ -85,3 +85,28 @@ def test_cluster_and_per_phase_paths_agree(V):
         A.be.set_kernel_timing(False)
     assert iters_close(t0.iters(), t1.iters())
     assert np.linalg.norm(x0 - x1) / np.linalg.norm(x1) < 1e-9
+
+
+@pytest.mark.parametrize("N", [30, 90, 150, 160])
+def test_small_bicgstab_matches_oracle(V, N):
+    # nonsymmetric upwind convection-diffusion, pipelined BiCGStab without a
+    # preconditioner; the cluster path below the limit, per-phase above
+    import torch
+    rp, ci, v = gen.convdiff2d(N, N, peclet=5.0, shift=0.05)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 14)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.bicgstab_tag(1e-10, 3000)
+    l0 = A.be.launches()
+    x = V.solve(A, torch.tensor(b, device="cuda"), tag)
+    launches = A.be.launches() - l0
+    _, it_ref, _ = oracle.solve("bicgstab", rp, ci, v, b, 1e-10, 3000, "none")
+    assert tag.status() == V.SUCCESS
+    # BiCGStab's recurrences amplify rounding differences: the iteration band
+    # of the other BiCGStab parity tests
+    assert abs(tag.iters() - it_ref) <= max(2, int(0.15 * it_ref)), (tag.iters(), it_ref)
+    assert oracle.rel_residual(rp, ci, v, x.cpu().numpy(), b) < 1e-8
+    if n <= LIMIT:
+        assert launches <= 4, launches
+    else:
+        assert launches > tag.iters(), launches

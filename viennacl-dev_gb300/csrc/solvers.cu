@@ -1317,9 +1317,10 @@ constexpr size_t kClusterSolveSmem = 192 * 1024;  // dynamic shared memory a CTA
 // runs the same steps on the same sums) and read by the block after a barrier
 template <typename T>
 struct ClState {
-  T part[2][16][2];  // every CTA's partial sums (by rank), double buffered by phase
-  T warp[2 * 16];  // block_sum scratch (2 values x 16 warps)
+  T part[2][16][3];  // every CTA's partial sums (by rank), double buffered by phase
+  T warp[4 * 16];    // block_sum scratch (up to 3 values x 16 warps)
   T rr, nrhs2, alpha, beta, ip;
+  T omega, nrhs, Ap_r0, s_s, r_r0;  // BiCGStab
   double error;
   unsigned iters;
   int done;
@@ -1558,6 +1559,108 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
   cl_barrier();
 }
 
+// pipelined BiCGStab without a preconditioner (EpiBicgAp, BicgS, EpiBicgAs,
+// BicgUpdate above) in one cluster; p and s are gathered by the products
+template <typename T>
+__global__ void __launch_bounds__(kClusterSolveThreads, 1)
+    cluster_bicgstab_kernel(CsrView<T> A, const T *b, T *x, St<T> *st, uint32_t shift) {
+  __shared__ ClState<T> cs;
+  extern __shared__ __align__(16) unsigned char cl_vec_bytes[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t rank = cl.block_rank(), len = 1u << shift;
+  T *sx = reinterpret_cast<T *>(cl_vec_bytes), *sr = sx + len, *sp = sr + len, *sr0 = sp + len;
+  T *sAp = sr0 + len, *ss = sAp + len, *sAs = ss + len;
+  const uint32_t n = A.rows;
+  const uint32_t r0 = min(rank << shift, n), r1 = min(r0 + len, n), m = r1 - r0;
+  const double tol = st->tol, abs_tol = st->abs_tol;
+  const unsigned max_iters = st->max_iters;
+  if (threadIdx.x == 0) {
+    cs.buf = 0;
+    cs.iters = 0;
+    cs.error = 0;
+  }
+  T d[1] = {T(0)};  // BicgInit
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+    const T bi = b[r0 + i];
+    sx[i] = T(0); sr[i] = bi; sp[i] = bi; sr0[i] = bi;
+    d[0] += bi * bi;
+  }
+  __syncthreads();
+  cl_step<1>(d, cs, [&](const T (&v)[1]) {
+    const T nrm = sqrt(v[0]);
+    cs.nrhs = nrm;
+    cs.r_r0 = nrm * nrm;
+    cs.done = ((double)nrm <= abs_tol) ? kConverged : kRunning;
+    if (cs.done == kRunning && max_iters == 0) { cs.done = kMaxIters; cs.error = 1.0; }
+  });
+  while (cs.done == kRunning) {
+    T e[1] = {T(0)};  // EpiBicgAp
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T acc = cl_row(A, r0 + i, sp, rank, shift);
+      sAp[i] = acc;
+      e[0] += acc * sr0[i];
+    }
+    cl_step<1>(e, cs, [&](const T (&v)[1]) {
+      cs.iters += 1;
+      cs.Ap_r0 = v[0];
+      cs.alpha = cs.r_r0 / v[0];
+    });
+    const T alpha = cs.alpha;
+    T f[1] = {T(0)};  // BicgS
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T v = sr[i] - alpha * sAp[i];
+      f[0] += v * v;
+      ss[i] = v;
+    }
+    cl_step<1>(f, cs, [&](const T (&v)[1]) { cs.s_s = v[0]; });
+    T g[3] = {T(0), T(0), T(0)};  // EpiBicgAs
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T acc = cl_row(A, r0 + i, ss, rank, shift);
+      sAs[i] = acc;
+      g[0] += acc * acc;
+      g[1] += ss[i] * acc;
+      g[2] += acc * sr0[i];
+    }
+    cl_step<3>(g, cs, [&](const T (&v)[3]) {
+      const T a = cs.r_r0 / cs.Ap_r0;
+      const T bb = -v[2] / cs.Ap_r0;
+      const T w = v[1] / v[0];
+      const T rn = sqrt(cs.s_s - T(2) * w * v[1] + w * w * v[0]);
+      cs.alpha = a;
+      cs.beta = bb;
+      cs.omega = w;
+      cs.error = (double)rn / (double)cs.nrhs;
+      if (fabs((double)rn / (double)cs.nrhs) < tol || (double)rn < abs_tol) cs.done = kConverged;
+      else if (!finite_(a) || !finite_(w) || !finite_(bb)) cs.done = kBreakdown;
+    });
+    if (cs.done != kRunning) break;  // converged before the x update, as bicgstab.hpp:197-198
+    const T a = cs.alpha, w = cs.omega, bb = cs.beta;
+    T h[1] = {T(0)};  // BicgUpdate
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      T vp = sp[i];
+      const T vs = ss[i];
+      sx[i] += a * vp + w * vs;
+      const T vr = vs - w * sAs[i];
+      vp = vr + bb * (vp - w * sAp[i]);
+      h[0] += vr * sr0[i];
+      sr[i] = vr;
+      sp[i] = vp;
+    }
+    cl_step<1>(h, cs, [&](const T (&v)[1]) {
+      cs.r_r0 = v[0];
+      if (cs.iters >= max_iters) cs.done = kMaxIters;
+    });
+  }
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) x[r0 + i] = sx[i];
+  if (rank == 0 && threadIdx.x == 0) {
+    st->iters = cs.iters;
+    st->error = cs.error;
+    st->done = cs.done;
+    st->resnorm = cs.error * cs.nrhs;
+  }
+  cl_barrier();
+}
+
 // CTAs of the small-system cluster the device can co-schedule (16, 8 or 4;
 // 0: none), once per precision
 template <typename T>
@@ -1568,7 +1671,12 @@ static int cluster_solve_ctas() {
   v = 0;
   auto k0 = cluster_cg_kernel<T, false>;
   auto k1 = cluster_cg_kernel<T, true>;
-  bool ok = cudaFuncSetAttribute(k0, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+  auto k2 = cluster_bicgstab_kernel<T>;
+  bool ok = cudaFuncSetAttribute(k2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kClusterSolveSmem) == cudaSuccess &&
+            cudaFuncSetAttribute(k0, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                 cudaSuccess &&
             cudaFuncSetAttribute(k1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                 cudaSuccess &&
@@ -1589,9 +1697,10 @@ static int cluster_solve_ctas() {
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    int c0 = 0, c1 = 0;
+    int c0 = 0, c1 = 0, c2 = 0;
     if (cudaOccupancyMaxActiveClusters(&c0, k0, &cfg) == cudaSuccess && c0 > 0 &&
-        cudaOccupancyMaxActiveClusters(&c1, k1, &cfg) == cudaSuccess && c1 > 0) {
+        cudaOccupancyMaxActiveClusters(&c1, k1, &cfg) == cudaSuccess && c1 > 0 &&
+        cudaOccupancyMaxActiveClusters(&c2, k2, &cfg) == cudaSuccess && c2 > 0) {
       v = cc;
       break;
     }
@@ -1601,26 +1710,30 @@ static int cluster_solve_ctas() {
   return v;
 }
 
-// Runs the small-system CG if it applies (CSR rows below the limit, no
-// preconditioner or a diagonal one, the vectors fit the CTAs' shared memory,
-// no kernel timing); false otherwise.
+// Launch geometry of a small-system cluster solve: rows a CTA (a power of two
+// covering n / cc, so a column's owner is a shift), threads a CTA (128, 256 or
+// 512: a cluster barrier over fewer warps is quicker, measured best per size)
+// and the shared memory of `vectors` slices; false if the solve does not
+// apply (rows above the limit, not CSR, kernel timing on, no cluster, or the
+// slices do not fit).
 template <typename T>
-static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st,
-                       const Precond *P) {
+static bool cluster_geometry(Backend &be, const Matrix &A, int vectors, int &cc, uint32_t &shift,
+                             uint32_t &threads, size_t &smem) {
   const uint32_t n = A.rows;
   if (n == 0 || n > kClusterSolveMaxRows || A.format != VCLGB_CSR || be.timing) return false;
-  if (P && !diag_needed(P)) return false;
-  const int cc = cluster_solve_ctas<T>();
+  cc = cluster_solve_ctas<T>();
   if (cc == 0) return false;
-  // rows a CTA: a power of two covering n / cc, so a column's owner is a shift
-  uint32_t shift = 5;
+  shift = 5;
   while (((uint64_t)cc << shift) < n) ++shift;
   const uint32_t len = 1u << shift;
-  // threads a CTA: 128, 256 or 512 (a cluster barrier over fewer warps is
-  // quicker; measured best per size)
-  const uint32_t threads = len <= 128 ? 128 : len <= 256 ? 256 : kClusterSolveThreads;
-  const size_t smem = (size_t)(P ? 6 : 4) * len * sizeof(T);
-  if (smem > kClusterSolveSmem) return false;
+  threads = len <= 128 ? 128 : len <= 256 ? 256 : kClusterSolveThreads;
+  smem = (size_t)vectors * len * sizeof(T);
+  return smem <= kClusterSolveSmem;
+}
+
+template <typename T, typename... KArgs, typename... Args>
+static void cluster_launch(Backend &be, void (*kern)(KArgs...), int cc, uint32_t threads,
+                           size_t smem, Args &&...args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cc);
   cfg.blockDim = dim3(threads);
@@ -1633,13 +1746,39 @@ static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), n};
+  VCLGB_CUDA(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+  be.launches++;
+}
+
+// Runs the small-system CG (no preconditioner or a diagonal one) if it
+// applies; false otherwise.
+template <typename T>
+static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st,
+                       const Precond *P) {
+  if (P && !diag_needed(P)) return false;
+  int cc;
+  uint32_t shift, threads;
+  size_t smem;
+  if (!cluster_geometry<T>(be, A, P ? 6 : 4, cc, shift, threads, smem)) return false;
+  const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), A.rows};
   const T *dg = P ? P->inv_diag.as<T>() : nullptr;
   if (P)
-    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, true>, view, b, x, dg, st, shift));
+    cluster_launch<T>(be, cluster_cg_kernel<T, true>, cc, threads, smem, view, b, x, dg, st, shift);
   else
-    VCLGB_CUDA(cudaLaunchKernelEx(&cfg, cluster_cg_kernel<T, false>, view, b, x, dg, st, shift));
-  be.launches++;
+    cluster_launch<T>(be, cluster_cg_kernel<T, false>, cc, threads, smem, view, b, x, dg, st,
+                      shift);
+  return true;
+}
+
+// Runs the small-system pipelined BiCGStab (no preconditioner) if it applies.
+template <typename T>
+static bool cluster_bicgstab(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st) {
+  int cc;
+  uint32_t shift, threads;
+  size_t smem;
+  if (!cluster_geometry<T>(be, A, 7, cc, shift, threads, smem)) return false;
+  const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), A.rows};
+  cluster_launch<T>(be, cluster_bicgstab_kernel<T>, cc, threads, smem, view, b, x, st, shift);
   return true;
 }
 
@@ -1728,6 +1867,10 @@ void bicgstab_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *ta
   uint32_t every = auto_check_every(tag, n);
   uint32_t chunks = tag->max_iters / every + 2;
 
+  if (!P && cluster_bicgstab<T>(be, A, b, x, st)) {
+    set_tag_outputs(be, st, tag);
+    return;
+  }
   if (!P) {
     vec_pass<T>(be, n, BicgInit<T>{b, x, r, p, r0, st}, red);
     run_iterations(be, done, chunks, every, true, [&]() {
