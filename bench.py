@@ -890,6 +890,17 @@ def profile_kernels(args):
         b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 4), device="cuda")
         x = V.solve(A, b, V.cg_tag(1e-6, 300), V.jacobi_precond(A))
         V.solve_adjoint(A, x, x - b, V.cg_tag(1e-6, 300), solver="cg")
+        # small systems (70^2 = 4,900 rows) in one cluster launch each: CG,
+        # Jacobi-PCG, BiCGStab (kernel timing off: it keeps the per-phase path)
+        V.backend().set_kernel_timing(False)
+        rp, ci, v = gen.laplace2d(70, 70)
+        A = V.compressed_matrix(rp, ci, v)
+        b = torch.tensor(gen.rhs_uniform(len(rp) - 1, 5), device="cuda")
+        V.solve(A, b, V.cg_tag(1e-10, 2000))
+        V.solve(A, b, V.cg_tag(1e-10, 2000), V.jacobi_precond(A))
+        rp, ci, v = gen.convdiff2d(70, 70, peclet=5.0, shift=0.05)
+        A = V.compressed_matrix(rp, ci, v)
+        V.solve(A, b, V.bicgstab_tag(1e-10, 2000))
         torch.cuda.synchronize()
         print("profile workload done")
         return
