@@ -88,19 +88,23 @@ def test_cluster_and_per_phase_paths_agree(V):
 
 
 @pytest.mark.parametrize("N", [30, 90, 150, 160])
-def test_small_bicgstab_matches_oracle(V, N):
-    # nonsymmetric upwind convection-diffusion, pipelined BiCGStab without a
-    # preconditioner; the cluster path below the limit, per-phase above
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_small_bicgstab_matches_oracle(V, N, pc):
+    # nonsymmetric upwind convection-diffusion; pipelined BiCGStab without a
+    # preconditioner, the restarted preconditioned form with Jacobi; the
+    # cluster path below the limit, per-phase above
     import torch
     rp, ci, v = gen.convdiff2d(N, N, peclet=5.0, shift=0.05)
     n = len(rp) - 1
     b = gen.rhs_uniform(n, 14)
     A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
     tag = V.bicgstab_tag(1e-10, 3000)
     l0 = A.be.launches()
-    x = V.solve(A, torch.tensor(b, device="cuda"), tag)
+    bd = torch.tensor(b, device="cuda")
+    x = V.solve(A, bd, tag, P) if P else V.solve(A, bd, tag)
     launches = A.be.launches() - l0
-    _, it_ref, _ = oracle.solve("bicgstab", rp, ci, v, b, 1e-10, 3000, "none")
+    _, it_ref, _ = oracle.solve("bicgstab", rp, ci, v, b, 1e-10, 3000, pc)
     assert tag.status() == V.SUCCESS
     # BiCGStab's recurrences amplify rounding differences: the iteration band
     # of the other BiCGStab parity tests

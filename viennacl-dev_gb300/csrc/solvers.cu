@@ -1322,8 +1322,9 @@ struct ClState {
   T rr, nrhs2, alpha, beta, ip;
   T omega, nrhs, Ap_r0, s_s, r_r0;  // BiCGStab
   double error;
-  unsigned iters;
+  unsigned iters, last_restart;
   int done;
+  int restart;
   int buf;
 };
 
@@ -1661,6 +1662,127 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
   cl_barrier();
 }
 
+// BiCGStab with a diagonal preconditioner (GbInit, EpiGbRestart<true>,
+// EpiGb1, GbS, EpiGb2, GbUpdate, GbP above, bicgstab.hpp:398-489) in one
+// cluster; products gather x (restarts), p and s
+template <typename T>
+__global__ void __launch_bounds__(kClusterSolveThreads, 1)
+    cluster_gb_kernel(CsrView<T> A, const T *b, T *x, const T *dg, St<T> *st, uint32_t shift) {
+  __shared__ ClState<T> cs;
+  extern __shared__ __align__(16) unsigned char cl_vec_bytes[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t rank = cl.block_rank(), len = 1u << shift;
+  T *sx = reinterpret_cast<T *>(cl_vec_bytes), *sr = sx + len, *sp = sr + len, *sr0 = sp + len;
+  T *st0 = sr0 + len, *ss = st0 + len, *st1 = ss + len, *sd = st1 + len;
+  const uint32_t n = A.rows;
+  const uint32_t r0 = min(rank << shift, n), r1 = min(r0 + len, n), m = r1 - r0;
+  const double tol = st->tol, abs_tol = st->abs_tol;
+  const unsigned max_iters = st->max_iters, max_before_restart = st->max_before_restart;
+  if (threadIdx.x == 0) {
+    cs.buf = 0;
+    cs.iters = 0;
+    cs.last_restart = 0;
+    cs.error = 0;
+  }
+  T d[1] = {T(0)};  // GbInit
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+    const T bi = b[r0 + i];
+    sx[i] = T(0);
+    sd[i] = dg[r0 + i];
+    d[0] += bi * bi;
+  }
+  __syncthreads();
+  cl_step<1>(d, cs, [&](const T (&v)[1]) {
+    const T nrm = sqrt(v[0]);
+    cs.nrhs = nrm;
+    cs.restart = 1;
+    cs.done = ((double)nrm <= abs_tol) ? kConverged : kRunning;
+    if (cs.done == kRunning && max_iters == 0) { cs.done = kMaxIters; cs.error = 1.0; }
+  });
+  while (cs.done == kRunning) {
+    if (cs.restart) {
+      T e[1] = {T(0)};  // EpiGbRestart (Jacobi): r = M^-1 (b - A x); p = r0* = r
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T acc = cl_row(A, r0 + i, sx, rank, shift);
+        const T v = (b[r0 + i] - acc) * sd[i];
+        sp[i] = v;
+        sr0[i] = v;
+        sr[i] = v;
+        e[0] += v * v;
+      }
+      cl_step<1>(e, cs, [&](const T (&v)[1]) {  // gb_restart_done
+        const T nr = sqrt(v[0]);
+        cs.ip = nr * nr;
+        cs.restart = 0;
+        cs.last_restart = cs.iters;
+      });
+    }
+    T e1[1] = {T(0)};  // EpiGb1: t0 = M^-1 A p; <t0, r0*>
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T v = cl_row(A, r0 + i, sp, rank, shift) * sd[i];
+      st0[i] = v;
+      e1[0] += v * sr0[i];
+    }
+    cl_step<1>(e1, cs, [&](const T (&v)[1]) {
+      cs.iters += 1;
+      cs.alpha = cs.ip / v[0];
+    });
+    const T alpha = cs.alpha;
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) ss[i] = sr[i] - alpha * st0[i];  // GbS
+    cl_barrier();  // s complete in every CTA before its product
+    T e2[2] = {T(0), T(0)};  // EpiGb2: t1 = M^-1 A s; ||t1||^2, <t1, s>
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T v = cl_row(A, r0 + i, ss, rank, shift) * sd[i];
+      st1[i] = v;
+      e2[0] += v * v;
+      e2[1] += v * ss[i];
+    }
+    cl_step<2>(e2, cs, [&](const T (&v)[2]) {  // gb_omega
+      const T nt1 = sqrt(v[0]);
+      cs.omega = v[1] / (nt1 * nt1);
+    });
+    const T a = cs.alpha, w = cs.omega;
+    T e3[2] = {T(0), T(0)};  // GbUpdate
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T vs = ss[i];
+      sx[i] += a * sp[i] + w * vs;
+      const T vr = vs - w * st1[i];
+      sr[i] = vr;
+      e3[0] += vr * vr;
+      e3[1] += vr * sr0[i];
+    }
+    cl_step<2>(e3, cs, [&](const T (&v)[2]) {
+      const T rn = sqrt(v[0]);
+      cs.error = (double)rn / (double)cs.nrhs;
+      if ((double)rn / (double)cs.nrhs < tol || (double)rn < abs_tol) {
+        cs.done = kConverged;
+        return;
+      }
+      const T new_ip = v[1];
+      cs.beta = new_ip / cs.ip * cs.alpha / cs.omega;
+      cs.ip = new_ip;
+      const unsigned it = cs.iters - 1;
+      if ((new_ip >= T(0) && new_ip <= T(0)) || (cs.omega >= T(0) && cs.omega <= T(0)) ||
+          it - cs.last_restart > max_before_restart)
+        cs.restart = 1;
+      if (!finite_(cs.alpha) || !finite_(cs.omega)) cs.done = kBreakdown;
+      else if (cs.iters >= max_iters) cs.done = kMaxIters;
+    });
+    if (cs.done != kRunning) break;
+    const T bb = cs.beta, w2 = cs.omega;
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x)  // GbP
+      sp[i] = sr[i] + bb * (sp[i] - w2 * st0[i]);
+    cl_barrier();  // p (and x) complete before the next products
+  }
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) x[r0 + i] = sx[i];
+  if (rank == 0 && threadIdx.x == 0) {
+    st->iters = cs.iters;
+    st->error = cs.error;
+    st->done = cs.done;
+  }
+  cl_barrier();
+}
+
 // CTAs of the small-system cluster the device can co-schedule (16, 8 or 4;
 // 0: none), once per precision
 template <typename T>
@@ -1672,7 +1794,12 @@ static int cluster_solve_ctas() {
   auto k0 = cluster_cg_kernel<T, false>;
   auto k1 = cluster_cg_kernel<T, true>;
   auto k2 = cluster_bicgstab_kernel<T>;
-  bool ok = cudaFuncSetAttribute(k2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+  auto k3 = cluster_gb_kernel<T>;
+  bool ok = cudaFuncSetAttribute(k3, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kClusterSolveSmem) == cudaSuccess &&
+            cudaFuncSetAttribute(k2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                 cudaSuccess &&
             cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kClusterSolveSmem) == cudaSuccess &&
@@ -1697,10 +1824,11 @@ static int cluster_solve_ctas() {
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    int c0 = 0, c1 = 0, c2 = 0;
+    int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
     if (cudaOccupancyMaxActiveClusters(&c0, k0, &cfg) == cudaSuccess && c0 > 0 &&
         cudaOccupancyMaxActiveClusters(&c1, k1, &cfg) == cudaSuccess && c1 > 0 &&
-        cudaOccupancyMaxActiveClusters(&c2, k2, &cfg) == cudaSuccess && c2 > 0) {
+        cudaOccupancyMaxActiveClusters(&c2, k2, &cfg) == cudaSuccess && c2 > 0 &&
+        cudaOccupancyMaxActiveClusters(&c3, k3, &cfg) == cudaSuccess && c3 > 0) {
       v = cc;
       break;
     }
@@ -1770,15 +1898,22 @@ static bool cluster_cg(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st
   return true;
 }
 
-// Runs the small-system pipelined BiCGStab (no preconditioner) if it applies.
+// Runs the small-system BiCGStab (pipelined without a preconditioner, or the
+// preconditioned form with a diagonal one) if it applies; false otherwise.
 template <typename T>
-static bool cluster_bicgstab(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st) {
+static bool cluster_bicgstab(Backend &be, const Matrix &A, const T *b, T *x, St<T> *st,
+                             const Precond *P) {
+  if (P && !diag_needed(P)) return false;
   int cc;
   uint32_t shift, threads;
   size_t smem;
-  if (!cluster_geometry<T>(be, A, 7, cc, shift, threads, smem)) return false;
+  if (!cluster_geometry<T>(be, A, P ? 8 : 7, cc, shift, threads, smem)) return false;
   const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), A.rows};
-  cluster_launch<T>(be, cluster_bicgstab_kernel<T>, cc, threads, smem, view, b, x, st, shift);
+  if (P)
+    cluster_launch<T>(be, cluster_gb_kernel<T>, cc, threads, smem, view, b, x,
+                      P->inv_diag.as<T>(), st, shift);
+  else
+    cluster_launch<T>(be, cluster_bicgstab_kernel<T>, cc, threads, smem, view, b, x, st, shift);
   return true;
 }
 
@@ -1867,7 +2002,7 @@ void bicgstab_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *ta
   uint32_t every = auto_check_every(tag, n);
   uint32_t chunks = tag->max_iters / every + 2;
 
-  if (!P && cluster_bicgstab<T>(be, A, b, x, st)) {
+  if (cluster_bicgstab<T>(be, A, b, x, st, P)) {
     set_tag_outputs(be, st, tag);
     return;
   }
