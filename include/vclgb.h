@@ -441,8 +441,8 @@ typedef struct {
   uint32_t max_iters;
   uint32_t krylov_dim;              /* GMRES restart length */
   uint32_t max_iters_before_restart;/* BiCGStab (generic preconditioned variant) */
-  uint32_t check_every;             /* iterations between host polls of the device
-                                       convergence flag (0 = automatic) */
+  uint32_t check_every;             /* iterations a trip of the device-side loop
+                                       runs before its status test (0 = automatic) */
   /* outputs */
   uint32_t iters;
   uint32_t status;                  /* vclgbStatus of the solve */
@@ -457,13 +457,17 @@ VCLGB_API void vclgbSolverTagInit(vclgbSolverTag *tag, int kind);
  * Chronopoulos-Gear CG (linalg/cg.hpp:128-187), otherwise the preconditioned
  * CG of linalg/cg.hpp:257-322, with the same stopping tests.  The whole
  * iteration (SpMV, reductions, scalar recurrences, convergence test) runs on
- * the device; the host only polls a flag every check_every iterations.
+ * the device, looping in a CUDA graph until the status word says done; the
+ * host waits once.  Systems of up to 24,000 rows (CSR, no preconditioner or a
+ * diagonal one) run in one thread-block-cluster launch.
  * d_b, d_x: contiguous device vectors of length rows; x is overwritten
  * (initial guess 0, as in the reference). */
 VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
                                    vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, bicgstab_tag[, precond]): pipelined (bicgstab.hpp:96-215)
- * without, generic (bicgstab.hpp:398-489) with a preconditioner. */
+ * without, generic (bicgstab.hpp:398-489) with a preconditioner.  Systems of
+ * up to 24,000 rows (CSR, no preconditioner or a diagonal one) run in one
+ * thread-block-cluster launch. */
 VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend be, vclgbMatrix A, const void *d_b,
                                          void *d_x, vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, gmres_tag[, precond]).  precond == NULL runs the

@@ -3,8 +3,8 @@
 //
 // Each solver is a fixed sequence of fused kernels per iteration; scalars
 // live in a device state struct written by the last block of the kernel that
-// completes the reduction, and read by the next kernel.  The host only polls
-// the status word every check_every iterations (see run_iterations).
+// completes the reduction, and read by the next kernel.  The iterations loop
+// on the device (run_iterations); small systems run in one cluster launch.
 #include <algorithm>
 #include <cmath>
 

@@ -113,7 +113,8 @@ struct Backend {
   cudaStream_t retired_stream = nullptr;
   std::string last_error;
   uint64_t launches = 0;
-  // pinned host words the solvers poll (convergence / status), two chunks
+  // pinned host words the solvers read (status, loop trips); in the
+  // host-polled mode (kernel timing, PDL) two chunks
   // in flight; the events mark when each status copy has landed
   int *host_flags = nullptr;
   cudaEvent_t poll_ev[2] = {nullptr, nullptr};
