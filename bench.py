@@ -462,6 +462,15 @@ def secondaries(V, torch, peak, args):
     t = time_events(lambda: V.solve(A, bd, tag, P), 20)
     sec["laplace2d_70_jacobi_pcg_latency"] = {"s": t, "iters": tag.iters(),
                                               "us_per_iter": 1e6 * t / max(tag.iters(), 1)}
+    # the same for a nonsymmetric 70^2 convection-diffusion matrix with BiCGStab
+    rp, ci, v = gen.convdiff2d(70, 70, peclet=5.0, shift=0.05)
+    A = V.compressed_matrix(rp, ci, v)
+    for _ in range(3):
+        V.solve(A, bd, V.bicgstab_tag(1e-10, 2000))
+    tag = V.bicgstab_tag(1e-10, 2000)
+    t = time_events(lambda: V.solve(A, bd, tag), 20)
+    sec["convdiff2d_70_bicgstab_latency"] = {"s": t, "iters": tag.iters(),
+                                             "us_per_iter": 1e6 * t / max(tag.iters(), 1)}
     return sec
 
 
