@@ -114,3 +114,41 @@ def test_small_bicgstab_matches_oracle(V, N, pc):
         assert launches <= 4, launches
     else:
         assert launches > tag.iters(), launches
+
+
+def _random_dominant(n, per_row, seed, symmetric):
+    # random pattern, up to 2 per_row off-diagonals a row spread over all
+    # columns (gathers cross CTAs), dominant diagonal
+    sp = pytest.importorskip("scipy.sparse")
+    rng = np.random.default_rng(seed)
+    r = np.repeat(np.arange(n), per_row)
+    c = rng.integers(0, n, n * per_row)
+    M = sp.coo_matrix((rng.uniform(-1, 1, n * per_row), (r, c)), shape=(n, n)).tocsr()
+    M = M + M.T if symmetric else M + sp.coo_matrix(
+        (rng.uniform(-1, 1, n * per_row), (c, r)), shape=(n, n)).tocsr()
+    M = M + sp.diags(np.asarray(abs(M).sum(axis=1)).ravel() + 0.5)
+    M = M.tocsr()
+    M.sum_duplicates()
+    M.sort_indices()
+    return M.indptr.astype(np.uint32), M.indices.astype(np.uint32), M.data.astype(np.float64)
+
+
+@pytest.mark.parametrize("solver,pc", [("cg", "none"), ("cg", "jacobi"),
+                                       ("bicgstab", "none"), ("bicgstab", "jacobi")])
+def test_small_random_matrices(V, solver, pc):
+    import torch
+    rp, ci, v = _random_dominant(9000, 10, seed=21, symmetric=(solver == "cg"))
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 15)
+    A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.cg_tag(1e-10, 3000) if solver == "cg" else V.bicgstab_tag(1e-10, 3000)
+    bd = torch.tensor(b, device="cuda")
+    l0 = A.be.launches()
+    x = V.solve(A, bd, tag, P) if P else V.solve(A, bd, tag)
+    assert A.be.launches() - l0 <= 4  # the cluster path
+    _, it_ref, _ = oracle.solve(solver, rp, ci, v, b, 1e-10, 3000, pc)
+    assert tag.status() == V.SUCCESS
+    band = 0.02 if solver == "cg" else 0.15
+    assert abs(tag.iters() - it_ref) <= max(2, int(band * it_ref)), (tag.iters(), it_ref)
+    assert oracle.rel_residual(rp, ci, v, x.cpu().numpy(), b) < 1e-8
