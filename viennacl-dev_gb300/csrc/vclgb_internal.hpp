@@ -516,31 +516,36 @@ __device__ __forceinline__ bool grid_reduce(T (&v)[NV], T *partials, unsigned *c
     __threadfence();
     unsigned t = atomicAdd(counter, 1u);
     am_last = (t == gridDim.x - 1);
+    // acquire in the thread that took the last ticket only: the barrier
+    // below orders the block's reads after it (a fence in every thread waited
+    // for each thread's own outstanding vector stores, on the serial tail)
+    if (am_last) __threadfence();
   }
   __syncthreads();
   if (!am_last) return false;
-  __threadfence();
   // The other blocks' partials are read at L2 (ld.global.cg: no stale L1
-  // line), four at a time: loads issued together, then added in the fixed
-  // order b = tid, tid + blockDim, ...  (volatile loads would be issued one
-  // after another, a full L2 round trip each, on the kernel's serial tail).
+  // line), every value's loads of a batch issued together -- one L2 round
+  // trip for grids up to W blocks a thread -- then added in the fixed order
+  // b = tid, tid + blockDim, ...  (volatile loads would be issued one after
+  // another, a full L2 round trip each, on the kernel's serial tail).
+  constexpr int W = NV >= 4 ? 2 : 8 / NV;
   T acc[NV];
 #pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    const T *src = partials + (size_t)i * gridDim.x;
-    T s = 0;
-    for (unsigned b0 = threadIdx.x; b0 < gridDim.x; b0 += 4 * blockDim.x) {
-      T q[4];
+  for (int i = 0; i < NV; ++i) acc[i] = T(0);
+  for (unsigned b0 = threadIdx.x; b0 < gridDim.x; b0 += W * blockDim.x) {
+    T q[NV][W];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
         const unsigned b = b0 + k * blockDim.x;
-        q[k] = b < gridDim.x ? __ldcg(src + b) : T(0);
+        q[i][k] = b < gridDim.x ? __ldcg(partials + (size_t)i * gridDim.x + b) : T(0);
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (b0 + k * blockDim.x < gridDim.x) s += q[k];
-    }
-    acc[i] = s;
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+      for (int k = 0; k < W; ++k)
+        if (b0 + k * blockDim.x < gridDim.x) acc[i] += q[i][k];
   }
   if constexpr (WIDE) block_sum_wide<NV>(acc, smem);
   else block_sum<NV>(acc, smem);
