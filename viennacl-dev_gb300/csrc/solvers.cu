@@ -774,12 +774,15 @@ __global__ void __launch_bounds__(256)
     for (int q = 0; q < 8; ++q) t += red[j * 8 + q];
     partials[(size_t)(j0 + j) * nb + blockIdx.x] = t;
   }
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1;
+  if (threadIdx.x == 0) {
+    // one acquire-release ticket (the barrier above orders the block's
+    // partial writes before it, the one below the last block's reads after)
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> ticket(*counter);
+    am_last = ticket.fetch_add(1u, cuda::memory_order_acq_rel) == gridDim.x * gridDim.y - 1;
+  }
   __syncthreads();
   if (!am_last) return;
-  __threadfence();
   // last block: one warp per projection, partials read at L2 in a fixed order
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int j = warp; j < k; j += 8) {

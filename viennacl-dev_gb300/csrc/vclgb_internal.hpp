@@ -1,6 +1,7 @@
 // vclgb_internal.hpp -- shared host/device definitions of the GB300 sparse engine.
 #pragma once
 
+#include <cuda/atomic>
 #include <cuda_runtime.h>
 #include <atomic>
 #include <initializer_list>
@@ -513,13 +514,14 @@ __device__ __forceinline__ bool grid_reduce(T (&v)[NV], T *partials, unsigned *c
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) partials[(size_t)i * gridDim.x + blockIdx.x] = v[i];
-    __threadfence();
-    unsigned t = atomicAdd(counter, 1u);
+    // one acquire-release ticket: it publishes this block's partials and, in
+    // the block that takes the last ticket, orders the reads below after every
+    // other block's partials (the barrier carries that to the whole block; a
+    // fence in every thread waited for each thread's own outstanding vector
+    // stores, on the serial tail)
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> ticket(*counter);
+    const unsigned t = ticket.fetch_add(1u, cuda::memory_order_acq_rel);
     am_last = (t == gridDim.x - 1);
-    // acquire in the thread that took the last ticket only: the barrier
-    // below orders the block's reads after it (a fence in every thread waited
-    // for each thread's own outstanding vector stores, on the serial tail)
-    if (am_last) __threadfence();
   }
   __syncthreads();
   if (!am_last) return false;
