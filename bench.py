@@ -38,8 +38,8 @@ import vclgb_gen as gen  # noqa: E402
 METRIC = "CG solve s @1e-10 FP64 resid: mixed/batched vs plain FP64 on GPU; SpMV GB/s"
 # DRAM bytes (read + write) of one launch of the CG SpMV phase kernel on the
 # 128^3 Laplacian, from the ncu capture summarised in
-# profiles/csr_fixed_laplace3d_128.md (200,195,840 read + 11,860,992 written)
-TRAFFIC_SPMV_CG = 212056832
+# profiles/csr_fixed_laplace3d_128.md (200,191,232 read + 12,301,824 written)
+TRAFFIC_SPMV_CG = 212493056
 WORKLOAD = "3D 7-point Laplacian 128^3 (2,097,152 rows, 14,581,760 nnz), FP64 CSR, pipelined CG to 1e-10"
 
 
