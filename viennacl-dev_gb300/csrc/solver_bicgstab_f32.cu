@@ -1,0 +1,6 @@
+// bicgstab_solve<float>: one instantiation of the solvers in solvers.cuh.
+#include "solvers.cuh"
+
+namespace vclgb {
+template void bicgstab_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *, const Precond *);
+}  // namespace vclgb

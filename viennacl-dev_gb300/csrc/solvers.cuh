@@ -1,10 +1,13 @@
-// solvers.cu -- CG, BiCGStab, GMRES and the mixed-precision solvers with every
-// reduction, scalar recurrence and convergence test on the device.
+// solvers.cuh -- CG, BiCGStab and GMRES with every reduction, scalar
+// recurrence and convergence test on the device.  Each solver_<method>_<type>.cu
+// translation unit instantiates one of them for one value type, so the six
+// compile in parallel.
 //
 // Each solver is a fixed sequence of fused kernels per iteration; scalars
 // live in a device state struct written by the last block of the kernel that
 // completes the reduction, and read by the next kernel.  The iterations loop
 // on the device (run_iterations); small systems run in one cluster launch.
+#pragma once
 #include <algorithm>
 #include <cmath>
 
@@ -1266,7 +1269,7 @@ struct Workspace {
   template <typename X> X *at(size_t off) const { return reinterpret_cast<X *>(buf.as<char>() + off); }
 };
 
-static uint32_t auto_check_every(const vclgbSolverTag *tag, uint32_t rows) {
+static inline uint32_t auto_check_every(const vclgbSolverTag *tag, uint32_t rows) {
   if (tag->check_every) return tag->check_every;
   if (rows < (1u << 16)) return 32;
   if (rows < (1u << 20)) return 16;
@@ -1296,7 +1299,7 @@ static St<T> make_state(const vclgbSolverTag *tag) {
   return s;
 }
 
-static bool diag_needed(const Precond *P) { return P && P->kind == 1; }
+static inline bool diag_needed(const Precond *P) { return P && P->kind == 1; }
 
 // ===========================================================================
 // Small systems in one thread-block cluster.  Below a few tens of thousands of
@@ -2218,12 +2221,5 @@ void gmres_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag,
   if (P) gmres_precond_solve<T>(be, A, b, x, tag, P);
   else gmres_pipelined_solve<T>(be, A, b, x, tag);
 }
-
-template void cg_solve<double>(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, const Precond *);
-template void cg_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *, const Precond *);
-template void bicgstab_solve<double>(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, const Precond *);
-template void bicgstab_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *, const Precond *);
-template void gmres_solve<double>(Backend &, Matrix &, const double *, double *, vclgbSolverTag *, const Precond *);
-template void gmres_solve<float>(Backend &, Matrix &, const float *, float *, vclgbSolverTag *, const Precond *);
 
 }  // namespace vclgb
