@@ -143,6 +143,37 @@ def barrier(ws):
 
 
 # ---------------------------------------------------------------------------
+def graph_apply_time(V, torch, P, vec, reps):
+    """Device time of one preconditioner apply replayed from a CUDA graph:
+    a second backend on a side stream, one apply captured on it, replayed
+    `reps` times between CUDA events on that stream.  None if the capture
+    fails."""
+    try:
+        s = torch.cuda.Stream()
+        be = V.Backend(stream=s.cuda_stream)
+        ptr = V._ptr(vec)
+        torch.cuda.synchronize()
+        for _ in range(3):
+            be.check(be.lib.vclgbPrecondApply(be.h, P.h, ptr))
+        be.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            be.check(be.lib.vclgbPrecondApply(be.h, P.h, ptr))
+        with torch.cuda.stream(s):
+            for _ in range(3):
+                g.replay()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                g.replay()
+            e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+    except Exception:
+        return None
+
+
 def time_events(fn, reps):
     """Average device time of fn() over reps, CUDA events, synchronised both sides."""
     import torch
@@ -569,7 +600,16 @@ def bench_chow_patel(V, torch, peak):
     r = {"rows": n, "setup_s": t_setup, "nnz_L": int(inf.nnz_L), "nnz_U": int(inf.nnz_U),
          "apply_us": t_apply * 1e6, "apply_bytes": int(apply_bytes),
          "apply_GBs": apply_bytes / t_apply / 1e9,
-         "apply_frac_of_peak": apply_bytes / t_apply / 1e9 / peak}
+         "apply_frac_of_peak": apply_bytes / t_apply / 1e9 / peak,
+         "apply_timing": "vclgbPrecondApply called from the host 20 times: the five "
+                         "launches' host submission sets the pace"}
+    t_graph = graph_apply_time(V, torch, P, bd.clone(), 50)
+    if t_graph is not None:
+        r["apply_graph_us"] = t_graph * 1e6
+        r["apply_graph_frac_of_peak"] = apply_bytes / t_graph / 1e9 / peak
+        r["apply_graph_timing"] = ("one apply captured in a CUDA graph on a side stream and "
+                                   "replayed 50 times, as the solvers run it inside their "
+                                   "captured iterations")
     tag = V.bicgstab_tag(1e-10, 5000)
     V.solve(A, bd, V.bicgstab_tag(1e-10, 5000), P)
     torch.cuda.synchronize()
