@@ -458,16 +458,17 @@ VCLGB_API void vclgbSolverTagInit(vclgbSolverTag *tag, int kind);
  * CG of linalg/cg.hpp:257-322, with the same stopping tests.  The whole
  * iteration (SpMV, reductions, scalar recurrences, convergence test) runs on
  * the device, looping in a CUDA graph until the status word says done; the
- * host waits once.  Systems of up to 24,000 rows (CSR, no preconditioner or a
- * diagonal one) run in one thread-block-cluster launch.
+ * host waits once.  Systems of up to 32,768 rows (CSR, no preconditioner or a
+ * diagonal one; at most 2,048 rows a CTA of the cluster) run in one
+ * thread-block-cluster launch.
  * d_b, d_x: contiguous device vectors of length rows; x is overwritten
  * (initial guess 0, as in the reference). */
 VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
                                    vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, bicgstab_tag[, precond]): pipelined (bicgstab.hpp:96-215)
  * without, generic (bicgstab.hpp:398-489) with a preconditioner.  Systems of
- * up to 24,000 rows (CSR, no preconditioner or a diagonal one) run in one
- * thread-block-cluster launch. */
+ * up to 32,768 rows (CSR, no preconditioner or a diagonal one; at most 2,048
+ * rows a CTA of the cluster) run in one thread-block-cluster launch. */
 VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend be, vclgbMatrix A, const void *d_b,
                                          void *d_x, vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, gmres_tag[, precond]).  precond == NULL runs the
