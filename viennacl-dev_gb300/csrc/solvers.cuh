@@ -1937,6 +1937,8 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
   size_t o_part = ws.add(8 * kMaxSpmvGrid * sizeof(T));
   size_t o_cnt = ws.add(64);
   size_t vb = std::max<size_t>(n, 1) * sizeof(T);
+  // x's working copy first, so that the vectors of an iteration are one range
+  size_t o_x = ws.add(vb);
   size_t o_r = ws.add(vb), o_p = ws.add(vb), o_q = ws.add(vb), o_z = ws.add(vb);
   size_t o_hyb = ws.add(hyb_scratch_bytes(A));
   ws.commit(be);
@@ -1954,6 +1956,13 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
     set_tag_outputs(be, st, tag);
     return;
   }
+  // x, r, p, q (and z with a preconditioner) kept in L2 while A streams:
+  // the iterations update the working copy of x, copied out at the end
+  T *const x_out = x;
+  const size_t vec_bytes = (size_t)((char *)((P ? z : q) + n) - (char *)ws.at<T>(o_x));
+  const size_t mat_bytes = (size_t)A.nnz * (4 + sizeof(T)) + ((size_t)n + 1) * 4;
+  L2Persist l2(be, ws.at<T>(o_x), vec_bytes, mat_bytes);
+  if (l2.on) x = ws.at<T>(o_x);
   if (!P) {
     // pipelined CG
     vec_pass<T>(be, n, CgInit<T>{b, x, r, p, st}, red);
@@ -1985,6 +1994,9 @@ void cg_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbSolverTag *tag, con
       vec_pass<T>(be, n, PcgP<T>{p, z, st}, red);
     });
   }
+  if (x != x_out)
+    VCLGB_CUDA(cudaMemcpyAsync(x_out, x, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice,
+                               be.stream));
   set_tag_outputs(be, st, tag);
 }
 

@@ -147,6 +147,11 @@ struct Backend {
   // 78.1 us without, 79.6 us with -- the serial tail of each kernel's
   // last-block reduction is not hidden by starting the next kernel early.
   bool pdl = false;
+  // L2 persisting access window put on every kernel launched through
+  // launch_kernel (num_bytes 0: none); open only inside an L2Persist scope
+  cudaAccessPolicyWindow l2_window = {};
+  // the device's persisting-L2 limit, largest window and L2 size (read once)
+  long l2_persist_max = -1, l2_window_max = 0, l2_bytes = 0;
 };
 
 // Launches kern<<<grid, block, smem, be.stream>>>(args...), with programmatic
@@ -161,13 +166,79 @@ inline void launch_kernel(Backend &be, void (*kern)(KArgs...), int grid, int blo
   cfg.blockDim = dim3((unsigned)block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = be.stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[2];
+  unsigned na = 0;
+  if (be.pdl) {
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
+  if (be.l2_window.num_bytes) {
+    attr[na].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[na].val.accessPolicyWindow = be.l2_window;
+    ++na;
+  }
   cfg.attrs = attr;
-  cfg.numAttrs = be.pdl ? 1 : 0;
+  cfg.numAttrs = na;
   VCLGB_CUDA(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
 }
+
+// Keeps a large solve's vectors resident in L2 while its matrix streams
+// through it: the launches inside the scope carry an access-policy window over
+// the vectors whose hits persist (the rest streams), backed by a persisting
+// set-aside of the context's L2.  Only where the vectors are large (32 MB or
+// more) and vectors and matrix together exceed L2; the set-aside is a limit of
+// the calling context, and the scope puts back the caller's value on exit,
+// after the stream has drained and the persisting lines are released.
+constexpr size_t kL2PersistMin = 32u << 20;
+
+struct L2Persist {
+  Backend &be;
+  size_t old_limit = 0;
+  bool on = false;
+  L2Persist(Backend &b, void *base, size_t bytes, size_t other_bytes) : be(b) {
+    if (be.l2_persist_max < 0) {
+      int pm = 0, wm = 0, l2 = 0;
+      if (cudaDeviceGetAttribute(&pm, cudaDevAttrMaxPersistingL2CacheSize, be.device) !=
+              cudaSuccess ||
+          cudaDeviceGetAttribute(&wm, cudaDevAttrMaxAccessPolicyWindowSize, be.device) !=
+              cudaSuccess ||
+          cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, be.device) != cudaSuccess)
+        pm = wm = l2 = 0;
+      (void)cudaGetLastError();
+      be.l2_persist_max = pm;
+      be.l2_window_max = wm;
+      be.l2_bytes = l2;
+    }
+    if (be.l2_persist_max <= 0 || be.l2_window_max <= 0 || bytes < kL2PersistMin ||
+        bytes + other_bytes <= (size_t)be.l2_bytes)
+      return;
+    const size_t carve = bytes < (size_t)be.l2_persist_max ? bytes : (size_t)be.l2_persist_max;
+    if (cudaDeviceGetLimit(&old_limit, cudaLimitPersistingL2CacheSize) != cudaSuccess ||
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, carve) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    cudaAccessPolicyWindow w = {};
+    w.base_ptr = base;
+    w.num_bytes = bytes < (size_t)be.l2_window_max ? bytes : (size_t)be.l2_window_max;
+    w.hitRatio = carve >= w.num_bytes ? 1.0f : (float)((double)carve / (double)w.num_bytes);
+    w.hitProp = cudaAccessPropertyPersisting;
+    w.missProp = cudaAccessPropertyStreaming;
+    be.l2_window = w;
+    on = true;
+  }
+  ~L2Persist() {
+    if (!on) return;
+    be.l2_window = cudaAccessPolicyWindow{};
+    (void)cudaStreamSynchronize(be.stream);
+    (void)cudaCtxResetPersistingL2Cache();
+    (void)cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, old_limit);
+    (void)cudaGetLastError();
+  }
+  L2Persist(const L2Persist &) = delete;
+  L2Persist &operator=(const L2Persist &) = delete;
+};
 
 // Starts a timed region of `kind` on the backend's stream; returns the pair
 // index, or -1 when timing is off.
