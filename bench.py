@@ -37,9 +37,11 @@ import vclgb_gen as gen  # noqa: E402
 
 METRIC = "CG solve s @1e-10 FP64 resid: mixed/batched vs plain FP64 on GPU; SpMV GB/s"
 # DRAM bytes (read + write) of one launch of the CG SpMV phase kernel on the
-# 128^3 Laplacian, from the ncu capture summarised in
-# profiles/csr_fixed_laplace3d_128.md (200,191,232 read + 12,301,824 written)
-TRAFFIC_SPMV_CG = 212493056
+# 128^3 Laplacian in the solve's steady state, with the solve's vectors held in
+# the persisting L2 window: the ncu capture summarised in
+# profiles/csr_fixed_laplace3d_128.md (183,493,248 read + 2,555,520 written, the
+# mean of two consecutive launches; the matrix alone is 183.4 MB)
+TRAFFIC_SPMV_CG = 186048768
 WORKLOAD = "3D 7-point Laplacian 128^3 (2,097,152 rows, 14,581,760 nnz), FP64 CSR, pipelined CG to 1e-10"
 
 
@@ -274,11 +276,12 @@ def run_ours(args):
     out["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                        "frac": gbs / peak, "peak_kind": peak_kind,
                        "kernel": "csr_fixed_kernel<1,7,double,EpiCg<double>> (CSR SpMV + CG dots, "
-                                 "thread per row; 68% of the solve's device time)",
+                                 "thread per row; 67% of the solve's device time)",
                        "algorithmic_bytes_per_launch": b_spmv,
                        "avg_launch_us": us_spmv, "launches_timed": int(t_spmv.size),
                        "traffic": TRAFFIC_SPMV_CG,
-                       "traffic_source": "profiles/csr_fixed_laplace3d_128.md (ncu, one launch)",
+                       "traffic_source": "profiles/csr_fixed_laplace3d_128.md (ncu, steady-state "
+                                         "launches, vectors in the L2 window)",
                        "second_kernel": {
                            "kernel": "vec_pass_kernel<double,CgUpdate<double>>",
                            "algorithmic_bytes_per_launch": b_vec, "avg_launch_us": us_vec,
