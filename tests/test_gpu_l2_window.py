@@ -1,0 +1,91 @@
+"""The persisting L2 window of large stencil solves (CG and BiCGStab): the
+context's persisting set-aside is put back after every solve, also when two
+solves on separate backends, streams and host threads overlap, and the
+overlapping solves give the results of the sequential ones bit for bit.  The
+limit is read through the CUDA runtime that PyTorch loaded (the library links
+its own copy, but both use the device's primary context)."""
+import ctypes
+import threading
+
+import numpy as np
+import pytest
+
+import vclgb_gen as gen
+from conftest import iters_close
+
+pytestmark = pytest.mark.gpu
+
+LIMIT_PERSISTING_L2 = 0x06  # cudaLimitPersistingL2CacheSize
+
+
+@pytest.fixture(scope="module")
+def V():
+    import torch
+    import vclgb
+    torch.cuda.set_device(0)
+    torch.zeros(1, device="cuda")
+    return vclgb
+
+
+def _runtime():
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    pytest.skip("no CUDA runtime library to read the limit through")
+
+
+def _persisting_limit(rt):
+    v = ctypes.c_size_t(0)
+    assert rt.cudaDeviceGetLimit(ctypes.byref(v), LIMIT_PERSISTING_L2) == 0
+    return v.value
+
+
+def _problem(V, be=None):
+    import torch
+    rp, ci, v = gen.laplace3d(128)
+    n = len(rp) - 1
+    A = V.compressed_matrix(rp, ci, v, be=be) if be is not None else V.compressed_matrix(rp, ci, v)
+    b = torch.tensor(gen.rhs_uniform(n, 1), device="cuda")
+    return A, b
+
+
+def test_set_aside_restored_and_overlapping_solves(V):
+    import torch
+    rt = _runtime()
+    before = _persisting_limit(rt)
+    A, b = _problem(V)
+    tag = V.cg_tag(1e-10, 3000)
+    x_seq = V.solve(A, b, tag).cpu().numpy()
+    assert tag.status() == V.SUCCESS and iters_close(tag.iters(), 536)
+    assert _persisting_limit(rt) == before
+    # two solves at once on their own backends (streams) from two host threads
+    out, errs = {}, []
+    streams = [torch.cuda.Stream() for _ in range(2)]
+    backends = [V.Backend(stream=s.cuda_stream) for s in streams]
+    problems = [_problem(V, be) for be in backends]
+    torch.cuda.synchronize()
+
+    def work(k):
+        try:
+            Ak, bk = problems[k]
+            t = V.cg_tag(1e-10, 3000)
+            with torch.cuda.stream(streams[k]):
+                xk = V.solve(Ak, bk, t)
+            backends[k].synchronize()
+            out[k] = (t.status(), t.iters(), xk.cpu().numpy())
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errs, errs
+    for k in range(2):
+        st, it, xk = out[k]
+        assert st == V.SUCCESS and it == tag.iters()
+        assert np.array_equal(xk, x_seq)
+    assert _persisting_limit(rt) == before

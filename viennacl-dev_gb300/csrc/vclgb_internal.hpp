@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -194,11 +195,25 @@ inline void launch_kernel(Backend &be, void (*kern)(KArgs...), int grid, int blo
 // lines are released.
 constexpr size_t kL2PersistMin = 32u << 20;
 
+// The persisting set-aside is a limit of the device's context, shared by every
+// solve of the process: the first scope to open saves the caller's value, a
+// concurrent one may only raise it, and the last to close releases the
+// persisting lines and puts the saved value back.
+struct L2SetAside {
+  std::mutex mu;
+  int active = 0;
+  size_t saved = 0, current = 0;
+};
+inline L2SetAside &l2_set_aside(int device) {
+  static L2SetAside per_device[64];
+  return per_device[device & 63];
+}
+
 struct L2Persist {
   Backend &be;
-  size_t old_limit = 0;
   bool on = false;
   L2Persist(Backend &b, void *base, size_t bytes, size_t other_bytes) : be(b) {
+    if (bytes < kL2PersistMin) return;
     if (be.l2_persist_max < 0) {
       int pm = 0, wm = 0, l2 = 0;
       if (cudaDeviceGetAttribute(&pm, cudaDevAttrMaxPersistingL2CacheSize, be.device) !=
@@ -212,7 +227,7 @@ struct L2Persist {
       be.l2_window_max = wm;
       be.l2_bytes = l2;
     }
-    if (be.l2_persist_max <= 0 || be.l2_window_max <= 0 || bytes < kL2PersistMin ||
+    if (be.l2_persist_max <= 0 || be.l2_window_max <= 0 ||
         bytes + other_bytes <= (size_t)be.l2_bytes)
       return;
     const size_t carve = bytes < (size_t)be.l2_persist_max ? bytes : (size_t)be.l2_persist_max;
@@ -220,11 +235,28 @@ struct L2Persist {
     // smaller normal L2 loses (Jacobi-PCG on 192^3 diffusion, 30 % held: 234 ->
     // 252 us an iteration; 60-100 % held: 4-9 % faster)
     if (carve * 2 < bytes) return;
-    if (cudaDeviceGetLimit(&old_limit, cudaLimitPersistingL2CacheSize) != cudaSuccess ||
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, carve) != cudaSuccess) {
+    int cur = -1;  // the limit belongs to the current device's context
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != be.device) {
       (void)cudaGetLastError();
       return;
     }
+    L2SetAside &g = l2_set_aside(be.device);
+    std::lock_guard<std::mutex> lock(g.mu);
+    if (g.active == 0) {
+      if (cudaDeviceGetLimit(&g.saved, cudaLimitPersistingL2CacheSize) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return;
+      }
+      g.current = g.saved;
+    }
+    if (carve > g.current) {
+      if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, carve) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return;
+      }
+      g.current = carve;
+    }
+    ++g.active;
     // the leading `carve` bytes of the range persist, all of them: a window
     // wider than the set-aside with a fractional hit ratio pins a random part
     // of every vector and leaves less L2 to the rest (measured slower)
@@ -241,8 +273,13 @@ struct L2Persist {
     if (!on) return;
     be.l2_window = cudaAccessPolicyWindow{};
     (void)cudaStreamSynchronize(be.stream);
-    (void)cudaCtxResetPersistingL2Cache();
-    (void)cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, old_limit);
+    L2SetAside &g = l2_set_aside(be.device);
+    std::lock_guard<std::mutex> lock(g.mu);
+    if (--g.active == 0) {
+      (void)cudaCtxResetPersistingL2Cache();
+      (void)cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, g.saved);
+      g.current = g.saved;
+    }
     (void)cudaGetLastError();
   }
   L2Persist(const L2Persist &) = delete;
