@@ -460,7 +460,12 @@ VCLGB_API void vclgbSolverTagInit(vclgbSolverTag *tag, int kind);
  * the device, looping in a CUDA graph until the status word says done; the
  * host waits once.  Systems of up to 32,768 rows (CSR, no preconditioner or a
  * diagonal one; at most 2,048 rows a CTA of the cluster) run in one
- * thread-block-cluster launch.
+ * thread-block-cluster launch.  Large stencil-like systems (one row-length
+ * bin, vectors of 32 MB or more, vectors and matrix beyond L2) keep their
+ * vectors in a persisting L2 window: for the duration of the call the
+ * current context's cudaLimitPersistingL2CacheSize is raised, and it is back
+ * at the caller's value when the call returns (overlapping calls in the
+ * process share one set-aside; the last to return restores it).
  * d_b, d_x: contiguous device vectors of length rows; x is overwritten
  * (initial guess 0, as in the reference). */
 VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
@@ -468,7 +473,9 @@ VCLGB_API vclgbStatus vclgbSolveCG(vclgbBackend be, vclgbMatrix A, const void *d
 /* linalg::solve(A, b, bicgstab_tag[, precond]): pipelined (bicgstab.hpp:96-215)
  * without, generic (bicgstab.hpp:398-489) with a preconditioner.  Systems of
  * up to 32,768 rows (CSR, no preconditioner or a diagonal one; at most 2,048
- * rows a CTA of the cluster) run in one thread-block-cluster launch. */
+ * rows a CTA of the cluster) run in one thread-block-cluster launch.  Large
+ * stencil-like systems use the persisting L2 window described for
+ * vclgbSolveCG. */
 VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend be, vclgbMatrix A, const void *d_b,
                                          void *d_x, vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, gmres_tag[, precond]).  precond == NULL runs the
