@@ -89,3 +89,33 @@ def test_set_aside_restored_and_overlapping_solves(V):
         assert st == V.SUCCESS and it == tag.iters()
         assert np.array_equal(xk, x_seq)
     assert _persisting_limit(rt) == before
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_bicgstab_with_window_matches_oracle(V, pc):
+    # 2,096,704 rows of upwind convection-diffusion: seven vectors (117 MB),
+    # 72 % of them in the set-aside; BiCGStab's iteration band of the parity tests
+    import oracle
+    rp, ci, v = gen.convdiff2d(1448, 1448, peclet=5.0, shift=0.01)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 3)
+    A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.bicgstab_tag(1e-10, 1000)
+    x = V.solve(A, b, tag, P) if P else V.solve(A, b, tag)
+    _, it_ref, _ = oracle.solve("bicgstab", rp, ci, v, b, 1e-10, 1000, pc)
+    assert tag.status() == V.SUCCESS
+    assert abs(tag.iters() - it_ref) <= max(2, int(0.15 * it_ref)), (tag.iters(), it_ref)
+    assert oracle.rel_residual(rp, ci, v, x.cpu().numpy(), b) < 1e-8
+
+
+def test_refined_solve_with_window_reaches_fp64_residual(V):
+    # 192^3 variable-coefficient diffusion: the FP32 inner Jacobi-PCG on the DIA
+    # copy keeps its vectors in the window; the FP64 refinement reaches 1e-10
+    import oracle
+    rp, ci, v, f = gen.diffusion3d(192)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.refined_cg_tag(1e-10, 40000, 1e-4)
+    x = V.solve(A, f, tag)
+    assert tag.status() == V.SUCCESS
+    assert oracle.rel_residual(rp, ci, v, x.cpu().numpy(), f) < 1e-10
