@@ -44,30 +44,45 @@ def _newest_header():
 
 
 def _compile(src, extra):
+    """(object path, whether it was compiled now).  The object is written under
+    a temporary name and renamed, so an interrupted or concurrent build never
+    leaves a partial object that looks up to date."""
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
             and os.path.getmtime(obj) >= _newest_header()):
-        return obj
-    cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
+        return obj, False
+    tmp = "%s.%d.tmp" % (obj, os.getpid())
+    cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
+        if os.path.exists(tmp):
+            os.remove(tmp)
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
-    return obj
+    os.replace(tmp, obj)
+    return obj, True
 
 
 def build(verbose=False, extra=None):
-    """Compile (incrementally) and link libvclgb.so; returns its path."""
+    """Compile (incrementally) and link libvclgb.so; returns its path.  The
+    library is relinked whenever an object was compiled by this call or is
+    newer than it, into a temporary file renamed over the old one."""
     extra = list(extra or [])
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
+        done = list(ex.map(lambda s: _compile(s, extra), srcs))
+    objs = [o for o, _ in done]
+    compiled = any(c for _, c in done)
     newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+    if compiled or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        tmp = "%s.%d.tmp" % (LIB, os.getpid())
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
+            if os.path.exists(tmp):
+                os.remove(tmp)
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+        os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)
     return LIB
