@@ -39,9 +39,9 @@ METRIC = "CG solve s @1e-10 FP64 resid: mixed/batched vs plain FP64 on GPU; SpMV
 # DRAM bytes (read + write) of one launch of the CG SpMV phase kernel on the
 # 128^3 Laplacian in the solve's steady state, with the solve's vectors held in
 # the persisting L2 window: the ncu capture summarised in
-# profiles/csr_fixed_laplace3d_128.md (183,493,248 read + 2,555,520 written, the
+# profiles/csr_fixed_laplace3d_128.md (183,556,096 read + 1,039,872 written, the
 # mean of two consecutive launches; the matrix alone is 183.4 MB)
-TRAFFIC_SPMV_CG = 186048768
+TRAFFIC_SPMV_CG = 184595968
 WORKLOAD = "3D 7-point Laplacian 128^3 (2,097,152 rows, 14,581,760 nnz), FP64 CSR, pipelined CG to 1e-10"
 
 
