@@ -249,9 +249,9 @@ struct L2Persist {
       }
       g.current = g.saved;
     }
-    // the device's whole set-aside even where the window is smaller: sized to
-    // the window (128^3 CG, 67 MB) half of its lines still missed in the
-    // steady state, and the solve took 70.2 against 69.1 us an iteration
+    // the device's whole set-aside even where the window is smaller: with a
+    // set-aside sized to the window (128^3 CG, 67 MB) the solve took 70.2 us an
+    // iteration, with the whole set-aside 69.1 us
     const size_t aside = (size_t)be.l2_persist_max;
     if (aside > g.current) {
       if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, aside) != cudaSuccess) {
