@@ -152,3 +152,58 @@ def test_small_random_matrices(V, solver, pc):
     band = 0.02 if solver == "cg" else 0.15
     assert abs(tag.iters() - it_ref) <= max(2, int(band * it_ref)), (tag.iters(), it_ref)
     assert oracle.rel_residual(rp, ci, v, x.cpu().numpy(), b) < 1e-8
+
+
+@pytest.mark.parametrize("N,kd", [(30, 10), (70, 20), (70, 30), (90, 30)])
+def test_small_gmres_matches_oracle(V, N, kd):
+    # unpreconditioned GMRES on upwind convection-diffusion in one cluster
+    # launch (x, r and the Krylov basis in shared memory): the oracle's
+    # iteration count within the GMRES band, the true residual at the tolerance
+    import torch
+    rp, ci, v = gen.convdiff2d(N, N, peclet=5.0, shift=0.05)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 16)
+    A = V.compressed_matrix(rp, ci, v)
+    tag = V.gmres_tag(1e-10, 3000, kd)
+    l0 = A.be.launches()
+    x = V.solve(A, torch.tensor(b, device="cuda"), tag)
+    launches = A.be.launches() - l0
+    _, it_ref, _ = oracle.solve("gmres", rp, ci, v, b, 1e-10, 3000, krylov_dim=kd)
+    assert tag.status() == V.SUCCESS
+    assert launches <= 4, launches
+    assert iters_close(tag.iters(), it_ref, 0.05), (tag.iters(), it_ref)
+    assert oracle.rel_residual(rp, ci, v, x.cpu().numpy(), b) < 1e-9
+
+
+def test_small_gmres_fp32_and_paths_agree(V):
+    import torch
+    rp, ci, v = gen.convdiff2d(60, 60, peclet=5.0, shift=0.05)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 17)
+    # FP32
+    A32 = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    t32 = V.gmres_tag(1e-5, 3000, 20)
+    x32 = V.solve(A32, torch.tensor(b.astype(np.float32), device="cuda"), t32)
+    assert t32.status() == V.SUCCESS
+    assert oracle.rel_residual(rp, ci, v, x32.cpu().numpy().astype(np.float64), b) < 1e-4
+    # the cluster path and, with kernel timing on, the per-phase kernels
+    A = V.compressed_matrix(rp, ci, v)
+    bd = torch.tensor(b, device="cuda")
+    t0 = V.gmres_tag(1e-12, 3000, 20)
+    x0 = V.solve(A, bd, t0).cpu().numpy()
+    A.be.set_kernel_timing(True)
+    try:
+        t1 = V.gmres_tag(1e-12, 3000, 20)
+        x1 = V.solve(A, bd, t1).cpu().numpy()
+        # a capped solve: the iteration count and status follow the same rule
+        c1 = V.gmres_tag(1e-12, 25, 10)
+        V.solve(A, bd, c1)
+    finally:
+        A.be.set_kernel_timing(False)
+    assert iters_close(t0.iters(), t1.iters())
+    assert np.linalg.norm(x0 - x1) / np.linalg.norm(x1) < 1e-9
+    c0 = V.gmres_tag(1e-12, 25, 10)
+    V.solve(A, bd, c0)
+    assert c0.status() == c1.status() == V.NOT_CONVERGED
+    assert c0.iters() == c1.iters()
+    assert abs(c0.error() - c1.error()) < 1e-6 * c1.error()

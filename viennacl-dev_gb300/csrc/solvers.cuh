@@ -1928,6 +1928,294 @@ static bool cluster_bicgstab(Backend &be, const Matrix &A, const T *b, T *x, St<
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Unpreconditioned GMRES of a small system in one cluster: the per-phase
+// solve's steps (GmInit, gm_cycle_check, GmScaleR, EpiGmResid, EpiGmV, the
+// classical Gram-Schmidt pass, GmNormalize, GmCycleEnd, GmUpdateX) with x, r
+// and the Krylov basis in shared memory, the products gathering through
+// distributed shared memory.  The k dot products of a Gram-Schmidt step are
+// summed in each CTA in chunks of eight, pushed to every CTA's slots and
+// added after one cluster barrier; the other reductions are cl_step's.  Every
+// CTA keeps the same GMRES state and runs the same scalar steps on thread 0.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kClusterGmresMaxK = 32;
+
+template <typename T>
+struct GcState {
+  ClState<T> cl;                        // single-value reductions (cl_step)
+  T mpart[2][16][kClusterGmresMaxK];    // multi-dot slots by rank, double buffered
+  T mwarp[8 * (kClusterSolveThreads / 32)];
+  T nrhs, rho0, inv_rho0, rho, vnorm2, inv_vnorm;
+  T R[kClusterGmresMaxK * kClusterGmresMaxK];
+  T xi[kClusterGmresMaxK], h[kClusterGmresMaxK], coef[kClusterGmresMaxK];
+  double tol, abs_tol, error;
+  unsigned K, iters, restart_count, max_restarts;
+  int kk, done, mbuf;
+};
+
+template <typename T>
+__device__ __forceinline__ void gc_cycle_check(GcState<T> &g) {  // gm_cycle_check
+  if ((double)g.rho0 <= g.abs_tol) { g.done = kConverged; return; }
+  g.rho = T(1);
+  if ((double)(g.rho0 / g.nrhs) < g.tol || (double)g.rho0 < g.abs_tol) {
+    g.done = kConverged;
+    return;
+  }
+  if (g.restart_count > g.max_restarts) g.done = kMaxIters;
+}
+
+template <typename T>
+__device__ __forceinline__ void gc_cycle_end(GcState<T> &g) {  // GmCycleEnd
+  if (g.done != kRunning) { g.kk = 0; return; }
+  const unsigned K = g.K;
+  unsigned k = K, full_k = K;
+  for (unsigned i = 0; i < k; ++i)
+    if (fabs((double)g.R[i + i * k]) < g.tol * (double)g.R[0]) { k = i; break; }
+  T rho = g.rho;
+  for (unsigned i = 0; i < k; ++i) {
+    g.iters += 1;
+    T xi = g.xi[i];
+    if (xi >= rho || xi <= -rho) { k = i; break; }
+    rho *= sin(acos(xi / rho));
+  }
+  g.rho = rho;
+  T eta[kClusterGmresMaxK];
+  for (unsigned i = 0; i < K; ++i) eta[i] = g.xi[i];
+  for (int i2 = (int)k - 1; i2 > -1; --i2) {
+    unsigned i = (unsigned)i2;
+    for (unsigned j = i + 1; j < k; ++j) eta[i] -= g.R[i + j * full_k] * eta[j];
+    eta[i] /= g.R[i + i * full_k];
+  }
+  for (unsigned i = 0; i < k; ++i) g.coef[i] = g.rho0 * eta[i];
+  g.kk = (int)k;
+  g.error = fabs((double)(rho * g.rho0 / g.nrhs));
+  g.restart_count += 1;
+}
+
+// h_j = <v_j, w> for j < k over the cluster (V: columns of len entries);
+// the sums land in g.h and in column k of R
+template <typename T>
+__device__ __forceinline__ void gc_multidot(const T *V, uint32_t len, const T *w, uint32_t m,
+                                            uint32_t k, GcState<T> &g) {
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned nct = cl.num_blocks(), me = cl.block_rank();
+  const int b = g.mbuf;
+  for (uint32_t c0 = 0; c0 < k; c0 += 8) {
+    T acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = T(0);
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+      const T wi = w[i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (c0 + j < k) acc[j] += V[(size_t)(c0 + j) * len + i] * wi;
+    }
+    block_sum<8>(acc, g.mwarp);  // valid in every lane of warp 0
+    if (threadIdx.x < nct) {
+      T *dst = cl.map_shared_rank(&g.mpart[b][me][c0], threadIdx.x);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (c0 + j < k) dst[j] = acc[j];
+    }
+  }
+  cl_barrier();
+  if (threadIdx.x < 32) {
+    for (uint32_t j = threadIdx.x; j < k; j += 32) {
+      T t = T(0);
+      for (unsigned r = 0; r < nct; ++r) t += g.mpart[b][r][j];
+      g.h[j] = t;
+      g.R[j + (size_t)k * g.K] = t;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) g.mbuf = b ^ 1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kClusterSolveThreads, 1)
+    cluster_gmres_kernel(CsrView<T> A, const T *b, T *x, Gm<T> *gout, uint32_t shift) {
+  __shared__ GcState<T> g;
+  extern __shared__ __align__(16) unsigned char cl_vec_bytes[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t rank = cl.block_rank(), len = 1u << shift;
+  T *sx = reinterpret_cast<T *>(cl_vec_bytes), *sr = sx + len, *sV = sr + len;
+  const uint32_t n = A.rows;
+  const uint32_t r0 = min(rank << shift, n), r1 = min(r0 + len, n), m = r1 - r0;
+  const uint32_t K = gout->K;
+  if (threadIdx.x == 0) {
+    g.cl.buf = 0;
+    g.mbuf = 0;
+    g.K = K;
+    g.tol = gout->tol;
+    g.abs_tol = gout->abs_tol;
+    g.max_restarts = gout->max_restarts;
+  }
+  T d[1] = {T(0)};  // GmInit
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+    const T bi = b[r0 + i];
+    sx[i] = T(0);
+    sr[i] = bi;
+    d[0] += bi * bi;
+  }
+  __syncthreads();
+  cl_step<1>(d, g.cl, [&](const T (&s)[1]) {
+    g.nrhs = sqrt(s[0]);
+    g.rho0 = g.nrhs;
+    g.inv_rho0 = T(1) / g.rho0;
+    g.rho = T(1);
+    g.iters = 0;
+    g.error = 0;
+    g.restart_count = 0;
+    g.done = kRunning;
+    gc_cycle_check(g);  // GmCheckFirst
+  });
+  {
+    const T inv = g.inv_rho0;  // GmScaleR
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) sr[i] *= inv;
+  }
+  cl_barrier();  // r complete before the first product gathers it
+  bool first = true;
+  while (g.done == kRunning) {
+    if (!first) {
+      T e[1] = {T(0)};  // EpiGmResid: r = b - A x
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T v = b[r0 + i] - cl_row(A, r0 + i, sx, rank, shift);
+        sr[i] = v;
+        e[0] += v * v;
+      }
+      cl_step<1>(e, g.cl, [&](const T (&s)[1]) {
+        g.rho0 = sqrt(s[0]);
+        g.inv_rho0 = T(1) / g.rho0;
+        gc_cycle_check(g);
+      });
+      if (g.done != kRunning) break;
+      const T inv = g.inv_rho0;  // GmScaleR
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) sr[i] *= inv;
+      cl_barrier();
+    }
+    first = false;
+    for (uint32_t k = 0; k < K; ++k) {
+      T *vk = sV + (size_t)k * len;
+      const T *src = k == 0 ? sr : sV + (size_t)(k - 1) * len;
+      T e[1] = {T(0)};  // EpiGmV: v_k = A src, ||v_k||^2
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T acc = cl_row(A, r0 + i, src, rank, shift);
+        vk[i] = acc;
+        e[0] += acc * acc;
+      }
+      // ||v_k||^2 of the product is used for k = 0 only (the Gram-Schmidt
+      // pass recomputes it after), and the pass reads this CTA's rows only
+      if (k == 0)
+        cl_step<1>(e, g.cl, [&](const T (&s)[1]) {
+          g.vnorm2 = s[0];
+          g.inv_vnorm = T(1) / sqrt(s[0]);
+        });
+      if (k > 0) {  // classical Gram-Schmidt against v_0 .. v_{k-1}
+        gc_multidot(sV, len, vk, m, k, g);
+        T e2[1] = {T(0)};
+        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+          T w = vk[i];
+          for (uint32_t j = 0; j < k; ++j) w -= g.h[j] * sV[(size_t)j * len + i];
+          vk[i] = w;
+          e2[0] += w * w;
+        }
+        cl_step<1>(e2, g.cl, [&](const T (&s)[1]) {
+          g.vnorm2 = s[0];
+          g.inv_vnorm = T(1) / sqrt(s[0]);
+        });
+      }
+      const T nv = g.inv_vnorm;  // GmNormalize: v_k /= ||v_k||, xi_k = <r, v_k>
+      T e3[1] = {T(0)};
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const T v = vk[i] * nv;
+        e3[0] += sr[i] * v;
+        vk[i] = v;
+      }
+      cl_step<1>(e3, g.cl, [&](const T (&s)[1]) {
+        g.xi[k] = s[0];
+        g.R[k + (size_t)k * g.K] = sqrt(g.vnorm2);
+      });
+    }
+    if (threadIdx.x == 0) gc_cycle_end(g);
+    __syncthreads();
+    if (g.done == kRunning && g.kk > 0) {  // GmUpdateX
+      const int kk = g.kk;
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        T v = sx[i] + g.coef[0] * sr[i];
+        for (int j = 1; j < kk; ++j) v += g.coef[j] * sV[(size_t)(j - 1) * len + i];
+        sx[i] = v;
+      }
+    }
+    cl_barrier();  // x complete before the next residual product gathers it
+  }
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) x[r0 + i] = sx[i];
+  if (rank == 0 && threadIdx.x == 0) {
+    gout->iters = g.iters;
+    gout->error = g.error;
+    gout->done = g.done;
+  }
+  cl_barrier();  // no CTA leaves while another may still read its shared memory
+}
+
+// CTAs of the small-system GMRES cluster (16, 8 or 4; 0: none), once per precision
+template <typename T>
+static int cluster_gmres_ctas() {
+  static std::atomic<int> cached{-1};
+  int v = cached.load(std::memory_order_relaxed);
+  if (v >= 0) return v;
+  v = 0;
+  auto k = cluster_gmres_kernel<T>;
+  const bool ok =
+      cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kClusterSolveSmem) == cudaSuccess;
+  for (int cc : {16, 8, 4}) {
+    if (!ok) break;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cc);
+    cfg.blockDim = dim3(kClusterSolveThreads);
+    cfg.dynamicSmemBytes = kClusterSolveSmem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cc;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int c = 0;
+    if (cudaOccupancyMaxActiveClusters(&c, k, &cfg) == cudaSuccess && c > 0) {
+      v = cc;
+      break;
+    }
+  }
+  (void)cudaGetLastError();
+  cached.store(v, std::memory_order_relaxed);
+  return v;
+}
+
+// Runs the unpreconditioned small-system GMRES if it applies (Krylov
+// dimension at most 32, x, r and the basis fit the CTAs' shared memory);
+// false otherwise.  g holds the solve's parameters and receives its outcome.
+template <typename T>
+static bool cluster_gmres(Backend &be, const Matrix &A, const T *b, T *x, Gm<T> *g,
+                          uint32_t K) {
+  if (K > kClusterGmresMaxK) return false;
+  const uint32_t n = A.rows;
+  if (n == 0 || n > kClusterSolveMaxRows || A.format != VCLGB_CSR || be.timing) return false;
+  const int cc = cluster_gmres_ctas<T>();
+  if (cc == 0) return false;
+  uint32_t shift = 5;
+  while (((uint64_t)cc << shift) < n) ++shift;
+  const uint32_t len = 1u << shift;
+  if (len > kClusterSolveMaxChunk) return false;
+  const size_t smem = (size_t)(K + 2) * len * sizeof(T);
+  if (smem > kClusterSolveSmem) return false;
+  const uint32_t threads = len <= 128 ? 128 : len <= 256 ? 256 : kClusterSolveThreads;
+  const CsrView<T> view{A.row_ptr, A.col_idx, static_cast<const T *>(A.values), A.rows};
+  cluster_launch<T>(be, cluster_gmres_kernel<T>, cc, threads, smem, view, b, x, g, shift);
+  return true;
+}
+
 // bytes a product streams from the matrix (indices, values, row pointers)
 static inline size_t matrix_stream_bytes(const Matrix &A) {
   return (size_t)A.nnz * (4 + A.vsize()) + ((size_t)A.rows + 1) * 4;
@@ -2135,6 +2423,20 @@ static void gmres_pipelined_solve(Backend &be, Matrix &A, const T *b, T *x, vclg
   T *r = ws.at<T>(o_r), *V = ws.at<T>(o_V);
   void *hyb = ws.at<void>(o_hyb);
   const int *done = &g->done;
+  auto read_outcome = [&]() {
+    Gm<T> h;
+    VCLGB_CUDA(cudaMemcpyAsync(&h, g, sizeof(h), cudaMemcpyDeviceToHost, be.stream));
+    VCLGB_CUDA(cudaStreamSynchronize(be.stream));
+    tag->iters = h.iters;
+    tag->error = h.error;
+    tag->status = h.done == kConverged ? VCLGB_SUCCESS
+                : h.done == kMaxIters  ? VCLGB_NOT_CONVERGED
+                                       : VCLGB_BREAKDOWN;
+  };
+  if (cluster_gmres<T>(be, A, b, x, g, K)) {
+    read_outcome();
+    return;
+  }
   vec_pass<T>(be, n, GmInit<T>{b, x, r, g}, red);
   scalar_step(be, GmCheckFirst<T>{g});
   vec_pass<T>(be, n, GmScaleR<T>{r, g}, red);
@@ -2161,14 +2463,7 @@ static void gmres_pipelined_solve(Backend &be, Matrix &A, const T *b, T *x, vclg
   first = false;
   uint32_t max_cycles = tag->max_iters / K + 3;
   run_iterations(be, done, max_cycles, 1, true, cycle);
-  Gm<T> h;
-  VCLGB_CUDA(cudaMemcpyAsync(&h, g, sizeof(h), cudaMemcpyDeviceToHost, be.stream));
-  VCLGB_CUDA(cudaStreamSynchronize(be.stream));
-  tag->iters = h.iters;
-  tag->error = h.error;
-  tag->status = h.done == kConverged ? VCLGB_SUCCESS
-              : h.done == kMaxIters  ? VCLGB_NOT_CONVERGED
-                                     : VCLGB_BREAKDOWN;
+  read_outcome();
 }
 
 // linalg::solve(A, b, gmres_tag, precond) with any preconditioner
