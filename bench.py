@@ -505,6 +505,13 @@ def secondaries(V, torch, peak, args):
     t = time_events(lambda: V.solve(A, bd, tag), 20)
     sec["convdiff2d_70_bicgstab_latency"] = {"s": t, "iters": tag.iters(),
                                              "us_per_iter": 1e6 * t / max(tag.iters(), 1)}
+    # and GMRES(20) on it (one cluster launch with the basis in shared memory)
+    for _ in range(3):
+        V.solve(A, bd, V.gmres_tag(1e-10, 2000, 20))
+    tag = V.gmres_tag(1e-10, 2000, 20)
+    t = time_events(lambda: V.solve(A, bd, tag), 20)
+    sec["convdiff2d_70_gmres20_latency"] = {"s": t, "iters": tag.iters(),
+                                            "us_per_iter": 1e6 * t / max(tag.iters(), 1)}
     return sec
 
 

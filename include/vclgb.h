@@ -487,7 +487,10 @@ VCLGB_API vclgbStatus vclgbSolveBiCGStab(vclgbBackend be, vclgbMatrix A, const v
  * orthonormal basis is formed by classical Gram-Schmidt with one repeated
  * pass when the first cancelled more than half of the vector's norm squared
  * (the same basis as the reflections', up to rounding).  The restart
- * bookkeeping (triangular solve of size krylov_dim) runs on the device too. */
+ * bookkeeping (triangular solve of size krylov_dim) runs on the device too.
+ * Without a preconditioner, small CSR systems (krylov_dim <= 32, x, r and
+ * the basis within the cluster's shared memory: up to 8,192 rows in FP64 at
+ * krylov_dim 30, 16,384 at 20) run in one thread-block-cluster launch. */
 VCLGB_API vclgbStatus vclgbSolveGMRES(vclgbBackend be, vclgbMatrix A, const void *d_b, void *d_x,
                                       vclgbSolverTag *tag, vclgbPrecond precond);
 /* linalg::solve(A, b, mixed_precision_cg_tag(tol, max_iters, inner_tol))
