@@ -950,7 +950,8 @@ def profile_kernels(args):
         x = V.solve(A, b, V.cg_tag(1e-6, 300), V.jacobi_precond(A))
         V.solve_adjoint(A, x, x - b, V.cg_tag(1e-6, 300), solver="cg")
         # small systems (70^2 = 4,900 rows) in one cluster launch each: CG,
-        # Jacobi-PCG, BiCGStab (kernel timing off: it keeps the per-phase path)
+        # Jacobi-PCG, BiCGStab, GMRES(20) (kernel timing off: it keeps the
+        # per-phase path)
         V.backend().set_kernel_timing(False)
         rp, ci, v = gen.laplace2d(70, 70)
         A = V.compressed_matrix(rp, ci, v)
@@ -960,6 +961,7 @@ def profile_kernels(args):
         rp, ci, v = gen.convdiff2d(70, 70, peclet=5.0, shift=0.05)
         A = V.compressed_matrix(rp, ci, v)
         V.solve(A, b, V.bicgstab_tag(1e-10, 2000))
+        V.solve(A, b, V.gmres_tag(1e-10, 2000, 20))
         torch.cuda.synchronize()
         print("profile workload done")
         return
