@@ -2097,44 +2097,37 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
     for (uint32_t k = 0; k < K; ++k) {
       T *vk = sV + (size_t)k * len;
       const T *src = k == 0 ? sr : sV + (size_t)(k - 1) * len;
-      T e[1] = {T(0)};  // EpiGmV: v_k = A src, ||v_k||^2
+      // v_k = A src; for k = 0 ||v_k||^2 and <r, v_k> come with it (EpiGmV)
+      T e[2] = {T(0), T(0)};
       for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
         const T acc = cl_row(A, r0 + i, src, rank, shift);
         vk[i] = acc;
         e[0] += acc * acc;
+        e[1] += sr[i] * acc;
       }
-      // ||v_k||^2 of the product is used for k = 0 only (the Gram-Schmidt
-      // pass recomputes it after), and the pass reads this CTA's rows only
-      if (k == 0)
-        cl_step<1>(e, g.cl, [&](const T (&s)[1]) {
-          g.vnorm2 = s[0];
-          g.inv_vnorm = T(1) / sqrt(s[0]);
-        });
-      if (k > 0) {  // classical Gram-Schmidt against v_0 .. v_{k-1}
+      if (k > 0) {  // classical Gram-Schmidt against v_0 .. v_{k-1}: w, ||w||^2, <r, w>
         gc_multidot(sV, len, vk, m, k, g);
-        T e2[1] = {T(0)};
+        e[0] = e[1] = T(0);
         for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
           T w = vk[i];
           for (uint32_t j = 0; j < k; ++j) w -= g.h[j] * sV[(size_t)j * len + i];
           vk[i] = w;
-          e2[0] += w * w;
+          e[0] += w * w;
+          e[1] += sr[i] * w;
         }
-        cl_step<1>(e2, g.cl, [&](const T (&s)[1]) {
-          g.vnorm2 = s[0];
-          g.inv_vnorm = T(1) / sqrt(s[0]);
-        });
       }
-      const T nv = g.inv_vnorm;  // GmNormalize: v_k /= ||v_k||, xi_k = <r, v_k>
-      T e3[1] = {T(0)};
-      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-        const T v = vk[i] * nv;
-        e3[0] += sr[i] * v;
-        vk[i] = v;
-      }
-      cl_step<1>(e3, g.cl, [&](const T (&s)[1]) {
-        g.xi[k] = s[0];
-        g.R[k + (size_t)k * g.K] = sqrt(g.vnorm2);
+      // GmNormalize from the same reduction: R(k,k) = ||w||, xi_k = <r, w> / ||w||,
+      // then v_k /= ||w|| on this CTA's rows and a barrier before the next
+      // product gathers them
+      cl_step<2>(e, g.cl, [&](const T (&s)[2]) {
+        g.vnorm2 = s[0];
+        g.inv_vnorm = T(1) / sqrt(s[0]);
+        g.xi[k] = s[1] * g.inv_vnorm;
+        g.R[k + (size_t)k * g.K] = sqrt(s[0]);
       });
+      const T nv = g.inv_vnorm;
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) vk[i] *= nv;
+      cl_barrier();
     }
     if (threadIdx.x == 0) gc_cycle_end(g);
     __syncthreads();
