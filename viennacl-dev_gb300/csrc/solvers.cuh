@@ -1327,8 +1327,8 @@ constexpr size_t kClusterSolveSmem = 192 * 1024;  // dynamic shared memory a CTA
 // runs the same steps on the same sums) and read by the block after a barrier
 template <typename T>
 struct ClState {
-  T part[2][16][3];  // every CTA's partial sums (by rank), double buffered by phase
-  T warp[4 * 16];    // block_sum scratch (up to 3 values x 16 warps)
+  T part[2][16][4];  // every CTA's partial sums (by rank), double buffered by phase
+  T warp[4 * 16];    // block_sum scratch (up to 4 values x 16 warps)
   T rr, nrhs2, alpha, beta, ip;
   T omega, nrhs, Ap_r0, s_s, r_r0;  // BiCGStab
   double error;
@@ -1617,22 +1617,22 @@ __global__ void __launch_bounds__(kClusterSolveThreads, 1)
       cs.alpha = cs.r_r0 / v[0];
     });
     const T alpha = cs.alpha;
-    T f[1] = {T(0)};  // BicgS
-    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-      const T v = sr[i] - alpha * sAp[i];
-      f[0] += v * v;
-      ss[i] = v;
-    }
-    cl_step<1>(f, cs, [&](const T (&v)[1]) { cs.s_s = v[0]; });
-    T g[3] = {T(0), T(0), T(0)};  // EpiBicgAs
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x)  // BicgS
+      ss[i] = sr[i] - alpha * sAp[i];
+    cl_barrier();  // s complete before the product gathers it
+    // EpiBicgAs, with ||s||^2 (BicgS's reduction) from the same pass over s
+    T g[4] = {T(0), T(0), T(0), T(0)};
     for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
       const T acc = cl_row(A, r0 + i, ss, rank, shift);
+      const T vs = ss[i];
       sAs[i] = acc;
       g[0] += acc * acc;
-      g[1] += ss[i] * acc;
+      g[1] += vs * acc;
       g[2] += acc * sr0[i];
+      g[3] += vs * vs;
     }
-    cl_step<3>(g, cs, [&](const T (&v)[3]) {
+    cl_step<4>(g, cs, [&](const T (&v)[4]) {
+      cs.s_s = v[3];
       const T a = cs.r_r0 / cs.Ap_r0;
       const T bb = -v[2] / cs.Ap_r0;
       const T w = v[1] / v[0];
