@@ -319,34 +319,34 @@ struct EpiBicgAp {  // Ap = A p, <Ap, r0*>
 };
 
 template <typename T>
-struct BicgS {  // alpha = <r,r0*>/<Ap,r0*>; s = r - alpha Ap; <s,s>
-  static constexpr int NDOT = 1;
+// s = r - alpha Ap (alpha = <r,r0*>/<Ap,r0*>); <s,s> comes from the next
+// product's epilogue, which reads the same s (one grid reduction fewer)
+struct BicgS {
+  static constexpr int NDOT = 0;
   T *s_; const T *r, *Ap; St<T> *st;
   struct S { T a; };
   __device__ bool skip() const { return st->done != kRunning; }
   __device__ S load() const { return {st->alpha}; }
-  __device__ void apply(size_t i, S s, T (&d)[1]) const {
-    T v = r[i] - s.a * Ap[i];
-    d[0] += v * v;
-    s_[i] = v;
-  }
-  __device__ void finalize(const T (&s)[1]) const { st->s_s = s[0]; }
+  __device__ void apply(size_t i, S s, T (&)[1]) const { s_[i] = r[i] - s.a * Ap[i]; }
+  __device__ void finalize(const T (&)[1]) const {}
 };
 
 template <typename T>
-struct EpiBicgAs {  // As = A s, <As,As>, <s,As>, <As,r0*>; scalars; residual estimate
-  static constexpr int NDOT = 3;
+struct EpiBicgAs {  // As = A s, <As,As>, <s,As>, <As,r0*>, <s,s>; scalars; residual estimate
+  static constexpr int NDOT = 4;
   T *As; const T *s_, *r0; St<T> *st;
   struct Pre { T s, r0; };
   __device__ bool skip() const { return st->done != kRunning; }
   __device__ Pre pre(uint32_t r) const { return {s_[r], r0[r]}; }
-  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[3]) const {
+  __device__ void row(uint32_t r, T acc, const Pre &v, T (&d)[4]) const {
     As[r] = acc;
     d[0] += acc * acc;
     d[1] += v.s * acc;
     d[2] += acc * v.r0;
+    d[3] += v.s * v.s;
   }
-  __device__ void finalize(const T (&s)[3]) const {
+  __device__ void finalize(const T (&s)[4]) const {
+    st->s_s = s[3];
     T alpha = st->r_r0 / st->Ap_r0;
     T beta = -s[2] / st->Ap_r0;
     T omega = s[1] / s[0];

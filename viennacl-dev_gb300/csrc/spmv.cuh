@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(kSpmvThreads)
 // host-side dispatch
 // ---------------------------------------------------------------------------
 struct Reduction {
-  void *partials = nullptr;  // >= 3 * grid entries of T
+  void *partials = nullptr;  // >= NDOT (at most 4) * grid entries of T
   unsigned *counter = nullptr;
 };
 
