@@ -693,6 +693,18 @@ struct GmScaleR {  // r /= rho0 (the reference scales before its convergence tes
   __device__ void finalize(const T (&)[1]) const {}
 };
 
+// v_k = A src for k > 0: the Gram-Schmidt pass reduces ||w||^2 after, so the
+// product carries no reduction
+template <typename T>
+struct EpiGmVStore {
+  static constexpr int NDOT = 0;
+  T *vk; Gm<T> *g;
+  VCLGB_NO_PRE
+  __device__ bool skip() const { return g->done != kRunning; }
+  __device__ void row(uint32_t i, T acc, const Pre &, T (&)[1]) const { vk[i] = acc; }
+  __device__ void finalize(const T (&)[1]) const {}
+};
+
 template <typename T>
 struct EpiGmV {  // v_k = A src, ||v_k||^2 (used for k = 0)
   static constexpr int NDOT = 1;
@@ -2442,7 +2454,11 @@ static void gmres_pipelined_solve(Backend &be, Matrix &A, const T *b, T *x, vclg
     for (uint32_t k = 0; k < K; ++k) {
       T *vk = V + (size_t)k * ld;
       const T *src = k == 0 ? r : V + (size_t)(k - 1) * ld;
-      spmv_launch<T>(be, A, src, 0, 1, EpiGmV<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done, hyb);
+      if (k == 0)
+        spmv_launch<T>(be, A, src, 0, 1, EpiGmV<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done, hyb);
+      else
+        spmv_launch<T>(be, A, src, 0, 1, EpiGmVStore<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done,
+                       hyb);
       if (k > 0)
         cgs_pass<T>(be, n, (int)k, V, ld, vk, GmDots<T>{g, (int)k}, GmOrthEnd<T>{g},
                     static_cast<T *>(red.partials), red.counter);
