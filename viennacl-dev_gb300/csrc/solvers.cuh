@@ -706,18 +706,22 @@ struct EpiGmVStore {
 };
 
 template <typename T>
-struct EpiGmV {  // v_k = A src, ||v_k||^2 (used for k = 0)
-  static constexpr int NDOT = 1;
-  T *vk; Gm<T> *g;
+struct EpiGmV {  // v_0 = A r with ||v_0||^2 and <r, v_0> (k = 0): R(0,0), xi_0
+  static constexpr int NDOT = 2;
+  T *vk; const T *r; Gm<T> *g;
   VCLGB_NO_PRE
   __device__ bool skip() const { return g->done != kRunning; }
-  __device__ void row(uint32_t i, T acc, const Pre &, T (&d)[1]) const {
+  __device__ void row(uint32_t i, T acc, const Pre &, T (&d)[2]) const {
     vk[i] = acc;
     d[0] += acc * acc;
+    d[1] += r[i] * acc;
   }
-  __device__ void finalize(const T (&s)[1]) const {
+  __device__ void finalize(const T (&s)[2]) const {
+    const T inv = T(1) / sqrt(s[0]);
     g->vnorm2 = s[0];
-    g->inv_vnorm = T(1) / sqrt(s[0]);
+    g->inv_vnorm = inv;
+    g->R[0] = sqrt(s[0]);
+    g->xi[0] = s[1] * inv;
   }
 };
 
@@ -820,10 +824,11 @@ __device__ __forceinline__ T cgs_sub_cols(T v, const T *__restrict__ Q, size_t l
   return v;
 }
 
-template <typename T, int TAIL>
-__device__ __forceinline__ T cgs_orth_rows(size_t n, int full, const T *__restrict__ Q, size_t ld,
-                                           T *__restrict__ w, const T *hs) {
-  T d = T(0);
+// d[0] += ||w||^2 and, for ND == 2, d[1] += <r, w> (w after the update)
+template <typename T, int TAIL, int ND>
+__device__ __forceinline__ void cgs_orth_rows(size_t n, int full, const T *__restrict__ Q,
+                                              size_t ld, T *__restrict__ w, const T *hs,
+                                              const T *__restrict__ r, T (&d)[ND]) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     T v = w[i];
@@ -831,36 +836,41 @@ __device__ __forceinline__ T cgs_orth_rows(size_t n, int full, const T *__restri
       v = cgs_sub_cols<T, kCgsCols>(v, Q + (size_t)c * kCgsCols * ld, ld, i, hs + c * kCgsCols);
     if constexpr (TAIL > 0)
       v = cgs_sub_cols<T, TAIL>(v, Q + (size_t)full * kCgsCols * ld, ld, i, hs + full * kCgsCols);
-    d += v * v;
+    d[0] += v * v;
+    if constexpr (ND == 2) d[1] += r[i] * v;
     w[i] = v;
   }
-  return d;
 }
 
-// Fin: skip(), h(j) (the projections), finalize(||w||^2)
+// Fin: NDOT (1: ||w||^2; 2: also <r, w> with r = dot_with()), skip(), h(j)
+// (the projections), finalize(sums)
 template <typename T, class Fin>
 __global__ void __launch_bounds__(256)
     cgs_orth_kernel(size_t n, int k, const T *__restrict__ Q, size_t ld, T *__restrict__ w, Fin fin,
                     T *partials, unsigned *counter) {
+  constexpr int ND = Fin::NDOT;
   if (fin.skip()) return;
   __shared__ T hs[kGmresMaxK];
-  __shared__ T smem[256];  // block_sum_wide over 256 threads
+  __shared__ T smem[ND * 256];  // block_sum_wide over 256 threads
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = fin.h(j);
   __syncthreads();
   const int full = k / kCgsCols;
-  T d[1];
+  const T *r = fin.dot_with();
+  T d[ND];
+#pragma unroll
+  for (int i = 0; i < ND; ++i) d[i] = T(0);
   switch (k % kCgsCols) {
-    case 0: d[0] = cgs_orth_rows<T, 0>(n, full, Q, ld, w, hs); break;
-    case 1: d[0] = cgs_orth_rows<T, 1>(n, full, Q, ld, w, hs); break;
-    case 2: d[0] = cgs_orth_rows<T, 2>(n, full, Q, ld, w, hs); break;
-    case 3: d[0] = cgs_orth_rows<T, 3>(n, full, Q, ld, w, hs); break;
-    case 4: d[0] = cgs_orth_rows<T, 4>(n, full, Q, ld, w, hs); break;
-    case 5: d[0] = cgs_orth_rows<T, 5>(n, full, Q, ld, w, hs); break;
-    case 6: d[0] = cgs_orth_rows<T, 6>(n, full, Q, ld, w, hs); break;
-    default: d[0] = cgs_orth_rows<T, 7>(n, full, Q, ld, w, hs); break;
+    case 0: cgs_orth_rows<T, 0, ND>(n, full, Q, ld, w, hs, r, d); break;
+    case 1: cgs_orth_rows<T, 1, ND>(n, full, Q, ld, w, hs, r, d); break;
+    case 2: cgs_orth_rows<T, 2, ND>(n, full, Q, ld, w, hs, r, d); break;
+    case 3: cgs_orth_rows<T, 3, ND>(n, full, Q, ld, w, hs, r, d); break;
+    case 4: cgs_orth_rows<T, 4, ND>(n, full, Q, ld, w, hs, r, d); break;
+    case 5: cgs_orth_rows<T, 5, ND>(n, full, Q, ld, w, hs, r, d); break;
+    case 6: cgs_orth_rows<T, 6, ND>(n, full, Q, ld, w, hs, r, d); break;
+    default: cgs_orth_rows<T, 7, ND>(n, full, Q, ld, w, hs, r, d); break;
   }
-  T s[1];
-  if (grid_reduce<1, true>(d, partials, counter, smem, s)) fin.finalize(s[0]);
+  T s[ND];
+  if (grid_reduce<ND, true>(d, partials, counter, smem, s)) fin.finalize(s);
 }
 
 // One Gram-Schmidt pass (multi-dot, then update) of w against Q's first k
@@ -890,33 +900,35 @@ struct GmDots {
     g->R[j + (size_t)k * g->K] = t;
   }
 };
+// ||w||^2 and <r, w> of the orthogonalised w give R(k,k) = ||w|| and
+// xi_k = <r, w> / ||w|| = <r, v_k> without a reduction over the normalised v_k
 template <typename T>
 struct GmOrthEnd {
-  Gm<T> *g;
+  static constexpr int NDOT = 2;
+  Gm<T> *g; const T *r; int k;
   __device__ bool skip() const { return g->done != kRunning; }
   __device__ T h(int j) const { return g->h[j]; }
-  __device__ void finalize(T s) const {
-    g->vnorm2 = s;
-    g->inv_vnorm = T(1) / sqrt(s);
+  __device__ const T *dot_with() const { return r; }
+  __device__ void finalize(const T (&s)[2]) const {
+    const T inv = T(1) / sqrt(s[0]);
+    g->vnorm2 = s[0];
+    g->inv_vnorm = inv;
+    g->R[k + (size_t)k * g->K] = sqrt(s[0]);
+    g->xi[k] = s[1] * inv;
   }
 };
 
 template <typename T>
-struct GmNormalize {  // R(k,k) = ||v_k||; v_k /= ||v_k||; xi_k = <r, v_k>
-  static constexpr int NDOT = 1;
-  T *vk; const T *r; Gm<T> *g; int k;
+struct GmNormalize {  // v_k /= ||v_k|| (R(k,k) and xi_k came with ||v_k||)
+  static constexpr int NDOT = 0;
+  T *vk; Gm<T> *g;
   struct S { T nv; };
   __device__ bool skip() const { return g->done != kRunning; }
   __device__ S load() const { return {g->inv_vnorm}; }
-  __device__ void apply(size_t i, S c, T (&d)[1]) const {
-    T v = vk[i] * c.nv;  // times 1/||v_k||, formed once by the kernel before
-    d[0] += r[i] * v;
-    vk[i] = v;
+  __device__ void apply(size_t i, S c, T (&)[1]) const {
+    vk[i] *= c.nv;  // times 1/||v_k||, formed once by the kernel before
   }
-  __device__ void finalize(const T (&s)[1]) const {
-    g->xi[k] = s[0];
-    g->R[k + (size_t)k * g->K] = sqrt(g->vnorm2);
-  }
+  __device__ void finalize(const T (&)[1]) const {}
 };
 
 // the host part of a restart cycle (gmres.hpp:287-345) as one device thread
@@ -1142,10 +1154,13 @@ struct GhDots {
 };
 template <typename T, bool SECOND>
 struct GhOrthEnd {
+  static constexpr int NDOT = 1;
   Gh<T> *g;
   __device__ bool skip() const { return SECOND ? g->reorth_skip : g->step_skip; }
   __device__ T h(int j) const { return g->h[j]; }
-  __device__ void finalize(T s) const {
+  __device__ const T *dot_with() const { return nullptr; }
+  __device__ void finalize(const T (&sums)[1]) const {
+    const T s = sums[0];
     g->vnorm2 = s;
     g->inv_vnorm = T(1) / sqrt(s);
     if (!SECOND) g->reorth_skip = !(s < T(0.5) * g->wnorm2);
@@ -2455,14 +2470,15 @@ static void gmres_pipelined_solve(Backend &be, Matrix &A, const T *b, T *x, vclg
       T *vk = V + (size_t)k * ld;
       const T *src = k == 0 ? r : V + (size_t)(k - 1) * ld;
       if (k == 0)
-        spmv_launch<T>(be, A, src, 0, 1, EpiGmV<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done, hyb);
+        spmv_launch<T>(be, A, src, 0, 1, EpiGmV<T>{vk, r, g}, red, vk, 0, 1, T(1), T(0), done,
+                       hyb);
       else
         spmv_launch<T>(be, A, src, 0, 1, EpiGmVStore<T>{vk, g}, red, vk, 0, 1, T(1), T(0), done,
                        hyb);
       if (k > 0)
-        cgs_pass<T>(be, n, (int)k, V, ld, vk, GmDots<T>{g, (int)k}, GmOrthEnd<T>{g},
+        cgs_pass<T>(be, n, (int)k, V, ld, vk, GmDots<T>{g, (int)k}, GmOrthEnd<T>{g, r, (int)k},
                     static_cast<T *>(red.partials), red.counter);
-      vec_pass<T>(be, n, GmNormalize<T>{vk, r, g, (int)k}, red);
+      vec_pass<T>(be, n, GmNormalize<T>{vk, g}, red);
     }
     scalar_step(be, GmCycleEnd<T>{g});
     vec_pass<T>(be, n, GmUpdateX<T>{x, r, V, ld, g}, red);
