@@ -1001,7 +1001,7 @@ struct Gh {  // device state of the preconditioned GMRES
   T h[kGmresMaxK];
   T coef[kGmresMaxK];
   int kk;                        // steps taken in the current cycle
-  int lost;                      // the cycle ended at the clamp of xi (see GhNormalize)
+  int lost;                      // the cycle ended at the clamp of xi (see gh_step)
   int upd;                       // coefficients pending for the x update
   int pending;                   // status to take after the update (0: keep running)
   unsigned restart_count, max_restarts;
@@ -1010,6 +1010,7 @@ struct Gh {  // device state of the preconditioned GMRES
   int done;
   int step_skip;                 // done || the cycle stopped
   int reorth_skip;               // step_skip || no second Gram-Schmidt pass needed
+  int step_at;                   // the step whose stopping test ran last (-1: none)
 };
 
 template <typename T>
@@ -1033,6 +1034,7 @@ struct GhInit {  // x = 0; ||b||
     g->done = ((double)g->nrhs <= g->abs_tol) ? kConverged : kRunning;
     g->step_skip = 1;
     g->reorth_skip = 1;
+    g->step_at = -1;
   }
 };
 
@@ -1041,6 +1043,7 @@ struct GhInit {  // x = 0; ||b||
 template <typename T>
 __device__ __forceinline__ void gh_cycle_start(Gh<T> *g, T rr) {
   const T rho0 = sqrt(rr);
+  g->step_at = -1;
   g->rho0 = rho0;
   if ((double)(rho0 / g->nrhs) < g->tol || (double)rho0 < g->abs_tol) {
     g->error = (double)(rho0 / g->nrhs);
@@ -1056,6 +1059,52 @@ __device__ __forceinline__ void gh_cycle_start(Gh<T> *g, T rr) {
   g->step_skip = 0;
   g->reorth_skip = 1;
   if (!finite_(rho0)) { g->done = kBreakdown; g->step_skip = 1; }
+}
+
+// A step's stopping test (gmres.hpp:570-590), run by the reduction that gives
+// the step's final ||w||^2 together with <r, w>: R(k,k) = ||w||, xi_k =
+// <r, w> / ||w|| = <r, q_k>, the clamp of xi and the tolerance test.  step_at
+// records the step, so that its normalisation still writes q_k when the test
+// ends the cycle there.
+template <typename T>
+__device__ __forceinline__ void gh_step(Gh<T> *g, int k, T ww, T rw) {
+  const T nv = sqrt(ww);
+  if (!(nv > T(0)) || !finite_(nv)) {
+    // w lies in the span of the basis (or is not finite): the cycle ends
+    // with the k steps before this one
+    g->step_skip = 1;
+    g->reorth_skip = 1;
+    if (!finite_(nv)) g->pending = kBreakdown;
+    return;
+  }
+  g->step_at = k;
+  g->R[(size_t)k * g->K + k] = nv;
+  T xi = rw * g->inv_vnorm;
+  const T rho = g->rho;
+  // |xi| <= rho holds in exact arithmetic; the reference clamps xi to +-rho
+  // ("machine precision reached", gmres.hpp:575-578), which makes rho 0 and
+  // stops the solve as converged.  The estimate rho = sqrt(1 - sum xi^2) of
+  // a residual normalised by its computed norm cannot resolve rho much below
+  // sqrt(n eps), so the clamp can fire while the true residual is far above
+  // the tolerance (seen: Jacobi GMRES on a 4M-row matrix whose M^-1 b is 467
+  // times ||b||, true residual 3.6e-3 at "convergence").  Here the cycle ends
+  // at the clamp without declaring convergence, and the next cycle's
+  // residual r = M^-1 (b - A x), computed from x, decides.
+  const bool clamped = xi >= rho || xi <= -rho;
+  if (xi > rho) xi = rho;
+  if (xi < -rho) xi = -rho;
+  g->proj[k] = xi;
+  const T nr = rho * sin(acos(xi / rho));
+  g->rho = nr;
+  g->kk = k + 1;
+  if (clamped) {
+    g->lost = 1;
+    g->step_skip = 1;
+    g->reorth_skip = 1;
+  } else if (fabs((double)(nr * g->rho0 / g->nrhs)) < g->tol) {  // gmres.hpp:583-588
+    g->step_skip = 1;
+    g->reorth_skip = 1;
+  }
 }
 
 template <typename T, bool JAC>
@@ -1108,34 +1157,49 @@ __device__ __forceinline__ void gh_w_done(Gh<T> *g, T ww) {
   g->inv_vnorm = T(1) / sqrt(ww);
 }
 
-template <typename T, bool JAC>
-struct EpiGhW {  // w = M^-1 A q (Jacobi fused) with ||w||^2; else raw A q
-  static constexpr int NDOT = 1;
+// w = M^-1 A q with Jacobi fused: ||w||^2 and, at step 0 (RDOT, no
+// Gram-Schmidt pass follows), <r, w> and the step's test; else the raw A q
+template <typename T, bool JAC, bool RDOT>
+struct EpiGhW {
+  static constexpr int NDOT = JAC ? (RDOT ? 2 : 1) : 0;
   static constexpr bool jacobi = JAC;
-  T *w; const T *inv_d; Gh<T> *g;
-  struct Pre { T id; };
+  T *w; const T *inv_d, *r; Gh<T> *g;
+  struct Pre { T id, r; };
   __device__ bool skip() const { return g->step_skip != 0; }
-  __device__ Pre pre(uint32_t i) const { return {jacobi ? inv_d[i] : T(1)}; }
-  __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
-    if (jacobi) {
+  __device__ Pre pre(uint32_t i) const {
+    return {jacobi ? inv_d[i] : T(1), (JAC && RDOT) ? r[i] : T(0)};
+  }
+  __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[DotArr<NDOT>::n]) const {
+    if constexpr (JAC) {
       acc = acc * pv.id;
       d[0] += acc * acc;
+      if constexpr (RDOT) d[1] += pv.r * acc;
     }
     w[i] = acc;
   }
-  __device__ void finalize(const T (&s)[1]) const {
-    if (jacobi) gh_w_done(g, s[0]);
+  __device__ void finalize(const T (&s)[DotArr<NDOT>::n]) const {
+    if constexpr (JAC) {
+      gh_w_done(g, s[0]);
+      if constexpr (RDOT) gh_step(g, 0, s[0], s[1]);
+    }
   }
 };
 
-template <typename T>
-struct GhWNorm {  // generic preconditioner: ||w||^2 after w = M^-1 A q
-  static constexpr int NDOT = 1;
-  const T *w; Gh<T> *g;
+template <typename T, bool RDOT>
+struct GhWNorm {  // generic preconditioner: ||w||^2 (and at step 0 <r, w>) after w = M^-1 A q
+  static constexpr int NDOT = RDOT ? 2 : 1;
+  const T *w, *r; Gh<T> *g;
   __device__ bool skip() const { return g->step_skip != 0; }
   __device__ NoScal load() const { return {}; }
-  __device__ void apply(size_t i, NoScal, T (&d)[1]) const { const T v = w[i]; d[0] += v * v; }
-  __device__ void finalize(const T (&s)[1]) const { gh_w_done(g, s[0]); }
+  __device__ void apply(size_t i, NoScal, T (&d)[NDOT]) const {
+    const T v = w[i];
+    d[0] += v * v;
+    if constexpr (RDOT) d[1] += r[i] * v;
+  }
+  __device__ void finalize(const T (&s)[NDOT]) const {
+    gh_w_done(g, s[0]);
+    if constexpr (RDOT) gh_step(g, 0, s[0], s[1]);
+  }
 };
 
 // Gram-Schmidt for the preconditioned form.  SECOND: the re-orthogonalisation
@@ -1152,72 +1216,35 @@ struct GhDots {
     else g->R[(size_t)k * g->K + j] = t;
   }
 };
+// the pass that leaves no second pass to run ends the step: its reduction
+// carries <r, w> for the step's test
 template <typename T, bool SECOND>
 struct GhOrthEnd {
-  static constexpr int NDOT = 1;
-  Gh<T> *g;
+  static constexpr int NDOT = 2;
+  Gh<T> *g; const T *r; int k;
   __device__ bool skip() const { return SECOND ? g->reorth_skip : g->step_skip; }
   __device__ T h(int j) const { return g->h[j]; }
-  __device__ const T *dot_with() const { return nullptr; }
-  __device__ void finalize(const T (&sums)[1]) const {
-    const T s = sums[0];
-    g->vnorm2 = s;
-    g->inv_vnorm = T(1) / sqrt(s);
-    if (!SECOND) g->reorth_skip = !(s < T(0.5) * g->wnorm2);
+  __device__ const T *dot_with() const { return r; }
+  __device__ void finalize(const T (&s)[2]) const {
+    g->vnorm2 = s[0];
+    g->inv_vnorm = T(1) / sqrt(s[0]);
+    if (!SECOND) g->reorth_skip = !(s[0] < T(0.5) * g->wnorm2);
     else g->reorth_skip = 1;
+    if (g->reorth_skip) gh_step(g, k, s[0], s[1]);
   }
 };
 
+// q_k = w / ||w||.  Skipped when the cycle stopped before this step; the step
+// whose test stopped it (step_at) still writes its q_k, which the update uses.
 template <typename T>
-struct GhNormalize {  // q_k = w / ||w||, xi_k = <r, q_k>; the step's stopping test
-  static constexpr int NDOT = 1;
-  T *q; const T *w, *r; Gh<T> *g; int k;
+struct GhNormalize {
+  static constexpr int NDOT = 0;
+  T *q; const T *w; Gh<T> *g; int k;
   struct S { T inv; };
-  __device__ bool skip() const { return g->step_skip != 0; }
+  __device__ bool skip() const { return g->step_skip != 0 && g->step_at != k; }
   __device__ S load() const { return {g->inv_vnorm}; }
-  __device__ void apply(size_t i, S c, T (&d)[1]) const {
-    const T v = w[i] * c.inv;
-    d[0] += r[i] * v;
-    q[i] = v;
-  }
-  __device__ void finalize(const T (&s)[1]) const {
-    const T nv = sqrt(g->vnorm2);
-    if (!(nv > T(0)) || !finite_(nv)) {
-      // w lies in the span of the basis (or is not finite): the cycle ends
-      // with the k steps before this one
-      g->step_skip = 1;
-      g->reorth_skip = 1;
-      if (!finite_(nv)) g->pending = kBreakdown;
-      return;
-    }
-    g->R[(size_t)k * g->K + k] = nv;
-    T xi = s[0];
-    const T rho = g->rho;
-    // |xi| <= rho holds in exact arithmetic; the reference clamps xi to +-rho
-    // ("machine precision reached", gmres.hpp:575-578), which makes rho 0 and
-    // stops the solve as converged.  The estimate rho = sqrt(1 - sum xi^2) of
-    // a residual normalised by its computed norm cannot resolve rho much below
-    // sqrt(n eps), so the clamp can fire while the true residual is far above
-    // the tolerance (seen: Jacobi GMRES on a 4M-row matrix whose M^-1 b is 467
-    // times ||b||, true residual 3.6e-3 at "convergence").  Here the cycle ends
-    // at the clamp without declaring convergence, and the next cycle's
-    // residual r = M^-1 (b - A x), computed from x, decides.
-    const bool clamped = xi >= rho || xi <= -rho;
-    if (xi > rho) xi = rho;
-    if (xi < -rho) xi = -rho;
-    g->proj[k] = xi;
-    const T nr = rho * sin(acos(xi / rho));
-    g->rho = nr;
-    g->kk = k + 1;
-    if (clamped) {
-      g->lost = 1;
-      g->step_skip = 1;
-      g->reorth_skip = 1;
-    } else if (fabs((double)(nr * g->rho0 / g->nrhs)) < g->tol) {  // gmres.hpp:583-588
-      g->step_skip = 1;
-      g->reorth_skip = 1;
-    }
-  }
+  __device__ void apply(size_t i, S c, T (&)[1]) const { q[i] = w[i] * c.inv; }
+  __device__ void finalize(const T (&)[1]) const {}
 };
 
 // end of a cycle (gmres.hpp:593-625) as one device thread: triangular solve,
@@ -1268,6 +1295,7 @@ struct GhCycleClose {  // after the update: take the pending status
   Gh<T> *g;
   __device__ void operator()() const {
     g->upd = 0;
+    g->step_at = -1;
     if (g->done == kRunning && g->pending != 0) {
       g->done = g->pending;
       g->step_skip = 1;
@@ -2548,22 +2576,28 @@ static void gmres_precond_solve(Backend &be, Matrix &A, const T *b, T *x, vclgbS
     vec_pass<T>(be, n, GhScaleR<T>{r, g}, red);
     for (uint32_t k = 0; k < K; ++k) {
       const T *src = k == 0 ? r : Q + (size_t)(k - 1) * ld;
-      if (jac) {
-        spmv_launch<T>(be, A, src, 0, 1, EpiGhW<T, true>{w, inv_d, g}, red, w, 0, 1, T(1), T(0),
-                       sskip, hyb);
+      // the step's test runs in the last reduction over w: the product's (or
+      // the norm pass's) at k = 0, the last Gram-Schmidt pass's after
+      if (jac && k == 0) {
+        spmv_launch<T>(be, A, src, 0, 1, EpiGhW<T, true, true>{w, inv_d, r, g}, red, w, 0, 1,
+                       T(1), T(0), sskip, hyb);
+      } else if (jac) {
+        spmv_launch<T>(be, A, src, 0, 1, EpiGhW<T, true, false>{w, inv_d, r, g}, red, w, 0, 1,
+                       T(1), T(0), sskip, hyb);
       } else {
-        spmv_launch<T>(be, A, src, 0, 1, EpiGhW<T, false>{w, inv_d, g}, red, w, 0, 1, T(1),
-                       T(0), sskip, hyb);
+        spmv_launch<T>(be, A, src, 0, 1, EpiGhW<T, false, false>{w, inv_d, r, g}, red, w, 0, 1,
+                       T(1), T(0), sskip, hyb);
         precond_apply(be, *P, w, sskip);
-        vec_pass<T>(be, n, GhWNorm<T>{w, g}, red);
+        if (k == 0) vec_pass<T>(be, n, GhWNorm<T, true>{w, r, g}, red);
+        else vec_pass<T>(be, n, GhWNorm<T, false>{w, r, g}, red);
       }
       if (k > 0) {
-        cgs_pass<T>(be, n, (int)k, Q, ld, w, GhDots<T, false>{g, (int)k}, GhOrthEnd<T, false>{g},
-                    part, red.counter);
-        cgs_pass<T>(be, n, (int)k, Q, ld, w, GhDots<T, true>{g, (int)k}, GhOrthEnd<T, true>{g},
-                    part, red.counter);
+        cgs_pass<T>(be, n, (int)k, Q, ld, w, GhDots<T, false>{g, (int)k},
+                    GhOrthEnd<T, false>{g, r, (int)k}, part, red.counter);
+        cgs_pass<T>(be, n, (int)k, Q, ld, w, GhDots<T, true>{g, (int)k},
+                    GhOrthEnd<T, true>{g, r, (int)k}, part, red.counter);
       }
-      vec_pass<T>(be, n, GhNormalize<T>{Q + (size_t)k * ld, w, r, g, (int)k}, red);
+      vec_pass<T>(be, n, GhNormalize<T>{Q + (size_t)k * ld, w, g, (int)k}, red);
     }
     scalar_step(be, GhCycleEnd<T>{g});
     vec_pass<T>(be, n, GhUpdateX<T>{x, r, Q, ld, g}, red);
