@@ -64,21 +64,25 @@ def test_gmres_against_oracle_and_reference(V, golden):
     assert oracle.rel_residual(d["rp"], d["ci"], d["v"], x, d["b"]) < 2e-10
 
 
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
 @pytest.mark.parametrize("kd", [1, 7, 45, 64])
-def test_gmres_per_phase_krylov_dims(V, kd):
-    # 40,000 rows, above the cluster launch's limit: the per-phase GMRES at
-    # Krylov dimensions from 1 (R(0,0) and xi_0 come from the first product's
-    # epilogue alone) to the largest, 64.  Dimension 1 stalls: capped at 60
-    # iterations, its status, count, error estimate and x follow the oracle's.
+def test_gmres_per_phase_krylov_dims(V, kd, pc):
+    # 40,000 rows, above the cluster launch's limit: the per-phase GMRES and the
+    # preconditioned (Householder-variant) GMRES at Krylov dimensions from 1
+    # (R(0,0), xi_0 and the step's test come from the first product's epilogue
+    # alone) to the largest, 64.  Dimension 1 stalls: capped at 60 iterations,
+    # its status, count, error estimate and x follow the oracle's.
     import torch
     rp, ci, v = gen.convdiff2d(200, 200, peclet=5.0, shift=0.05)
     n = len(rp) - 1
     b = gen.rhs_uniform(n, 18)
     A = V.compressed_matrix(rp, ci, v)
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
     cap = 60 if kd == 1 else 3000
     tag = V.gmres_tag(1e-10, cap, kd)
-    x = _np(V.solve(A, torch.tensor(b, device="cuda"), tag))
-    xo, it_o, err_o = oracle.solve("gmres", rp, ci, v, b, 1e-10, cap, krylov_dim=kd)
+    bd = torch.tensor(b, device="cuda")
+    x = _np(V.solve(A, bd, tag, P) if P else V.solve(A, bd, tag))
+    xo, it_o, err_o = oracle.solve("gmres", rp, ci, v, b, 1e-10, cap, pc, krylov_dim=kd)
     if kd == 1:
         assert tag.status() == V.NOT_CONVERGED
         assert tag.iters() == it_o == cap
@@ -88,7 +92,8 @@ def test_gmres_per_phase_krylov_dims(V, kd):
     assert tag.status() == V.SUCCESS
     assert iters_close(tag.iters(), it_o, 0.05), (tag.iters(), it_o)
     assert rel_err(x, xo) < 1e-7
-    assert oracle.rel_residual(rp, ci, v, x, b) < 2e-10
+    # the Jacobi form stops on the preconditioned residual (4e-10 true here)
+    assert oracle.rel_residual(rp, ci, v, x, b) < (2e-10 if pc == "none" else 1e-9)
 
 
 @pytest.mark.parametrize("pc", ["jacobi", "ilu0", "row1", "cpilu"])
