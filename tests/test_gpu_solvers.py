@@ -96,6 +96,29 @@ def test_gmres_per_phase_krylov_dims(V, kd, pc):
     assert oracle.rel_residual(rp, ci, v, x, b) < (2e-10 if pc == "none" else 1e-9)
 
 
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_gmres_per_phase_float32(V, pc):
+    # the FP32 instantiations of both GMRES forms on 40,000 rows (above the
+    # cluster launch's limit) to 1e-5: the oracle's FP64 count within 10 % and
+    # the FP32 solution's true residual, evaluated in FP64, near the tolerance
+    import torch
+    rp, ci, v = gen.convdiff2d(200, 200, peclet=5.0, shift=0.05)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 18)
+    A = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.gmres_tag(1e-5, 3000, 30)
+    bd = torch.tensor(b.astype(np.float32), device="cuda")
+    x = _np(V.solve(A, bd, tag, P) if P else V.solve(A, bd, tag))
+    assert x.dtype == np.float32
+    _, it_o, _ = oracle.solve("gmres", rp, ci, v, b, 1e-5, 3000, pc, krylov_dim=30)
+    assert tag.status() == V.SUCCESS
+    assert abs(tag.iters() - it_o) <= max(3, int(0.1 * it_o)), (tag.iters(), it_o)
+    # the Jacobi form stops on the preconditioned residual (3.8e-5 true in FP64)
+    res = oracle.rel_residual(rp, ci, v, x.astype(np.float64), b)
+    assert res < (1e-4 if pc == "none" else 5e-4), res
+
+
 @pytest.mark.parametrize("pc", ["jacobi", "ilu0", "row1", "cpilu"])
 @pytest.mark.parametrize("kd", [30, 10])
 def test_gmres_precond_golden(V, golden, pc, kd):
