@@ -119,6 +119,29 @@ def test_gmres_per_phase_float32(V, pc):
     assert res < (1e-4 if pc == "none" else 5e-4), res
 
 
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+def test_bicgstab_per_phase_float32(V, pc):
+    # the FP32 instantiation of the per-phase BiCGStab (40,000 rows, above the
+    # cluster launch's limit) to 1e-5.  BiCGStab's count follows rounding (the
+    # oracle's threaded dot products gave 47 and 49 on this input), so the
+    # oracle is a sanity band; the true residual, in FP64, is the check.
+    import torch
+    rp, ci, v = gen.convdiff2d(200, 200, peclet=5.0, shift=0.05)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 18)
+    A = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    P = V.jacobi_precond(A) if pc == "jacobi" else None
+    tag = V.bicgstab_tag(1e-5, 3000)
+    bd = torch.tensor(b.astype(np.float32), device="cuda")
+    x = _np(V.solve(A, bd, tag, P) if P else V.solve(A, bd, tag))
+    assert x.dtype == np.float32
+    _, it_o, _ = oracle.solve("bicgstab", rp, ci, v, b, 1e-5, 3000, pc)
+    assert tag.status() == V.SUCCESS
+    assert abs(tag.iters() - it_o) <= 0.35 * it_o, (tag.iters(), it_o)
+    res = oracle.rel_residual(rp, ci, v, x.astype(np.float64), b)
+    assert res < 5e-4, res
+
+
 @pytest.mark.parametrize("pc", ["jacobi", "ilu0", "row1", "cpilu"])
 @pytest.mark.parametrize("kd", [30, 10])
 def test_gmres_precond_golden(V, golden, pc, kd):
