@@ -118,6 +118,35 @@ def test_bicgstab_with_window(V, pc):
     assert abs(tag.iters() - it_ref) <= 0.35 * it_ref, (tag.iters(), it_ref)
 
 
+def test_float32_cg_with_window(V):
+    # FP32 pipelined CG on the 160^3 Laplacian (4,096,000 rows: the four
+    # iteration vectors, 65.5 MB, in the set-aside) to 1e-6: repeats bit for
+    # bit, the set-aside is put back, the oracle's FP64 count within 10 % and
+    # the FP32 solution's true residual, in FP64, near the tolerance
+    import oracle
+    import torch
+    rt = _runtime()
+    before = _persisting_limit(rt)
+    rp, ci, v = gen.laplace3d(160)
+    n = len(rp) - 1
+    b = gen.rhs_uniform(n, 1)
+    A = V.compressed_matrix(rp, ci, v.astype(np.float32))
+    bd = torch.tensor(b.astype(np.float32), device="cuda")
+    xs, its = [], []
+    for _ in range(2):
+        tag = V.cg_tag(1e-6, 3000)
+        xs.append(V.solve(A, bd, tag).cpu().numpy())
+        assert tag.status() == V.SUCCESS
+        its.append(tag.iters())
+    assert xs[0].dtype == np.float32
+    assert its[0] == its[1] and np.array_equal(xs[0], xs[1])
+    assert _persisting_limit(rt) == before
+    _, it_ref, _ = oracle.solve("cg", rp, ci, v, b, 1e-6, 3000)
+    assert abs(its[0] - it_ref) <= 0.1 * it_ref, (its[0], it_ref)
+    res = oracle.rel_residual(rp, ci, v, xs[0].astype(np.float64), b)
+    assert res < 1e-5, res
+
+
 def test_refined_solve_with_window_reaches_fp64_residual(V):
     # 192^3 variable-coefficient diffusion: the FP32 inner Jacobi-PCG on the DIA
     # copy keeps its vectors in the window; the FP64 refinement reaches 1e-10
