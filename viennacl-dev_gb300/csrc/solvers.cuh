@@ -1109,7 +1109,7 @@ __device__ __forceinline__ void gh_step(Gh<T> *g, int k, T ww, T rw) {
 
 template <typename T, bool JAC>
 struct EpiGhResid {  // r = M^-1 (b - A x): Jacobi fused with ||r||^2, else raw b - A x
-  static constexpr int NDOT = 1;
+  static constexpr int NDOT = JAC ? 1 : 0;
   static constexpr bool jacobi = JAC;
   T *r; const T *b, *inv_d; Gh<T> *g;
   struct Pre { T b, id; };
@@ -1117,14 +1117,14 @@ struct EpiGhResid {  // r = M^-1 (b - A x): Jacobi fused with ||r||^2, else raw 
   __device__ Pre pre(uint32_t i) const { return {b[i], jacobi ? inv_d[i] : T(1)}; }
   __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
     T v = pv.b - acc;
-    if (jacobi) {
+    if constexpr (JAC) {
       v = v * pv.id;
       d[0] += v * v;
     }
     r[i] = v;
   }
   __device__ void finalize(const T (&s)[1]) const {
-    if (jacobi) gh_cycle_start(g, s[0]);
+    if constexpr (JAC) gh_cycle_start(g, s[0]);
   }
 };
 
