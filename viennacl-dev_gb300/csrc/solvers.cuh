@@ -229,7 +229,7 @@ __device__ __forceinline__ void pcg_check(St<T> *st, T new_ip) {
 // PcgP's reads of r and d).
 template <typename T, bool JAC>
 struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (generic)
-  static constexpr int NDOT = 1;
+  static constexpr int NDOT = JAC ? 1 : 0;
   static constexpr bool jacobi = JAC;
   T *x, *r, *z; const T *p, *tmp, *dg; St<T> *st;
   struct S { T a; };
@@ -240,7 +240,7 @@ struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (ge
     x[i] += s.a * vp;
     T vr = r[i] - s.a * tmp[i];
     r[i] = vr;
-    if (jacobi) {
+    if constexpr (JAC) {
       const T zi = vr * dg[i];
       z[i] = zi;
       d[0] += vr * zi;
@@ -249,7 +249,7 @@ struct PcgUpdate {  // x += a p; r -= a tmp; z = r/d, <r,z> (Jacobi) / z = r (ge
     }
   }
   __device__ void finalize(const T (&s)[1]) const {
-    if (jacobi) pcg_check(st, s[0]);
+    if constexpr (JAC) pcg_check(st, s[0]);
   }
 };
 
@@ -424,7 +424,7 @@ __device__ __forceinline__ void gb_restart_done(St<T> *st, T rr) {
 
 template <typename T, bool JAC>
 struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0* = r; ||r||^2
-  static constexpr int NDOT = 1;
+  static constexpr int NDOT = JAC ? 1 : 0;
   static constexpr bool jacobi = JAC;
   T *r, *p, *r0; const T *b, *dg; St<T> *st;
   struct Pre { T b, d; };
@@ -432,7 +432,7 @@ struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0
   __device__ Pre pre(uint32_t i) const { return {b[i], jacobi ? dg[i] : T(1)}; }
   __device__ void row(uint32_t i, T acc, const Pre &pv, T (&d)[1]) const {
     T v = pv.b - acc;
-    if (jacobi) {
+    if constexpr (JAC) {
       v = v * pv.d;
       p[i] = v;
       r0[i] = v;
@@ -441,7 +441,7 @@ struct EpiGbRestart {  // r = M^-1 (b - A x) (Jacobi fused, else raw); p = r; r0
     r[i] = v;
   }
   __device__ void finalize(const T (&s)[1]) const {
-    if (jacobi) gb_restart_done(st, s[0]);
+    if constexpr (JAC) gb_restart_done(st, s[0]);
   }
 };
 
